@@ -1,0 +1,135 @@
+/*
+  wendy_gb300.h -- C ABI of the GB300-native approximate integrator.
+
+  One shared library (wendy_gb300/_wendy_gb300.so) exposes plain-C entry
+  points with pointers and sizes only, loaded from Python through ctypes the
+  way wendy loads its own C extension (wendy/wendy.py:13-37).  Every entry
+  returns an int status (WG_OK or a negative WG_ERR_* code); nothing throws
+  across the boundary and nothing calls back into the host.
+
+  Physics and argument meaning follow the reference's approximate path:
+  masses are already multiplied by 2 pi G, `totmass` is their sum as the
+  caller computed it, `omega2` is omega^2 or a negative number for "no
+  harmonic term", and the time of a time-dependent external force lags the
+  positions and advances by dt per force evaluation
+  (wendy/wendy.c:385-418, wendy/wendy.py:363-383).
+
+  External forces are registered closed forms (WG_EXT_*) rather than host
+  callbacks: the force is evaluated inside the fused device kernel.
+*/
+#ifndef WENDY_GB300_H
+#define WENDY_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define WG_OK 0
+#define WG_ERR_ARG (-1)      /* invalid argument (sizes, non-finite or negative masses, ...) */
+#define WG_ERR_CUDA (-2)     /* a CUDA runtime call failed; see wg_last_error() */
+#define WG_ERR_NOMEM (-3)    /* device allocation failed */
+#define WG_ERR_DEVICE (-4)   /* a kernel raised its error word (e.g. a bounded wait expired) */
+#define WG_ERR_EXT (-5)      /* unknown external-force id or bad parameter count */
+#define WG_ERR_BUDGET (-6)   /* request exceeds the memory budget it was admitted under */
+#define WG_ERR_NODEV (-7)    /* no CUDA device */
+
+/* ---- registered external forces ---------------------------------------- */
+#define WG_EXT_NONE 0
+#define WG_EXT_HARMONIC 1    /* F = -p[0] x                                  (1 param)  */
+#define WG_EXT_PULSE_TANH 2  /* F = p[0] exp(-(t-p[1])^2/(2 p[2]^2)) tanh(x/p[3]) (4 params) */
+
+/* Same layout as wendy's `struct array_w_index` (wendy/wendy.h:12-16). */
+typedef struct wg_sheet {
+  int idx;
+  double val;
+} wg_sheet;
+
+typedef struct wg_sim wg_sim; /* opaque: one simulation resident on the device */
+
+typedef struct wg_stats {
+  int64_t n;                 /* sheets */
+  int64_t substeps;          /* force evaluations run so far */
+  int64_t sorts_full;        /* sub-steps that needed a full radix sort */
+  int64_t sorts_skipped;     /* sub-steps whose order was already sorted */
+  int64_t sorts_window;      /* sub-steps repaired by the bounded-window fix-up */
+  double last_max_disp;      /* largest |dx| of the last drift */
+  int64_t device_bytes;      /* device memory held by the simulation */
+  int64_t launches;          /* kernels this handle has launched */
+} wg_stats;
+
+/* Library and device information. */
+int wg_version(void);
+const char *wg_status_string(int status);
+const char *wg_last_error(void); /* detail of the last failure on this thread */
+int wg_device_info(int *sm_count, int64_t *free_bytes, int64_t *total_bytes);
+
+/* ---- the stateful path behind nbody(..., approx=True, sort='cuda') ------
+   Replaces the per-output ctypes call to _wendy_nbody_approx_onestep
+   (wendy/wendy.py:425-433, wendy/wendy.c:385-418) with a handle that keeps
+   the sheets on the device, in sorted order, between outputs. */
+
+/* Copy n sheets to the device (original order) and validate them.
+   Reference: the set-up half of _nbody_approx, wendy/wendy.py:363-387. */
+int wg_create(int64_t n, const double *x, const double *v, const double *m, double totmass,
+              double omega2, int ext_kind, const double *ext_params, int n_ext_params,
+              wg_sim **out);
+
+/* Advance by one output interval: nleap leapfrog sub-steps of dt each
+   (dt here is the reference's dt_leap = dt_output / nleap).  *t0 is updated
+   exactly as the reference does (repeated += dt, only with an external
+   force); *time_elapsed receives the device time of the call in seconds.
+   Reference: _wendy_nbody_approx_onestep, wendy/wendy.c:385-418. */
+int wg_step(wg_sim *s, double dt, int nleap, double *t0, double *time_elapsed);
+
+/* Copy positions and velocities back in original particle order.
+   Reference: the de-sort at wendy/wendy.c:413-415 and the in-place yield
+   of wendy/wendy.py:434-437. */
+int wg_download(wg_sim *s, double *x, double *v);
+
+int wg_get_stats(wg_sim *s, wg_stats *out);
+int wg_destroy(wg_sim *s);
+
+/* Average device time (seconds, CUDA events on the handle's stream) of one
+   component over `reps` back-to-back launches on the resident sheets,
+   without changing them: what = WG_PROF_FORCE (the fused force / kick /
+   drift kernel with dt = 0), WG_PROF_SORT (a full re-sort).  For the
+   measurement harness; no reference counterpart. */
+#define WG_PROF_FORCE 0
+#define WG_PROF_SORT 1
+int wg_profile(wg_sim *s, int what, int reps, double *avg_seconds);
+
+/* Page-lock (or release) caller memory so that downloads and uploads run
+   at full link speed.  No reference counterpart (wendy's buffers are plain
+   numpy arrays). */
+int wg_host_register(void *ptr, int64_t bytes);
+int wg_host_unregister(void *ptr);
+
+/* ---- stateless entry points ------------------------------------------- */
+
+/* One force evaluation at positions x (original order): accelerations in
+   original order and the sort permutation used (perm[i] = original index of
+   the sheet at sorted slot i).  Either output may be NULL.
+   Reference: _nbody_force, wendy/wendy.c:334-384. */
+int wg_accel(int64_t n, const double *x, const double *m, double totmass, double omega2,
+             int ext_kind, const double *ext_params, int n_ext_params, double t, double *a,
+             int32_t *perm);
+
+/* Drop-in shape of the reference's step function: same buffers, same
+   in/out meaning (xi updated to the new sorted order and positions, x
+   de-sorted, v updated, a = accelerations of the last force evaluation in
+   original order, *t0 advanced), with the external force given as a
+   registered id instead of a function pointer.  Every call uploads its
+   inputs and downloads its outputs.
+   Reference: _wendy_nbody_approx_onestep, wendy/wendy.c:385-418 and its
+   argtypes at wendy/wendy.py:76-93. */
+int wg_nbody_approx_onestep(int n, wg_sheet *xi, double *x, double *v, const double *m,
+                            double *a, double totmass, double dt, int nleap, double *t0,
+                            double omega2, int ext_kind, const double *ext_params,
+                            int n_ext_params, int *err, double *time_elapsed);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WENDY_GB300_H */

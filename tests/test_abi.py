@@ -1,0 +1,77 @@
+"""CPU-side checks of the C ABI library and the host logic (no GPU needed)."""
+import os
+import re
+
+import numpy
+import pytest
+
+import wendy_gb300
+from wendy_gb300 import _lib
+from wendy_gb300.extforce import Harmonic, PulseTanh, resolve
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "wendy_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(wg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_bound_symbols():
+    assert declared_symbols() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("CUDA library not built here")
+    L = _lib.load_raw()
+    for name in declared_symbols():
+        assert hasattr(L, name), name
+
+
+def test_library_reports_missing_device_cleanly():
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("CUDA library not built here")
+    import ctypes
+    L = _lib.lib()
+    sm = ctypes.c_int(0)
+    rc = L.wg_device_info(ctypes.byref(sm), None, None)
+    assert rc in (0, -7)
+    assert L.wg_status_string(-7).decode() == "no CUDA device"
+
+
+def test_nleap_error_message_matches_reference():
+    g = wendy_gb300.nbody(numpy.array([-1., 1.]), numpy.zeros(2), numpy.ones(2), 2, approx=True)
+    with pytest.raises(ValueError) as e:
+        next(g)
+    assert str(e.value) == ("When approx is True, the number of leapfrog steps nleap= per "
+                            "output time step needs to be set")
+
+
+def test_cpu_sorts_are_rejected_not_emulated():
+    g = wendy_gb300.nbody(numpy.array([-1., 1.]), numpy.zeros(2), numpy.ones(2), 2, approx=True,
+                          nleap=2, sort="quick")
+    with pytest.raises(ValueError):
+        next(g)
+
+
+def test_callables_are_rejected():
+    with pytest.raises(ValueError):
+        resolve(lambda x, t: -x)
+    assert resolve(Harmonic(1.1))[0] == _lib.EXT_HARMONIC
+    k, p = resolve(PulseTanh(0.3, 5., 1., 0.5))
+    assert k == _lib.EXT_PULSE_TANH and p == (0.3, 5., 1., 0.5)
+
+
+def test_registered_forces_evaluate_like_numpy():
+    x = numpy.linspace(-2, 2, 9)
+    f = PulseTanh(0.3, 5., 1., 0.5)
+    assert numpy.array_equal(f(x, 4.2), 0.3 * numpy.exp(-(4.2 - 5.) ** 2 / 2.) * numpy.tanh(x / .5))
+    assert numpy.array_equal(Harmonic(1.1)(x, 0.), -(1.1 ** 2.) * x)
+
+
+def test_exact_solver_is_not_offered():
+    g = wendy_gb300.nbody(numpy.array([-1., 1.]), numpy.zeros(2), numpy.ones(2), 2)
+    with pytest.raises(NotImplementedError):
+        next(g)

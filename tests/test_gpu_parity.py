@@ -1,0 +1,210 @@
+"""Parity of the CUDA path with the reference (golden vectors) and the oracle.
+
+Tolerances (FP64 throughout):
+  * sort permutation: bit-exact for distinct positions;
+  * accelerations from identical state: |a_gpu - a_ref| <= 1e-12 * S, where
+    S = max(totmass, max|a_ref|) is the acceleration scale -- the GPU forms
+    the cumulative mass exactly in 128-bit fixed point, the reference sums
+    left to right in double, so only rounding of the sum differs;
+  * positions / velocities after one output of nleap sub-steps: 1e-10
+    absolute (unit-scale systems);
+  * long runs: the maximum relative energy error matches the reference's
+    within 10 %.
+"""
+import numpy
+import pytest
+
+import wendy_gb300
+from oracle import oracle as O
+from wendy_gb300 import _lib, ics
+from wendy_gb300.extforce import Harmonic, PulseTanh
+
+pytestmark = pytest.mark.gpu
+
+PULSE = PulseTanh(0.3, 5.0, 1.0, 0.5)
+
+
+def _ext_from_par(par):
+    kind = int(par[3])
+    if kind == 0:
+        return None, None
+    if kind == O.EXT_HARMONIC:
+        f = Harmonic(1.0)
+        f.omega2 = par[4]
+        f.params = (par[4],)
+        return f, (kind, [par[4]])
+    return PulseTanh(*par[4:8]), (kind, list(par[4:8]))
+
+
+def _scale(a_ref, totmass):
+    return max(float(totmass), float(numpy.max(numpy.abs(a_ref))))
+
+
+def test_accel_matches_reference_golden(golden):
+    g = golden("accel")
+    for name in g["names"]:
+        name = str(name)
+        x, m, par = g[name + "/x"], g[name + "/m"], g[name + "/par"]
+        f, _ = _ext_from_par(par)
+        a, perm = wendy_gb300.accel(x, m, par[0], omega2=par[1], ext_force=f, t=par[2])
+        assert numpy.array_equal(perm, g[name + "/perm"]), name
+        err = numpy.max(numpy.abs(a - g[name + "/a"]))
+        assert err <= 1e-12 * _scale(g[name + "/a"], par[0]), (name, err)
+
+
+@pytest.mark.parametrize("n", [2047, 2048, 2049, 4096 * 3 + 17, 1 << 20])
+def test_accel_matches_oracle(n):
+    x, v, m = ics.sech2_disk(n, seed=n, masses="lognormal")
+    tot = numpy.sum(m)
+    a, perm = wendy_gb300.accel(x, m, tot, omega2=1.21)
+    ra, rperm = O.accel(x, m, tot, 1.21)
+    assert numpy.array_equal(perm, rperm)
+    assert numpy.max(numpy.abs(a - ra)) <= 1e-12 * _scale(ra, tot)
+
+
+def test_accel_at_large_n_equal_masses_is_exact():
+    # N = 2^24 equal masses 2^-24: every partial sum is representable, so the
+    # reference's serial sum is exact and both sides must agree bit for bit.
+    n = 1 << 24
+    x, v, m = ics.top_hat(n, seed=3)
+    tot = numpy.sum(m)
+    a, perm = wendy_gb300.accel(x, m, tot)
+    ra, rperm = O.accel(x, m, tot)
+    assert numpy.array_equal(perm, rperm)
+    assert numpy.array_equal(a, ra)
+
+
+def test_trajectories_match_reference_golden(golden):
+    g = golden("traj")
+    for name in g["names"]:
+        name = str(name)
+        x0, v0, m, par = g[name + "/x0"], g[name + "/v0"], g[name + "/m"], g[name + "/par"]
+        dt, nleap, nout, omega, t0 = par
+        keep = sorted(int(k) for k in g[name + "/keep"])
+        ext = PULSE if name == "tophat_pulse" else None
+        gen = wendy_gb300.nbody(x0, v0, m, dt, approx=True, nleap=int(nleap), t0=t0,
+                                omega=None if omega < 0 else omega, ext_force=ext)
+        for k in range(1, int(nout) + 1):
+            tx, tv = next(gen)
+            if k in keep:
+                rx, rv = g["%s/x%d" % (name, k)], g["%s/v%d" % (name, k)]
+                # one output of nleap sub-steps: 1e-10; later outputs allow the
+                # (chaotic) growth of the rounding differences by 10x per output
+                tol = 1e-10 * (10.0 ** (k - 1)) if k > 1 else 1e-10
+                tol = min(tol, 1e-6)
+                assert numpy.max(numpy.abs(tx - rx)) <= tol, (name, k)
+                assert numpy.max(numpy.abs(tv - rv)) <= tol, (name, k)
+
+
+def test_stateless_step_matches_oracle():
+    n = 1500
+    x, v, m = ics.gaussian(n, seed=21, masses="lognormal")
+    tot = numpy.sum(m)
+    outs = []
+    for which in ("gpu", "oracle"):
+        xx, vv, a = x.copy(), v.copy(), numpy.zeros(n)
+        xi = O.make_sheets(xx)
+        t0 = 4.5
+        for _ in range(3):
+            if which == "gpu":
+                t0, _el = wendy_gb300.approx_onestep(xi, xx, vv, m, a, tot, 0.002, 10, t0,
+                                                     omega2=-1., ext_force=PULSE)
+            else:
+                t0, _el = O.onestep(xi, xx, vv, m, a, tot, 0.002, 10, t0, -1.,
+                                    (O.EXT_PULSE_TANH, [0.3, 5.0, 1.0, 0.5]))
+        outs.append((xi.copy(), xx, vv, a, t0))
+    (gxi, gx, gv, ga, gt), (rxi, rx, rv, ra, rt) = outs
+    assert gt == rt
+    assert numpy.array_equal(gxi["idx"], rxi["idx"])
+    assert numpy.max(numpy.abs(gxi["val"] - rxi["val"])) <= 1e-10
+    assert numpy.max(numpy.abs(gx - rx)) <= 1e-10
+    assert numpy.max(numpy.abs(gv - rv)) <= 1e-10
+    assert numpy.max(numpy.abs(ga - ra)) <= 1e-10
+
+
+def test_energy_drift_matches_reference(golden):
+    g = golden("energy")
+    n, _, dt, nleap, nout = g["par"]
+    x, v, m = ics.sech2_disk(int(n), seed=0)
+    E0 = wendy_gb300.energy(x, v, m)
+    gen = wendy_gb300.nbody(x, v, m, dt, approx=True, nleap=int(nleap))
+    dE = numpy.empty(int(nout))
+    for k in range(int(nout)):
+        tx, tv = next(gen)
+        dE[k] = (wendy_gb300.energy(tx, tv, m) - E0) / E0
+    ref = numpy.max(numpy.abs(g["dE"]))
+    got = numpy.max(numpy.abs(dE))
+    assert abs(got - ref) <= 0.10 * ref, (got, ref)
+
+
+def test_against_exact_solver(golden):
+    # tests/test_approx.py:213-232 of the reference, against its exact solver
+    g = golden("exact")
+    gen = wendy_gb300.nbody(g["x0"], g["v0"], g["m"], 0.05, approx=True, nleap=2000)
+    for k in range(1, 21):
+        tx, tv = next(gen)
+        assert numpy.all(numpy.fabs(tx - g["x%d" % k]) < 1e-5)
+        assert numpy.all(numpy.fabs(tv - g["v%d" % k]) < 1e-5)
+
+
+def test_coincident_positions():
+    # tests/test_approx.py:234-248: two sheets meet at the first force evaluation
+    x = numpy.array([-1.1, -2. * 0.05 / 2. / 10000, 0.3 * 0.05 / 2. / 10000, 1.3])
+    v = numpy.array([3., 2., -.3, -5.])
+    m = numpy.array([1., 1., 1., 1.])
+    g = wendy_gb300.nbody(x, v, m, 0.05, approx=True, nleap=10000)
+    E = wendy_gb300.energy(x, v, m)
+    tx, tv = next(g)
+    assert numpy.fabs(wendy_gb300.energy(tx, tv, m) - E) / E < 1e-6
+
+
+def test_energy_and_momentum_conservation_small():
+    # tests/test_approx.py:6-32,151-163 (nleap reduced from 1e5 to 1e4)
+    x = numpy.array([-1.1, 0.1, 1.3])
+    v = numpy.array([3., 2., -5.])
+    m = numpy.array([1., 2., 3.])
+    g = wendy_gb300.nbody(x, v, m, 0.05, approx=True, nleap=10000)
+    E = wendy_gb300.energy(x, v, m)
+    p = wendy_gb300.momentum(v, m)
+    for _ in range(10):
+        tx, tv = next(g)
+        assert numpy.fabs(wendy_gb300.energy(tx, tv, m) - E) / E < 1e-6
+        assert numpy.fabs(wendy_gb300.momentum(tv, m) - p) < 1e-10
+
+
+def test_tracers_and_harmonic():
+    x, v, m = ics.sech2_disk(101, seed=4)
+    v = v - numpy.mean(v)
+    m = m.copy()
+    m[50:] = 0.
+    m *= 2.
+    g = wendy_gb300.nbody(x, v, m, 0.05, approx=True, nleap=1000, omega=1.1)
+    E = wendy_gb300.energy(x, v, m, omega=1.1)
+    for _ in range(20):
+        tx, tv = next(g)
+        assert numpy.fabs(wendy_gb300.energy(tx, tv, m, omega=1.1) - E) / E < 1e-6
+
+
+def test_runs_are_deterministic():
+    x, v, m = ics.top_hat(50000, seed=9)
+    res = []
+    for _ in range(2):
+        g = wendy_gb300.nbody(x, v, m, 0.01, approx=True, nleap=10, ext_force=PULSE, t0=4.0)
+        for _ in range(3):
+            tx, tv = next(g)
+        res.append((tx.copy(), tv.copy()))
+    assert numpy.array_equal(res[0][0], res[1][0]) and numpy.array_equal(res[0][1], res[1][1])
+
+
+def test_full_output_reports_device_time():
+    x, v, m = ics.sech2_disk(101, seed=5)
+    g = wendy_gb300.nbody(x, v, m, 0.05, approx=True, nleap=1000, full_output=True)
+    tx, tv, el = next(g)
+    assert 0 < el < 1.
+
+
+def test_bad_inputs_raise():
+    with pytest.raises(_lib.WendyGPUError):
+        wendy_gb300.Simulation(numpy.zeros(3), numpy.zeros(3), numpy.array([1., -1., 1.]), 1.)
+    with pytest.raises(_lib.WendyGPUError):
+        wendy_gb300.Simulation(numpy.array([0., numpy.nan, 1.]), numpy.zeros(3), numpy.ones(3), 3.)

@@ -1,0 +1,111 @@
+"""ctypes binding of the C ABI in include/wendy_gb300.h.
+
+Loads ``_wendy_gb300.so`` from this package directory, the way wendy loads
+``wendy_c`` (wendy/wendy.py:13-37), and declares the argument types of every
+entry point.  There is no fallback: if the library is missing or the CUDA
+runtime cannot load it, :func:`lib` raises.
+"""
+import ctypes
+import os
+
+import numpy
+from numpy.ctypeslib import ndpointer
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_wendy_gb300.so")
+
+WG_OK = 0
+STATUS_NAMES = {0: "WG_OK", -1: "WG_ERR_ARG", -2: "WG_ERR_CUDA", -3: "WG_ERR_NOMEM",
+                -4: "WG_ERR_DEVICE", -5: "WG_ERR_EXT", -6: "WG_ERR_BUDGET", -7: "WG_ERR_NODEV"}
+
+EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH = 0, 1, 2
+
+# Every symbol include/wendy_gb300.h declares.
+EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", "wg_create",
+           "wg_step", "wg_download", "wg_get_stats", "wg_destroy", "wg_accel",
+           "wg_nbody_approx_onestep", "wg_profile", "wg_host_register", "wg_host_unregister")
+
+
+class WgSheet(ctypes.Structure):
+    """``wg_sheet`` == wendy's ``struct array_w_index`` (wendy/wendy.h:12-16)."""
+
+    _fields_ = [("idx", ctypes.c_int), ("val", ctypes.c_double)]
+
+
+SHEET_DTYPE = numpy.dtype({"names": ["idx", "val"], "formats": [numpy.int32, numpy.float64],
+                           "offsets": [0, 8], "itemsize": 16})
+
+
+class WgStats(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("substeps", ctypes.c_int64),
+                ("sorts_full", ctypes.c_int64), ("sorts_skipped", ctypes.c_int64),
+                ("sorts_window", ctypes.c_int64), ("last_max_disp", ctypes.c_double),
+                ("device_bytes", ctypes.c_int64), ("launches", ctypes.c_int64)]
+
+
+class WendyGPUError(RuntimeError):
+    def __init__(self, status, where, detail):
+        self.status = status
+        super().__init__("%s failed with %s (%d): %s" % (where, STATUS_NAMES.get(status, "?"),
+                                                         status, detail))
+
+
+_F64 = ndpointer(dtype=numpy.float64, flags=("C_CONTIGUOUS",))
+_F64W = ndpointer(dtype=numpy.float64, flags=("C_CONTIGUOUS", "WRITEABLE"))
+_I32W = ndpointer(dtype=numpy.int32, flags=("C_CONTIGUOUS", "WRITEABLE"))
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+
+_lib = None
+
+
+def load_raw(path=LIB_PATH):
+    """Load the shared library without needing a GPU (symbols only)."""
+    if not os.path.exists(path):
+        raise ImportError("wendy_gb300 CUDA library not built: %s is missing "
+                          "(run `python -m wendy_gb300.build`)" % path)
+    return ctypes.CDLL(path)
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    L = load_raw()
+    L.wg_version.restype = _I
+    L.wg_status_string.argtypes = [_I]
+    L.wg_status_string.restype = ctypes.c_char_p
+    L.wg_last_error.restype = ctypes.c_char_p
+    L.wg_device_info.argtypes = [ctypes.POINTER(_I), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
+    L.wg_create.argtypes = [_I64, _F64, _F64, _F64, _D, _D, _I, _F64, _I,
+                            ctypes.POINTER(_P)]
+    L.wg_step.argtypes = [_P, _D, _I, ctypes.POINTER(_D), ctypes.POINTER(_D)]
+    L.wg_download.argtypes = [_P, _P, _P]
+    L.wg_get_stats.argtypes = [_P, ctypes.POINTER(WgStats)]
+    L.wg_destroy.argtypes = [_P]
+    L.wg_accel.argtypes = [_I64, _F64, _F64, _D, _D, _I, _F64, _I, _D, _P, _P]
+    L.wg_nbody_approx_onestep.argtypes = [_I, _P, _F64W, _F64W, _F64, _F64W, _D, _D, _I,
+                                          ctypes.POINTER(_D), _D, _I, _F64, _I,
+                                          ctypes.POINTER(_I), ctypes.POINTER(_D)]
+    L.wg_profile.argtypes = [_P, _I, _I, ctypes.POINTER(_D)]
+    L.wg_host_register.argtypes = [_P, _I64]
+    L.wg_host_unregister.argtypes = [_P]
+    for name in EXPORTS:
+        if name not in ("wg_status_string", "wg_last_error"):
+            getattr(L, name).restype = _I
+    _lib = L
+    return L
+
+
+def check(status, where):
+    if status != WG_OK:
+        detail = lib().wg_last_error().decode(errors="replace")
+        raise WendyGPUError(status, where, detail)
+
+
+def ext_params(params):
+    p = numpy.zeros(4)
+    p[:len(params)] = params
+    return p

@@ -1,0 +1,720 @@
+// wg_api.cu -- the C ABI (include/wendy_gb300.h): simulation handles, the
+// per-output step sequence, and the stateless entry points.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/wendy_gb300.h"
+#include "wg_internal.cuh"
+
+using namespace wg;
+
+namespace {
+
+thread_local char g_last_error[512] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+}
+
+#define WG_CUDA(call)                                                              \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                __LINE__);                                                         \
+      return e_ == cudaErrorMemoryAllocation ? WG_ERR_NOMEM : WG_ERR_CUDA;         \
+    }                                                                              \
+  } while (0)
+
+size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Host copy of the device conversion: round(m * 2^E) in 128 bits.
+u128 host_mass_to_fixed(double m, int E) {
+  uint64_t b;
+  std::memcpy(&b, &m, 8);
+  int ex = (int)((b >> 52) & 0x7FF);
+  uint64_t mant = b & 0xFFFFFFFFFFFFFull;
+  if (ex == 0) {
+    if (mant == 0) return 0;
+    ex = 1;
+  } else {
+    mant |= 1ull << 52;
+  }
+  const int s = ex - 1075 + E;
+  if (s >= 0) return ((u128)mant) << s;
+  const int r = -s;
+  if (r > 54) return 0;
+  return (u128)((mant + (1ull << (r - 1))) >> r);
+}
+
+int check_ext(int kind, const double* p, int np, ExtForce* out) {
+  out->kind = kind;
+  for (int i = 0; i < 4; ++i) out->p[i] = 0.0;
+  const int need = kind == WG_EXT_NONE ? 0 : kind == WG_EXT_HARMONIC ? 1 : kind == WG_EXT_PULSE_TANH ? 4 : -1;
+  if (need < 0) {
+    set_error("unknown external-force id %d", kind);
+    return WG_ERR_EXT;
+  }
+  if (np < need || (need > 0 && !p)) {
+    set_error("external force %d needs %d parameters, got %d", kind, need, np);
+    return WG_ERR_EXT;
+  }
+  for (int i = 0; i < need; ++i) {
+    if (!std::isfinite(p[i])) {
+      set_error("external-force parameter %d is not finite", i);
+      return WG_ERR_EXT;
+    }
+    out->p[i] = p[i];
+  }
+  if (kind == WG_EXT_PULSE_TANH && (p[2] == 0.0 || p[3] == 0.0)) {
+    set_error("pulsed force needs tau != 0 and h != 0");
+    return WG_ERR_EXT;
+  }
+  return WG_OK;
+}
+
+}  // namespace
+
+struct wg_sim {
+  int64_t n = 0;
+  int64_t n_tiles = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  void* big = nullptr;       // per-sheet arrays
+  void* small = nullptr;     // tables, flags, per-call parameters
+  size_t bytes = 0;
+  StateTable* table = nullptr;  // device
+  StateRef set[2];
+  TileRec* recs = nullptr;
+  RadixWork radix;
+  double* x_out = nullptr;
+  double* v_out = nullptr;
+  double* a_sorted = nullptr;
+  unsigned* err = nullptr;
+  int cap = 0;                   // sub-steps the per-call arrays hold
+  StepFlags* flags = nullptr;    // [cap + 1]
+  unsigned* tickets = nullptr;   // [cap]
+  double* t_seq = nullptr;       // [cap]
+  unsigned* epochs = nullptr;    // [cap]
+  void* stage = nullptr;         // staging of the reference-layout entry point
+  wg_sheet* stage_xi = nullptr;
+  double* stage_a = nullptr;
+  double* h_t = nullptr;         // pinned host mirrors
+  unsigned* h_ep = nullptr;
+  StepFlags* h_flags = nullptr;
+  // physics
+  uint64_t T_lo = 0, T_hi = 0;
+  int E = 0;
+  double totmass = 0, omega2 = -1;
+  ExtForce ext{};
+  unsigned epoch = 1;
+  wg_stats st{};
+};
+
+namespace {
+
+int alloc_call_arrays(wg_sim* s, int nleap) {
+  if (nleap <= s->cap) return WG_OK;
+  int cap = 64;
+  while (cap < nleap) cap *= 2;
+  // Keep which sorted set is current across the re-allocation.
+  StateTable t;
+  t.cur = s->set[0];
+  t.other = s->set[1];
+  if (s->table) {
+    WG_CUDA(cudaStreamSynchronize(s->stream));
+    WG_CUDA(cudaMemcpy(&t, s->table, sizeof(t), cudaMemcpyDeviceToHost));
+  }
+  if (s->small) cudaFree(s->small);
+  if (s->h_t) cudaFreeHost(s->h_t);
+  if (s->h_ep) cudaFreeHost(s->h_ep);
+  if (s->h_flags) cudaFreeHost(s->h_flags);
+  s->small = nullptr;
+  s->h_t = nullptr;
+  s->h_ep = nullptr;
+  s->h_flags = nullptr;
+  const size_t b = al(sizeof(StateTable)) + al(64) + al(sizeof(StepFlags) * (cap + 1)) +
+                   al(4 * (size_t)cap) + al(8 * (size_t)cap) + al(4 * (size_t)cap);
+  WG_CUDA(cudaMalloc(&s->small, b));
+  char* p = static_cast<char*>(s->small);
+  s->table = reinterpret_cast<StateTable*>(p); p += al(sizeof(StateTable));
+  s->err = reinterpret_cast<unsigned*>(p); p += al(64);
+  s->flags = reinterpret_cast<StepFlags*>(p); p += al(sizeof(StepFlags) * (cap + 1));
+  s->tickets = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)cap);
+  s->t_seq = reinterpret_cast<double*>(p); p += al(8 * (size_t)cap);
+  s->epochs = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)cap);
+  WG_CUDA(cudaMemsetAsync(s->small, 0, b, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->table, &t, sizeof(t), cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMallocHost(&s->h_t, 8 * (size_t)cap));
+  WG_CUDA(cudaMallocHost(&s->h_ep, 4 * (size_t)cap));
+  WG_CUDA(cudaMallocHost(&s->h_flags, sizeof(StepFlags) * (cap + 1)));
+  WG_CUDA(cudaStreamSynchronize(s->stream));
+  s->cap = cap;
+  return WG_OK;
+}
+
+void free_sim(wg_sim* s) {
+  if (!s) return;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->big) cudaFree(s->big);
+  if (s->small) cudaFree(s->small);
+  if (s->stage) cudaFree(s->stage);
+  if (s->h_t) cudaFreeHost(s->h_t);
+  if (s->h_ep) cudaFreeHost(s->h_ep);
+  if (s->h_flags) cudaFreeHost(s->h_flags);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+// Allocate a simulation for n sheets with the given physics; sheet data is
+// uploaded by the caller.
+int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_sim** out) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    set_error("no CUDA device visible");
+    return WG_ERR_NODEV;
+  }
+  wg_sim* s = new wg_sim();
+  s->n = n;
+  s->n_tiles = (n + kForceTile - 1) / kForceTile;
+  s->totmass = totmass;
+  s->omega2 = omega2;
+  s->ext = ext;
+  // Fixed-point scale: totmass < 2^eT, so 8 * totmass * 2^E < 2^126.
+  if (totmass > 0) {
+    int eT = 0;
+    std::frexp(totmass, &eT);
+    s->E = 123 - eT;
+  } else {
+    s->E = 0;
+  }
+  const u128 T = host_mass_to_fixed(totmass, s->E);
+  s->T_lo = (uint64_t)T;
+  s->T_hi = (uint64_t)(T >> 64);
+  int rc = WG_OK;
+  auto fail = [&](int code) {
+    free_sim(s);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) {
+    set_error("stream/event creation failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail(WG_ERR_CUDA);
+  }
+  const size_t nd = al((size_t)n * 8), ni = al((size_t)n * 4);
+  const size_t set_b = 3 * nd + ni;
+  const size_t recs_b = al(sizeof(TileRec) * (size_t)s->n_tiles);
+  const size_t radix_b = radix_bytes(n);
+  const size_t out_b = 3 * nd;  // x_out, v_out, a_sorted
+  const size_t total = 2 * set_b + recs_b + radix_b + out_b;
+  cudaError_t e = cudaMalloc(&s->big, total);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaMalloc of %zu bytes for %lld sheets failed: %s", total, (long long)n,
+              cudaGetErrorString(e));
+    return fail(WG_ERR_NOMEM);
+  }
+  s->bytes = total;
+  char* p = static_cast<char*>(s->big);
+  for (int k = 0; k < 2; ++k) {
+    s->set[k].x = reinterpret_cast<double*>(p); p += nd;
+    s->set[k].v = reinterpret_cast<double*>(p); p += nd;
+    s->set[k].m = reinterpret_cast<double*>(p); p += nd;
+    s->set[k].idx = reinterpret_cast<int32_t*>(p); p += ni;
+  }
+  s->recs = reinterpret_cast<TileRec*>(p); p += recs_b;
+  radix_bind(&s->radix, p, n); p += radix_b;
+  s->x_out = reinterpret_cast<double*>(p); p += nd;
+  s->v_out = reinterpret_cast<double*>(p); p += nd;
+  s->a_sorted = reinterpret_cast<double*>(p); p += nd;
+  if (cudaMemsetAsync(s->recs, 0, recs_b, s->stream) != cudaSuccess) {
+    set_error("memset failed");
+    return fail(WG_ERR_CUDA);
+  }
+  rc = alloc_call_arrays(s, 64);
+  if (rc != WG_OK) return fail(rc);
+  s->st.n = n;
+  s->st.device_bytes = (int64_t)(total);
+  *out = s;
+  return WG_OK;
+}
+
+int validate_sheets(int64_t n, const double* x, const double* v, const double* m,
+                    double totmass) {
+  if (n < 1 || n >= (1ll << 30)) {
+    set_error("number of sheets %lld outside [1, 2^30)", (long long)n);
+    return WG_ERR_ARG;
+  }
+  if (!x || !v || !m) {
+    set_error("null array");
+    return WG_ERR_ARG;
+  }
+  if (!std::isfinite(totmass) || totmass < 0) {
+    set_error("totmass must be finite and >= 0");
+    return WG_ERR_ARG;
+  }
+  double mmax = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!(m[i] >= 0) || !std::isfinite(m[i])) {
+      set_error("mass %lld is negative or not finite", (long long)i);
+      return WG_ERR_ARG;
+    }
+    if (!std::isfinite(x[i]) || !std::isfinite(v[i])) {
+      set_error("position or velocity %lld is not finite", (long long)i);
+      return WG_ERR_ARG;
+    }
+    if (m[i] > mmax) mmax = m[i];
+  }
+  if (mmax > 2 * totmass) {
+    set_error("a single mass exceeds twice totmass; totmass must be the sum of the masses");
+    return WG_ERR_ARG;
+  }
+  return WG_OK;
+}
+
+// Read the device error word and the per-sub-step flags of the last call.
+int finish_call(wg_sim* s, int nleap) {
+  unsigned err = 0;
+  WG_CUDA(cudaMemcpyAsync(&err, s->err, 4, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(StepFlags) * (nleap + 1),
+                          cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaStreamSynchronize(s->stream));
+  for (int i = 0; i < nleap; ++i) {
+    if (s->h_flags[i].unsorted)
+      s->st.sorts_full++;
+    else
+      s->st.sorts_skipped++;
+  }
+  s->st.substeps += nleap;
+  if (err) {
+    set_error("device error word 0x%x (bounded wait expired or internal check)", err);
+    cudaMemsetAsync(s->err, 0, 4, s->stream);
+    return WG_ERR_DEVICE;
+  }
+  return WG_OK;
+}
+
+// Enqueue one output interval: half drift, nleap x [sort, force/kick/drift].
+// The last force evaluation's accelerations go to s->a_sorted when
+// want_accel is set.  t_seq must be in s->h_t already.
+int enqueue_step(wg_sim* s, double dt, int nleap, bool want_accel, double dt_last_drift) {
+  for (int i = 0; i < nleap; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
+  s->epoch += (unsigned)nleap;
+  if (s->epoch > (1u << 29)) {  // keep (epoch << 2) in 32 bits: restart epochs
+    WG_CUDA(cudaMemsetAsync(s->recs, 0, sizeof(TileRec) * (size_t)s->n_tiles, s->stream));
+    s->epoch = 1;
+    for (int i = 0; i < nleap; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
+    s->epoch += (unsigned)nleap;
+  }
+  WG_CUDA(cudaMemcpyAsync(s->t_seq, s->h_t, 8 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->epochs, s->h_ep, 4 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemsetAsync(s->flags, 0, sizeof(StepFlags) * (nleap + 1), s->stream));
+  WG_CUDA(cudaMemsetAsync(s->tickets, 0, 4 * (size_t)nleap, s->stream));
+  launch_drift(s->table, s->n, dt / 2., &s->flags[0], s->stream);
+  s->st.launches += 1 + (int64_t)nleap * (1 + kRadixLaunches);
+  ForceArgs a;
+  a.table = s->table;
+  a.n = s->n;
+  a.T_lo = s->T_lo;
+  a.T_hi = s->T_hi;
+  a.E = s->E;
+  a.has_omega = s->omega2 >= 0;
+  a.omega2 = s->omega2;
+  a.ext = s->ext;
+  a.t_seq = s->t_seq;
+  a.epochs = s->epochs;
+  a.recs = s->recs;
+  a.err = s->err;
+  for (int i = 0; i < nleap; ++i) {
+    radix_sort_state(s->table, s->n, &s->radix, &s->flags[i], s->err, s->stream);
+    a.sub = i;
+    a.dt_kick = dt;
+    a.dt_drift = (i == nleap - 1) ? dt_last_drift : dt;
+    a.a_out = (want_accel && i == nleap - 1) ? s->a_sorted : nullptr;
+    a.ticket = s->tickets + i;
+    a.flag_out = &s->flags[i + 1];
+    launch_force(a, s->n_tiles, s->stream);
+  }
+  WG_CUDA(cudaGetLastError());
+  return WG_OK;
+}
+
+void fill_times(wg_sim* s, double dt, int nleap, double* t0) {
+  double t = t0 ? *t0 : 0.0;
+  for (int i = 0; i < nleap; ++i) {
+    s->h_t[i] = t;
+    if (s->ext.kind != EXT_NONE) t += dt;  // wendy/wendy.c:403-404,409-410
+  }
+  if (t0) *t0 = t;
+}
+
+// Cache of one simulation for the stateless reference-shaped entry point.
+std::mutex g_cache_mu;
+wg_sim* g_cache = nullptr;
+
+__global__ void k_load_sheets(StateTable* table, int64_t n, const wg_sheet* xi, const double* v,
+                              const double* m) {
+  const StateRef st = table->cur;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int32_t j = xi[i].idx;
+    st.idx[i] = j;
+    st.x[i] = xi[i].val;
+    st.v[i] = v[j];
+    st.m[i] = m[j];
+  }
+}
+
+__global__ void k_store_sheets(const StateTable* table, int64_t n, wg_sheet* xi) {
+  const StateRef st = table->cur;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    wg_sheet r;
+    r.idx = st.idx[i];
+    r.val = st.x[i];
+    xi[i] = r;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int wg_version(void) { return 100; }
+
+const char* wg_status_string(int status) {
+  switch (status) {
+    case WG_OK: return "ok";
+    case WG_ERR_ARG: return "invalid argument";
+    case WG_ERR_CUDA: return "CUDA runtime error";
+    case WG_ERR_NOMEM: return "device memory allocation failed";
+    case WG_ERR_DEVICE: return "device-side error (bounded wait expired or internal check)";
+    case WG_ERR_EXT: return "unknown external force or bad parameters";
+    case WG_ERR_BUDGET: return "memory budget exceeded";
+    case WG_ERR_NODEV: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char* wg_last_error(void) { return g_last_error; }
+
+int wg_device_info(int* sm_count, int64_t* free_bytes, int64_t* total_bytes) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    set_error("no CUDA device visible");
+    return WG_ERR_NODEV;
+  }
+  int dev = 0;
+  WG_CUDA(cudaGetDevice(&dev));
+  if (sm_count) WG_CUDA(cudaDeviceGetAttribute(sm_count, cudaDevAttrMultiProcessorCount, dev));
+  size_t fr = 0, tot = 0;
+  WG_CUDA(cudaMemGetInfo(&fr, &tot));
+  if (free_bytes) *free_bytes = (int64_t)fr;
+  if (total_bytes) *total_bytes = (int64_t)tot;
+  return WG_OK;
+}
+
+int wg_create(int64_t n, const double* x, const double* v, const double* m, double totmass,
+              double omega2, int ext_kind, const double* ext_params, int n_ext_params,
+              wg_sim** out) {
+  if (!out) {
+    set_error("null output handle");
+    return WG_ERR_ARG;
+  }
+  *out = nullptr;
+  int rc = validate_sheets(n, x, v, m, totmass);
+  if (rc) return rc;
+  if (!std::isfinite(omega2)) {
+    set_error("omega2 must be finite");
+    return WG_ERR_ARG;
+  }
+  ExtForce ext;
+  rc = check_ext(ext_kind, ext_params, n_ext_params, &ext);
+  if (rc) return rc;
+  wg_sim* s = nullptr;
+  rc = make_sim(n, totmass, omega2, ext, &s);
+  if (rc) return rc;
+  const StateRef c = s->set[0];
+  auto up = [&](void* d, const void* h, size_t b) {
+    return cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, s->stream);
+  };
+  if (up(c.x, x, 8 * n) != cudaSuccess || up(c.v, v, 8 * n) != cudaSuccess ||
+      up(c.m, m, 8 * n) != cudaSuccess) {
+    set_error("upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+    free_sim(s);
+    return WG_ERR_CUDA;
+  }
+  launch_init_state(s->table, n, s->stream);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) {
+    set_error("initialisation failed: %s", cudaGetErrorString(cudaGetLastError()));
+    free_sim(s);
+    return WG_ERR_CUDA;
+  }
+  *out = s;
+  return WG_OK;
+}
+
+int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
+  if (!s) {
+    set_error("null simulation");
+    return WG_ERR_ARG;
+  }
+  if (nleap < 1 || !std::isfinite(dt)) {
+    set_error("nleap must be >= 1 and dt finite");
+    return WG_ERR_ARG;
+  }
+  int rc = alloc_call_arrays(s, nleap);
+  if (rc) return rc;
+  fill_times(s, dt, nleap, t0);
+  WG_CUDA(cudaEventRecord(s->ev0, s->stream));
+  rc = enqueue_step(s, dt, nleap, false, dt / 2.);
+  if (rc) return rc;
+  WG_CUDA(cudaEventRecord(s->ev1, s->stream));
+  rc = finish_call(s, nleap);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+  if (time_elapsed) *time_elapsed = ms * 1e-3;
+  const double vmax = [&] {
+    double d;
+    unsigned long long b = s->h_flags[nleap].max_v;
+    std::memcpy(&d, &b, 8);
+    return d;
+  }();
+  s->st.last_max_disp = vmax * std::fabs(dt / 2.);
+  return rc;
+}
+
+int wg_download(wg_sim* s, double* x, double* v) {
+  if (!s) {
+    set_error("null simulation");
+    return WG_ERR_ARG;
+  }
+  launch_desort(s->table, s->n, s->x_out, s->v_out, s->stream);
+  if (x) WG_CUDA(cudaMemcpyAsync(x, s->x_out, 8 * s->n, cudaMemcpyDeviceToHost, s->stream));
+  if (v) WG_CUDA(cudaMemcpyAsync(v, s->v_out, 8 * s->n, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaStreamSynchronize(s->stream));
+  return WG_OK;
+}
+
+int wg_get_stats(wg_sim* s, wg_stats* out) {
+  if (!s || !out) {
+    set_error("null argument");
+    return WG_ERR_ARG;
+  }
+  *out = s->st;
+  return WG_OK;
+}
+
+int wg_destroy(wg_sim* s) {
+  free_sim(s);
+  return WG_OK;
+}
+
+int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
+  if (!s || reps < 1 || !avg_seconds || (what != WG_PROF_FORCE && what != WG_PROF_SORT)) {
+    set_error("bad arguments to wg_profile");
+    return WG_ERR_ARG;
+  }
+  int rc = alloc_call_arrays(s, reps);
+  if (rc) return rc;
+  for (int i = 0; i < reps; ++i) {
+    s->h_t[i] = 0.0;
+    s->h_ep[i] = s->epoch + (unsigned)i;
+  }
+  s->epoch += (unsigned)reps;
+  WG_CUDA(cudaMemcpyAsync(s->t_seq, s->h_t, 8 * (size_t)reps, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->epochs, s->h_ep, 4 * (size_t)reps, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemsetAsync(s->tickets, 0, 4 * (size_t)reps, s->stream));
+  // flags[i].unsorted = 1 forces every sort to run in full
+  for (int i = 0; i < reps; ++i) s->h_flags[i] = StepFlags{1u, 0u, 0ull};
+  WG_CUDA(cudaMemcpyAsync(s->flags, s->h_flags, sizeof(StepFlags) * (size_t)reps,
+                          cudaMemcpyHostToDevice, s->stream));
+  ForceArgs a;
+  a.table = s->table;
+  a.n = s->n;
+  a.T_lo = s->T_lo;
+  a.T_hi = s->T_hi;
+  a.E = s->E;
+  a.has_omega = s->omega2 >= 0;
+  a.omega2 = s->omega2;
+  a.ext = s->ext;
+  a.t_seq = s->t_seq;
+  a.epochs = s->epochs;
+  a.recs = s->recs;
+  a.err = s->err;
+  a.a_out = nullptr;
+  a.dt_kick = 0.0;
+  a.dt_drift = 0.0;
+  a.flag_out = &s->flags[s->cap];  // scratch slot
+  WG_CUDA(cudaStreamSynchronize(s->stream));
+  WG_CUDA(cudaEventRecord(s->ev0, s->stream));
+  for (int i = 0; i < reps; ++i) {
+    if (what == WG_PROF_FORCE) {
+      a.sub = i;
+      a.ticket = s->tickets + i;
+      launch_force(a, s->n_tiles, s->stream);
+    } else {
+      radix_sort_state(s->table, s->n, &s->radix, &s->flags[i], s->err, s->stream);
+    }
+  }
+  WG_CUDA(cudaEventRecord(s->ev1, s->stream));
+  WG_CUDA(cudaStreamSynchronize(s->stream));
+  WG_CUDA(cudaGetLastError());
+  float ms = 0;
+  WG_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+  *avg_seconds = ms * 1e-3 / reps;
+  s->st.launches += what == WG_PROF_FORCE ? reps : (int64_t)reps * kRadixLaunches;
+  unsigned err = 0;
+  WG_CUDA(cudaMemcpy(&err, s->err, 4, cudaMemcpyDeviceToHost));
+  if (err) {
+    set_error("device error word 0x%x during profiling", err);
+    cudaMemset(s->err, 0, 4);
+    return WG_ERR_DEVICE;
+  }
+  return WG_OK;
+}
+
+int wg_host_register(void* ptr, int64_t bytes) {
+  if (!ptr || bytes <= 0) {
+    set_error("bad arguments to wg_host_register");
+    return WG_ERR_ARG;
+  }
+  WG_CUDA(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+  return WG_OK;
+}
+
+int wg_host_unregister(void* ptr) {
+  WG_CUDA(cudaHostUnregister(ptr));
+  return WG_OK;
+}
+
+int wg_accel(int64_t n, const double* x, const double* m, double totmass, double omega2,
+             int ext_kind, const double* ext_params, int n_ext_params, double t, double* a,
+             int32_t* perm) {
+  std::vector<double> zero((size_t)(n > 0 ? n : 1), 0.0);
+  int rc = validate_sheets(n, x, zero.data(), m, totmass);
+  if (rc) return rc;
+  ExtForce ext;
+  rc = check_ext(ext_kind, ext_params, n_ext_params, &ext);
+  if (rc) return rc;
+  wg_sim* s = nullptr;
+  rc = make_sim(n, totmass, omega2, ext, &s);
+  if (rc) return rc;
+  const StateRef c = s->set[0];
+  cudaMemcpyAsync(c.x, x, 8 * n, cudaMemcpyHostToDevice, s->stream);
+  cudaMemsetAsync(c.v, 0, 8 * n, s->stream);
+  cudaMemcpyAsync(c.m, m, 8 * n, cudaMemcpyHostToDevice, s->stream);
+  launch_init_state(s->table, n, s->stream);
+  s->h_t[0] = t;
+  // One force evaluation: a zero-length drift (v = 0) leaves x as given and
+  // marks the order for sorting, then sort and one force kernel with
+  // dt_kick = dt_drift = 0.
+  rc = enqueue_step(s, 0.0, 1, true, 0.0);
+  if (rc == WG_OK) {
+    StateTable tab;
+    launch_scatter_accel(s->table, n, s->a_sorted, s->x_out, s->stream);
+    cudaMemcpyAsync(&tab, s->table, sizeof(tab), cudaMemcpyDeviceToHost, s->stream);
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) {
+      set_error("accel failed: %s", cudaGetErrorString(cudaGetLastError()));
+      rc = WG_ERR_CUDA;
+    } else {
+      if (a) cudaMemcpy(a, s->x_out, 8 * n, cudaMemcpyDeviceToHost);
+      if (perm) cudaMemcpy(perm, tab.cur.idx, 4 * n, cudaMemcpyDeviceToHost);
+      rc = finish_call(s, 1);
+    }
+  }
+  free_sim(s);
+  return rc;
+}
+
+int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const double* m,
+                            double* a, double totmass, double dt, int nleap, double* t0,
+                            double omega2, int ext_kind, const double* ext_params,
+                            int n_ext_params, int* err, double* time_elapsed) {
+  if (err) *err = 0;
+  if (!xi || !x || !v || !m || !a || nleap < 1 || n < 1) {
+    set_error("null buffer, n < 1 or nleap < 1");
+    return WG_ERR_ARG;
+  }
+  ExtForce ext;
+  int rc = check_ext(ext_kind, ext_params, n_ext_params, &ext);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_cache_mu);
+  wg_sim* s = g_cache;
+  if (!s || s->n != n) {
+    free_sim(s);
+    g_cache = nullptr;
+    rc = make_sim(n, totmass, omega2, ext, &s);
+    if (rc) return rc;
+    g_cache = s;
+  }
+  // physics of this call
+  s->totmass = totmass;
+  s->omega2 = omega2;
+  s->ext = ext;
+  if (totmass > 0) {
+    int eT = 0;
+    std::frexp(totmass, &eT);
+    s->E = 123 - eT;
+  } else {
+    s->E = 0;
+  }
+  const u128 T = host_mass_to_fixed(totmass, s->E);
+  s->T_lo = (uint64_t)T;
+  s->T_hi = (uint64_t)(T >> 64);
+  rc = alloc_call_arrays(s, nleap);
+  if (rc) return rc;
+  if (!s->stage) {
+    const size_t b = al(sizeof(wg_sheet) * (size_t)n) + al(8 * (size_t)n);
+    WG_CUDA(cudaMalloc(&s->stage, b));
+    s->stage_xi = static_cast<wg_sheet*>(s->stage);
+    s->stage_a = reinterpret_cast<double*>(static_cast<char*>(s->stage) +
+                                           al(sizeof(wg_sheet) * (size_t)n));
+    s->st.device_bytes += (int64_t)b;
+  }
+  // v and m arrive in original order; the desort buffers hold them until the
+  // sheets are loaded into sorted-state layout.
+  wg_sheet* d_xi = s->stage_xi;
+  double* d_v = s->x_out;
+  double* d_m = s->v_out;
+  StateTable t0tab;
+  t0tab.cur = s->set[0];
+  t0tab.other = s->set[1];
+  WG_CUDA(cudaEventRecord(s->ev0, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->table, &t0tab, sizeof(t0tab), cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemcpyAsync(d_xi, xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemcpyAsync(d_v, v, 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemcpyAsync(d_m, m, 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  k_load_sheets<<<152 * 8, 256, 0, s->stream>>>(s->table, n, d_xi, d_v, d_m);
+  fill_times(s, dt, nleap, t0);
+  rc = enqueue_step(s, dt, nleap, true, dt / 2.);
+  if (rc) return rc;
+  k_store_sheets<<<152 * 8, 256, 0, s->stream>>>(s->table, n, d_xi);
+  launch_desort(s->table, n, s->x_out, s->v_out, s->stream);
+  launch_scatter_accel(s->table, n, s->a_sorted, s->stage_a, s->stream);
+  WG_CUDA(cudaMemcpyAsync(xi, d_xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaMemcpyAsync(x, s->x_out, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaMemcpyAsync(v, s->v_out, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaMemcpyAsync(a, s->stage_a, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaEventRecord(s->ev1, s->stream));
+  rc = finish_call(s, nleap);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+  if (time_elapsed) *time_elapsed = ms * 1e-3;
+  if (rc && err) *err = rc;
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// wg_common.cuh -- shared device helpers of the GB300 approximate integrator.
+//
+// Order-preserving position keys, the exact fixed-point mass arithmetic the
+// force kernel is built on, and the acquire/release primitives of the
+// decoupled look-back scans.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wg {
+
+typedef unsigned __int128 u128;
+typedef __int128 i128;
+
+// Device error word bits (read back by the host after every call).
+enum : unsigned {
+  DEV_ERR_LOOKBACK_TIMEOUT = 1u << 0,  // a look-back wait hit its iteration limit
+  DEV_ERR_RADIX_TIMEOUT = 1u << 1,     // a radix-sort look-back wait hit its limit
+  DEV_ERR_BUCKET_OVERFLOW = 1u << 2,   // a bucket received more sheets than its capacity
+  DEV_ERR_FIXED_RANGE = 1u << 3,       // a mass outside the fixed-point range
+  DEV_ERR_BAD_STATE = 1u << 4,         // an internal consistency check failed
+};
+
+// Upper bound on the iterations of any spin-wait on another CTA's flag.  Each
+// iteration backs off with __nanosleep, so the bound is well above a second
+// of wall time; after it the waiter records an error and stops waiting.
+constexpr unsigned kSpinLimit = 1u << 22;
+
+// ---------------------------------------------------------------------------
+// Position keys.  key_of is strictly increasing in x over the non-NaN doubles
+// except that -0.0 and +0.0 share a key (the reference's comparator treats
+// them as equal, wendy/wendy.c:21).  Sorting by (key, original index) is the
+// total order every path of this library uses.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t key_of(double x) {
+  uint64_t b = (uint64_t)__double_as_longlong(x);
+  if (b == 0x8000000000000000ull) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// ---------------------------------------------------------------------------
+// Fixed-point masses.  A mass m >= 0 is represented by the integer
+// round(m * 2^E) in 128 bits, where the host picks E so that
+// 8 * totmass * 2^E < 2^127.  Prefix sums of these integers are exact and
+// independent of association order, so the cumulative mass -- and with it the
+// acceleration -- does not depend on tile size, look-back pattern or batching.
+// The acceleration totmass - 2 C_i - m_i (wendy/wendy.c:375-383) is formed
+// exactly in the integers and rounded to double once.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ u128 mass_to_fixed(double m, int E) {
+  uint64_t b = (uint64_t)__double_as_longlong(m);
+  int ex = (int)((b >> 52) & 0x7FF);
+  uint64_t mant = b & 0xFFFFFFFFFFFFFull;
+  if (ex == 0) {
+    if (mant == 0) return 0;
+    ex = 1;
+  } else {
+    mant |= 1ull << 52;
+  }
+  int s = ex - 1075 + E;  // m = mant * 2^(ex - 1075)
+  if (s >= 0) return ((u128)mant) << s;
+  int r = -s;
+  if (r > 54) return 0;  // below half a unit
+  return (u128)((mant + (1ull << (r - 1))) >> r);
+}
+
+// Signed 128-bit integer A times 2^-E, rounded to nearest even.  The normal
+// range is handled with integer operations only (FP64 issue slots are the
+// scarce resource on this part); an out-of-range exponent falls back to
+// ldexp.
+__device__ __forceinline__ double fixed_to_double(i128 A, int E) {
+  if (A == 0) return 0.0;
+  const bool neg = A < 0;
+  const u128 u = neg ? (u128)(-A) : (u128)A;
+  const uint64_t hi = (uint64_t)(u >> 64), lo = (uint64_t)u;
+  const int lz = hi ? __clzll((long long)hi) : 64 + __clzll((long long)lo);
+  const int p = 127 - lz;  // index of the leading one
+  uint64_t mant;
+  int e2;  // |A| ~= mant * 2^e2, mant in [2^52, 2^53)
+  if (p <= 52) {
+    mant = lo << (52 - p);
+    e2 = p - 52;
+  } else {
+    int sh = p - 52;
+    mant = (uint64_t)(u >> sh);
+    const u128 rem = u & ((((u128)1) << sh) - 1);
+    const u128 half = ((u128)1) << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) {
+      ++mant;
+      if (mant == (1ull << 53)) {
+        mant >>= 1;
+        ++sh;
+      }
+    }
+    e2 = sh;
+  }
+  const int bexp = e2 - E + 52 + 1023;
+  if (bexp <= 0 || bexp >= 2047) {
+    const double r = ldexp((double)mant, e2 - E);
+    return neg ? -r : r;
+  }
+  const uint64_t bits = ((uint64_t)bexp << 52) | (mant & 0xFFFFFFFFFFFFFull) |
+                        (neg ? 0x8000000000000000ull : 0ull);
+  return __longlong_as_double((long long)bits);
+}
+
+// ---------------------------------------------------------------------------
+// Memory-model helpers for flags that other CTAs spin on.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_cg_u64(const uint64_t* p) {
+  return (uint64_t)__ldcg((const unsigned long long*)p);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Warp-wide inclusive scan of a 128-bit unsigned value.
+__device__ __forceinline__ u128 warp_inclusive_scan_u128(u128 v, int lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint64_t lo = __shfl_up_sync(0xffffffffu, (unsigned long long)(uint64_t)v, d);
+    const uint64_t hi = __shfl_up_sync(0xffffffffu, (unsigned long long)(uint64_t)(v >> 64), d);
+    if (lane >= d) v += (((u128)hi) << 64) | lo;
+  }
+  return v;
+}
+
+__device__ __forceinline__ u128 shfl_u128(u128 v, int src) {
+  const uint64_t lo = __shfl_sync(0xffffffffu, (unsigned long long)(uint64_t)v, src);
+  const uint64_t hi = __shfl_sync(0xffffffffu, (unsigned long long)(uint64_t)(v >> 64), src);
+  return (((u128)hi) << 64) | lo;
+}
+
+__device__ __forceinline__ u128 warp_sum_u128(u128 v) {
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) {
+    const uint64_t lo = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)v, d);
+    const uint64_t hi = __shfl_xor_sync(0xffffffffu, (unsigned long long)(uint64_t)(v >> 64), d);
+    v += (((u128)hi) << 64) | lo;
+  }
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Registered external forces (closed forms replacing wendy's ext_force
+// callables, wendy/wendy.py:389-418).
+// ---------------------------------------------------------------------------
+enum : int { EXT_NONE = 0, EXT_HARMONIC = 1, EXT_PULSE_TANH = 2, EXT_MAX = 2 };
+
+struct ExtForce {
+  int kind;
+  double p[4];
+};
+
+// Time factor of the pulsed force, A exp(-(t-t0)^2 / (2 tau^2)); evaluated
+// once per force evaluation, with the numpy expression's operation order.
+__device__ __forceinline__ double pulse_amplitude(const ExtForce& f, double t) {
+  const double d = t - f.p[1];
+  return f.p[0] * exp(-(d * d) / (2.0 * (f.p[2] * f.p[2])));
+}
+
+// F(x, t) given the per-evaluation amplitude `amp` (pulse) -- harmonic:
+// -p0 x; pulse: amp * tanh(x / h).
+__device__ __forceinline__ double ext_force_at(const ExtForce& f, double amp, double x) {
+  if (f.kind == EXT_HARMONIC) return -f.p[0] * x;
+  if (f.kind == EXT_PULSE_TANH) return amp * tanh(x / f.p[3]);
+  return 0.0;
+}
+
+}  // namespace wg

@@ -1,0 +1,391 @@
+// wg_radix.cu -- full on-device re-sort of the sheets: a least-significant-
+// digit radix sort of the 64-bit position keys with 8-bit digits, one pass
+// per digit, each pass a single read and write of (key, slot) pairs whose
+// tile offsets come from a decoupled look-back over per-tile digit counts
+// ("onesweep").  It replaces the serial argsort of the reference
+// (wendy/wendy.c:341-357) when the order cannot be repaired locally.
+//
+//   hist   one read of the positions: all eight digit histograms
+//   plan   exclusive digit offsets; passes whose digit is the same for every
+//          key are skipped (decided on the device)
+//   pass   8x: rank within the tile (warp match + shared-memory counters,
+//          stable), look-back for the tile's global digit offsets, stage in
+//          shared memory, write out
+//   gather permute x, v, m, idx into the other state set
+//   ties   equal keys are ordered by original index (rare; usually no-op)
+//   flip   the other set becomes the current one
+//
+// Every kernel first reads the sub-step's `unsorted` flag and returns at once
+// when the sheets are already in order, so the sequence can be captured in a
+// CUDA graph and still cost nothing when no sort is needed.
+#include <cstdint>
+
+#include "wg_internal.cuh"
+
+namespace wg {
+
+namespace {
+
+constexpr int R = 256;
+constexpr unsigned kStatA = 1u << 30, kStatP = 2u << 30, kCountMask = (1u << 30) - 1;
+
+// plan layout (uint32 words)
+constexpr int kPlanActive = 0;   // [8]
+constexpr int kPlanSrc = 8;      // [8]
+constexpr int kPlanDst = 16;     // [8]
+constexpr int kPlanFinal = 24;   // [1]
+constexpr int kPlanStarts = 32;  // [8 * 256]
+constexpr int kPlanWords = kPlanStarts + 8 * R;
+
+struct PassArgs {
+  const StateTable* table;
+  int64_t n;
+  int pass;
+  int64_t n_tiles;
+  uint64_t* keys0;
+  uint64_t* keys1;
+  uint32_t* pos0;
+  uint32_t* pos1;
+  const uint32_t* plan;
+  uint32_t* status;
+  uint32_t* counters;
+  const StepFlags* flag;
+  unsigned* err;
+};
+
+__global__ void k_radix_hist(const StateTable* table, int64_t n, uint32_t* hist,
+                             const StepFlags* flag) {
+  if (!flag->unsorted) return;
+  __shared__ uint32_t sh[8 * R];
+  for (int i = threadIdx.x; i < 8 * R; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const double* x = table->cur.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint64_t k = key_of(x[i]);
+#pragma unroll
+    for (int p = 0; p < 8; ++p) atomicAdd(&sh[p * R + ((k >> (8 * p)) & 255u)], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 8 * R; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// One block of 256 threads.
+__global__ void k_radix_plan(int64_t n, const uint32_t* hist, uint32_t* plan,
+                             const StepFlags* flag) {
+  if (!flag->unsorted) return;
+  __shared__ uint32_t s_tmp[R / 32];
+  __shared__ int s_trivial[8];
+  const int d = threadIdx.x, lane = d & 31, warp = d >> 5;
+  for (int p = 0; p < 8; ++p) {
+    const uint32_t c = hist[p * R + d];
+    const int triv = __syncthreads_or(c == (uint32_t)n);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_tmp[warp] = incl;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int w = 0; w < warp; ++w) wpre += s_tmp[w];
+    plan[kPlanStarts + p * R + d] = wpre + incl - c;
+    if (d == 0) s_trivial[p] = triv;
+    __syncthreads();
+  }
+  if (d == 0) {
+    int cur = 0;
+    plan[kPlanActive + 0] = 1;
+    plan[kPlanSrc + 0] = 0;
+    plan[kPlanDst + 0] = 0;
+    for (int p = 1; p < 8; ++p) {
+      const int act = !s_trivial[p];
+      plan[kPlanActive + p] = act;
+      plan[kPlanSrc + p] = cur;
+      plan[kPlanDst + p] = act ? 1 - cur : cur;
+      if (act) cur = 1 - cur;
+    }
+    plan[kPlanFinal] = cur;
+  }
+}
+
+template <int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS) k_radix_pass(const PassArgs a) {
+  constexpr int TILE = THREADS * ITEMS;
+  constexpr int WARPS = THREADS / 32;
+  static_assert(THREADS == R, "one thread per digit");
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t* skeys = reinterpret_cast<uint64_t*>(smem);
+  uint32_t* svals = reinterpret_cast<uint32_t*>(skeys + TILE);
+  __shared__ uint32_t s_whist[WARPS][R];
+  __shared__ uint32_t s_tile_excl[R];
+  __shared__ uint32_t s_gbase[R];
+  __shared__ uint32_t s_tmp[WARPS];
+  __shared__ unsigned s_tile;
+
+  if (!a.flag->unsorted) return;
+  const int pass = a.pass;
+  if (!a.plan[kPlanActive + pass]) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(&a.counters[pass], 1u);
+  for (int i = tid; i < WARPS * R; i += THREADS) (&s_whist[0][0])[i] = 0;
+  __syncthreads();
+  const int64_t tile = s_tile;
+  const int64_t base = tile * TILE;
+  const int tile_n = (int)((a.n - base) < TILE ? (a.n - base) : TILE);
+  const int shift = 8 * pass;
+  const int srcb = (int)a.plan[kPlanSrc + pass], dstb = (int)a.plan[kPlanDst + pass];
+  const uint64_t* ksrc = srcb ? a.keys1 : a.keys0;
+  const uint32_t* psrc = srcb ? a.pos1 : a.pos0;
+  uint64_t* kdst = dstb ? a.keys1 : a.keys0;
+  uint32_t* pdst = dstb ? a.pos1 : a.pos0;
+  const double* x = a.table->cur.x;
+
+  uint64_t key[ITEMS];
+  uint32_t val[ITEMS];
+  uint32_t rank[ITEMS];
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i) {
+    const int local = warp * (32 * ITEMS) + i * 32 + lane;
+    const int64_t e = base + local;
+    if (local < tile_n) {
+      if (pass == 0) {
+        key[i] = key_of(x[e]);
+        val[i] = (uint32_t)e;
+      } else {
+        key[i] = ksrc[e];
+        val[i] = psrc[e];
+      }
+    } else {
+      key[i] = 0;
+      val[i] = 0;
+    }
+  }
+  // Stable ranking inside the warp: items in order, lanes in order.
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i) {
+    const int local = warp * (32 * ITEMS) + i * 32 + lane;
+    const bool ok = local < tile_n;
+    const unsigned d = ok ? (unsigned)((key[i] >> shift) & 255u) : (0x100u + lane);
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    uint32_t old = 0;
+    if (ok) {
+      old = s_whist[warp][d];
+      rank[i] = old + __popc(peers & lanemask_lt());
+    }
+    __syncwarp();
+    if (ok && lane == __ffs(peers) - 1) s_whist[warp][d] = old + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // Column of digit `tid`: exclusive offsets of the warps, tile count.
+  const int d = tid;
+  uint32_t count = 0;
+#pragma unroll
+  for (int w = 0; w < WARPS; ++w) {
+    const uint32_t c = s_whist[w][d];
+    s_whist[w][d] = count;
+    count += c;
+  }
+  // Decoupled look-back over the same digit of earlier tiles.
+  uint32_t* stat = a.status + ((int64_t)pass * a.n_tiles) * R;
+  uint32_t excl = 0;
+  if (tile == 0) {
+    st_release_u32(&stat[d], kStatP | count);
+  } else {
+    st_release_u32(&stat[tile * R + d], kStatA | count);
+    int64_t j = tile - 1;
+    unsigned spins = 0;
+    for (;;) {
+      const unsigned s = ld_acquire_u32(&stat[j * R + d]);
+      if ((s >> 30) == 0u) {
+        if (++spins > kSpinLimit) {
+          atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
+          break;
+        }
+        __nanosleep(16);
+        continue;
+      }
+      excl += s & kCountMask;
+      if ((s >> 30) == 2u || j == 0) break;
+      --j;
+    }
+    st_release_u32(&stat[tile * R + d], kStatP | (excl + count));
+  }
+  // Exclusive scan of the tile's counts over digits.
+  uint32_t incl = count;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_tmp[warp] = incl;
+  __syncthreads();
+  uint32_t wpre = 0;
+#pragma unroll
+  for (int w = 0; w < WARPS; ++w) wpre += (w < warp) ? s_tmp[w] : 0u;
+  const uint32_t tex = wpre + incl - count;
+  s_tile_excl[d] = tex;
+  s_gbase[d] = a.plan[kPlanStarts + pass * R + d] + excl - tex;
+  __syncthreads();
+  // Stage the tile in digit order.
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i) {
+    const int local = warp * (32 * ITEMS) + i * 32 + lane;
+    if (local < tile_n) {
+      const unsigned dd = (unsigned)((key[i] >> shift) & 255u);
+      const uint32_t p = s_tile_excl[dd] + s_whist[warp][dd] + rank[i];
+      skeys[p] = key[i];
+      svals[p] = val[i];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    const int p = j * THREADS + tid;
+    if (p < tile_n) {
+      const uint64_t k = skeys[p];
+      const unsigned dd = (unsigned)((k >> shift) & 255u);
+      const int64_t o = (int64_t)s_gbase[dd] + p;
+      kdst[o] = k;
+      pdst[o] = svals[p];
+    }
+  }
+}
+
+__global__ void k_radix_gather(StateTable* table, int64_t n, const uint64_t* keys0,
+                               const uint64_t* keys1, const uint32_t* pos0, const uint32_t* pos1,
+                               const uint32_t* plan, uint32_t* counters, const StepFlags* flag) {
+  if (!flag->unsorted) return;
+  const int fb = (int)plan[kPlanFinal];
+  const uint64_t* keys = fb ? keys1 : keys0;
+  const uint32_t* pos = fb ? pos1 : pos0;
+  const StateRef cur = table->cur, oth = table->other;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  bool tie = false;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += stride) {
+    const uint32_t q = pos[p];
+    oth.x[p] = cur.x[q];
+    oth.v[p] = cur.v[q];
+    oth.m[p] = cur.m[q];
+    oth.idx[p] = cur.idx[q];
+    if (p + 1 < n && keys[p] == keys[p + 1]) tie = true;
+  }
+  if (__syncthreads_or(tie) && threadIdx.x == 0) atomicOr(&counters[8], 1u);
+}
+
+// Equal keys: order each run by original index (insertion sort of the run).
+__global__ void k_radix_ties(StateTable* table, int64_t n, const uint64_t* keys0,
+                             const uint64_t* keys1, const uint32_t* plan,
+                             const uint32_t* counters, const StepFlags* flag) {
+  if (!flag->unsorted || !counters[8]) return;
+  const int fb = (int)plan[kPlanFinal];
+  const uint64_t* keys = fb ? keys1 : keys0;
+  const StateRef oth = table->other;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p + 1 < n; p += stride) {
+    if (keys[p] != keys[p + 1] || (p > 0 && keys[p - 1] == keys[p])) continue;
+    int64_t e = p + 1;
+    while (e + 1 < n && keys[e + 1] == keys[p]) ++e;
+    for (int64_t i = p + 1; i <= e; ++i) {
+      const double xi = oth.x[i], vi = oth.v[i], mi = oth.m[i];
+      const int32_t ii = oth.idx[i];
+      int64_t j = i - 1;
+      while (j >= p && oth.idx[j] > ii) {
+        oth.x[j + 1] = oth.x[j];
+        oth.v[j + 1] = oth.v[j];
+        oth.m[j + 1] = oth.m[j];
+        oth.idx[j + 1] = oth.idx[j];
+        --j;
+      }
+      oth.x[j + 1] = xi;
+      oth.v[j + 1] = vi;
+      oth.m[j + 1] = mi;
+      oth.idx[j + 1] = ii;
+    }
+  }
+}
+
+__global__ void k_radix_flip(StateTable* table, const StepFlags* flag) {
+  if (!flag->unsorted) return;
+  const StateRef t = table->cur;
+  table->cur = table->other;
+  table->other = t;
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+size_t radix_bytes(int64_t n) {
+  const int64_t tiles = (n + kRadixTile - 1) / kRadixTile;
+  size_t b = 0;
+  b += 2 * align256((size_t)n * 8);
+  b += 2 * align256((size_t)n * 4);
+  b += align256(8 * R * 4);
+  b += align256(kPlanWords * 4);
+  b += align256((size_t)8 * tiles * R * 4 + 16 * 4);
+  return b;
+}
+
+void radix_bind(RadixWork* w, void* base, int64_t n) {
+  char* p = static_cast<char*>(base);
+  w->n_tiles = (n + kRadixTile - 1) / kRadixTile;
+  w->keys[0] = reinterpret_cast<uint64_t*>(p); p += align256((size_t)n * 8);
+  w->keys[1] = reinterpret_cast<uint64_t*>(p); p += align256((size_t)n * 8);
+  w->pos[0] = reinterpret_cast<uint32_t*>(p); p += align256((size_t)n * 4);
+  w->pos[1] = reinterpret_cast<uint32_t*>(p); p += align256((size_t)n * 4);
+  w->hist = reinterpret_cast<uint32_t*>(p); p += align256(8 * R * 4);
+  w->plan = reinterpret_cast<uint32_t*>(p); p += align256(kPlanWords * 4);
+  w->status = reinterpret_cast<uint32_t*>(p);
+  w->counters = w->status + (size_t)8 * w->n_tiles * R;
+  w->scratch_bytes = (size_t)8 * w->n_tiles * R * 4 + 16 * 4;
+}
+
+void radix_sort_state(StateTable* table, int64_t n, RadixWork* w, const StepFlags* flag,
+                      unsigned* err, cudaStream_t s) {
+  static bool attr_set = false;
+  constexpr size_t dyn = (size_t)kRadixTile * (8 + 4);
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_radix_pass<kRadixThreads, kRadixItems>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    attr_set = true;
+  }
+  cudaMemsetAsync(w->hist, 0, 8 * R * 4, s);
+  cudaMemsetAsync(w->status, 0, w->scratch_bytes, s);
+  int hist_grid = (int)((n + 255) / 256);
+  if (hist_grid > 152 * 8) hist_grid = 152 * 8;
+  if (hist_grid < 1) hist_grid = 1;
+  k_radix_hist<<<hist_grid, 256, 0, s>>>(table, n, w->hist, flag);
+  k_radix_plan<<<1, R, 0, s>>>(n, w->hist, w->plan, flag);
+  PassArgs a;
+  a.table = table;
+  a.n = n;
+  a.n_tiles = w->n_tiles;
+  a.keys0 = w->keys[0];
+  a.keys1 = w->keys[1];
+  a.pos0 = w->pos[0];
+  a.pos1 = w->pos[1];
+  a.plan = w->plan;
+  a.status = w->status;
+  a.counters = w->counters;
+  a.flag = flag;
+  a.err = err;
+  for (int p = 0; p < 8; ++p) {
+    a.pass = p;
+    k_radix_pass<kRadixThreads, kRadixItems>
+        <<<(unsigned)w->n_tiles, kRadixThreads, dyn, s>>>(a);
+  }
+  int g = (int)((n + 255) / 256);
+  if (g > 152 * 16) g = 152 * 16;
+  if (g < 1) g = 1;
+  k_radix_gather<<<g, 256, 0, s>>>(table, n, w->keys[0], w->keys[1], w->pos[0], w->pos[1],
+                                   w->plan, w->counters, flag);
+  k_radix_ties<<<g, 256, 0, s>>>(table, n, w->keys[0], w->keys[1], w->plan, w->counters,
+                                 flag);
+  k_radix_flip<<<1, 1, 0, s>>>(table, flag);
+}
+
+}  // namespace wg

@@ -1,0 +1,161 @@
+"""wendy's public generator API, running the approximate integrator on the GPU.
+
+``nbody(x, v, m, dt, approx=True, nleap=..., sort='cuda', ...)`` has the
+signature, argument meaning, error behaviour and yield semantics of
+``wendy.nbody`` (wendy/wendy.py:112-206) and ``wendy._nbody_approx``
+(wendy/wendy.py:336-437): masses are multiplied by twopiG, ``totmass`` is
+numpy's sum of them, ``omega=None`` means no harmonic term, and every
+``next()`` advances one output interval of ``nleap`` leapfrog sub-steps and
+yields the same ``x, v`` arrays, updated in place, in original particle
+order (plus the elapsed time with ``full_output=True``).
+
+The sheets stay on the device between outputs; each ``next()`` is one call
+into the C ABI (include/wendy_gb300.h) followed by a copy of x and v back.
+"""
+import copy
+import ctypes
+
+import numpy
+
+from . import _lib
+from .diagnostics import energy, momentum, potential  # noqa: F401  (public API)
+from .extforce import resolve
+
+CPU_SORTS = ("quick", "merge", "tim", "qsort", "parallel")
+
+
+class Simulation:
+    """One simulation resident on the GPU (a ``wg_sim`` handle)."""
+
+    def __init__(self, x, v, m, totmass, omega2=-1., ext_force=None):
+        L = _lib.lib()
+        kind, params = resolve(ext_force)
+        self._L = L
+        self.n = len(x)
+        self._h = ctypes.c_void_p()
+        x = numpy.ascontiguousarray(x, dtype=numpy.float64)
+        v = numpy.ascontiguousarray(v, dtype=numpy.float64)
+        m = numpy.ascontiguousarray(m, dtype=numpy.float64)
+        _lib.check(L.wg_create(self.n, x, v, m, float(totmass), float(omega2), int(kind),
+                               _lib.ext_params(params), len(params), ctypes.byref(self._h)),
+                   "wg_create")
+
+    def step(self, dt_leap, nleap, t0):
+        """One output interval; ``t0`` is a ctypes.c_double updated in place.
+        Returns the device time in seconds."""
+        elapsed = ctypes.c_double(0.)
+        _lib.check(self._L.wg_step(self._h, float(dt_leap), int(nleap), ctypes.byref(t0),
+                                   ctypes.byref(elapsed)), "wg_step")
+        return elapsed.value
+
+    def download(self, x, v):
+        for arr in (x, v):
+            if not (arr.flags.c_contiguous and arr.flags.writeable and arr.dtype == numpy.float64
+                    and len(arr) == self.n):
+                raise ValueError("download buffers must be writeable contiguous float64[n]")
+        _lib.check(self._L.wg_download(self._h, x.ctypes.data, v.ctypes.data), "wg_download")
+
+    def stats(self):
+        st = _lib.WgStats()
+        _lib.check(self._L.wg_get_stats(self._h, ctypes.byref(st)), "wg_get_stats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.wg_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def nbody(x, v, m, dt, t0=0., twopiG=1., omega=None, ext_force=None, approx=False, nleap=None,
+          sort="cuda", maxcoll=100000, warn_maxcoll=False, full_output=False):
+    """Run a 1D N-body simulation (wendy/wendy.py:112-157 for the approximate path).
+
+    Only ``approx=True`` with ``sort='cuda'`` runs here; the exact
+    event-driven solver and the CPU sorts are the reference's.
+    """
+    if approx:
+        if nleap is None:
+            raise ValueError("When approx is True, the number of leapfrog steps nleap= per output "
+                             "time step needs to be set")
+        for item in _nbody_approx(x, v, m, dt, nleap, t0=t0, sort=sort, omega=omega,
+                                  ext_force=ext_force, twopiG=twopiG, full_output=full_output):
+            yield item
+    raise NotImplementedError("wendy_gb300 implements the approximate integrator (approx=True); "
+                              "the exact event-driven solver is the reference wendy's")
+
+
+def _nbody_approx(x, v, m, dt, nleap, t0=0., omega=None, ext_force=None, sort="cuda", twopiG=1.,
+                  full_output=False):
+    """Generator mirroring wendy._nbody_approx (wendy/wendy.py:336-437)."""
+    if sort != "cuda":
+        if sort in CPU_SORTS:
+            raise ValueError("sort=%r is a CPU sort of the reference wendy; wendy_gb300 runs "
+                             "sort='cuda'" % (sort,))
+        raise ValueError("unknown sort %r" % (sort,))
+    if omega is None:
+        omega2 = -1.
+    else:
+        omega2 = omega ** 2.
+    x = numpy.require(copy.copy(x), dtype=numpy.float64, requirements=["C", "W"])
+    v = numpy.require(copy.copy(v), dtype=numpy.float64, requirements=["C", "W"])
+    m = numpy.require(twopiG * copy.copy(m), dtype=numpy.float64, requirements=["C", "W"])
+    totmass = numpy.sum(m)
+    sim = Simulation(x, v, m, totmass, omega2, ext_force)
+    t = ctypes.c_double(t0)
+    dt_leap = dt / nleap
+    while True:
+        elapsed = sim.step(dt_leap, nleap, t)
+        sim.download(x, v)
+        if full_output:
+            yield (x, v, elapsed)
+        else:
+            yield (x, v)
+
+
+def accel(x, m, totmass, omega2=-1., ext_force=None, t=0.):
+    """One force evaluation at positions x (original order).
+
+    Returns (a, perm): accelerations in original order and the sort
+    permutation (perm[i] = original index of the sheet at sorted slot i),
+    the quantities of wendy's _nbody_force (wendy/wendy.c:334-384).  Masses
+    are used as given (already times twopiG).
+    """
+    L = _lib.lib()
+    kind, params = resolve(ext_force)
+    x = numpy.ascontiguousarray(x, dtype=numpy.float64)
+    m = numpy.ascontiguousarray(m, dtype=numpy.float64)
+    a = numpy.empty(len(x))
+    perm = numpy.empty(len(x), dtype=numpy.int32)
+    _lib.check(L.wg_accel(len(x), x, m, float(totmass), float(omega2), int(kind),
+                          _lib.ext_params(params), len(params), float(t), a.ctypes.data,
+                          perm.ctypes.data), "wg_accel")
+    return a, perm
+
+
+def approx_onestep(xi, x, v, m, a, totmass, dt, nleap, t0, omega2=-1., ext_force=None):
+    """The reference-shaped stateless step (wendy/wendy.c:385-418) on the GPU.
+
+    ``xi`` is a structured array with fields idx (int32) and val (float64)
+    laid out like ``struct array_w_index``; xi, x, v and a are updated in
+    place exactly as the reference's C function updates them.  Returns
+    (t0, time_elapsed).
+    """
+    L = _lib.lib()
+    kind, params = resolve(ext_force)
+    if xi.dtype != _lib.SHEET_DTYPE or not xi.flags.c_contiguous:
+        raise ValueError("xi must be a contiguous array of dtype wendy_gb300._lib.SHEET_DTYPE")
+    tc = ctypes.c_double(t0)
+    el = ctypes.c_double(0.)
+    err = ctypes.c_int(0)
+    _lib.check(L.wg_nbody_approx_onestep(len(x), xi.ctypes.data, x, v, m, a, float(totmass),
+                                         float(dt), int(nleap), ctypes.byref(tc), float(omega2),
+                                         int(kind), _lib.ext_params(params), len(params),
+                                         ctypes.byref(err), ctypes.byref(el)),
+               "wg_nbody_approx_onestep")
+    return tc.value, el.value
