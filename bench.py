@@ -41,6 +41,8 @@ WORKLOADS = {
     # name: (n, ics, ics kwargs, dt, nleap, omega, ext)
     "sech2_2p24": dict(n=1 << 24, family="sech2", kw=dict(masses="lognormal", sigma_ln=0.5),
                        dt=0.02, nleap=20, omega=1.1, ext=None),
+    "sech2_2p23": dict(n=1 << 23, family="sech2", kw=dict(masses="lognormal", sigma_ln=0.5),
+                       dt=0.02, nleap=20, omega=1.1, ext=None),
     "sech2_1e4": dict(n=10000, family="sech2", kw=dict(masses="equal"), dt=0.05, nleap=10,
                       omega=None, ext=None),
     "tophat_2p27": dict(n=1 << 27, family="tophat", kw=dict(masses="equal"), dt=0.01,
@@ -195,6 +197,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sech2_2p24", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -260,7 +263,7 @@ def main():
 
     # end to end through the reference-shaped call, page-locked host buffers
     e2e = None
-    if rank == 0 or world > 1:
+    if not args.no_e2e:
         from wendy_gb300 import _lib as LL
         xi = numpy.zeros(n, dtype=LL.SHEET_DTYPE)
         xi["idx"] = numpy.arange(n, dtype=numpy.int32)
