@@ -94,10 +94,12 @@ int wg_destroy(wg_sim *s);
 /* Average device time (seconds, CUDA events on the handle's stream) of one
    component over `reps` back-to-back launches on the resident sheets,
    without changing them: what = WG_PROF_FORCE (the fused force / kick /
-   drift kernel with dt = 0), WG_PROF_SORT (a full re-sort).  For the
-   measurement harness; no reference counterpart. */
+   drift kernel on sorted sets, dt = 0), WG_PROF_SORT (a full re-sort),
+   WG_PROF_BUCKET (the fused bucket sub-step, dt = 0; needs one wg_step
+   first).  For the measurement harness; no reference counterpart. */
 #define WG_PROF_FORCE 0
 #define WG_PROF_SORT 1
+#define WG_PROF_BUCKET 2
 int wg_profile(wg_sim *s, int what, int reps, double *avg_seconds);
 
 /* Page-lock (or release) caller memory so that downloads and uploads run

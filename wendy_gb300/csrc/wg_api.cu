@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/wendy_gb300.h"
+#include "wg_bucket.cuh"
 #include "wg_internal.cuh"
 
 using namespace wg;
@@ -16,6 +17,8 @@ using namespace wg;
 namespace {
 
 thread_local char g_last_error[512] = "";
+
+
 
 void set_error(const char* fmt, ...) {
   va_list ap;
@@ -110,6 +113,28 @@ struct wg_sim {
   double* h_t = nullptr;         // pinned host mirrors
   unsigned* h_ep = nullptr;
   StepFlags* h_flags = nullptr;
+  // bucketed layout (the fast path of wg_step)
+  void* bk = nullptr;
+  int64_t nb = 0;
+  double* bx[2] = {nullptr, nullptr};
+  double* bv[2] = {nullptr, nullptr};
+  double* bm[2] = {nullptr, nullptr};
+  int32_t* bi[2] = {nullptr, nullptr};
+  unsigned* bcnt[2] = {nullptr, nullptr};
+  uint64_t* qk[2] = {nullptr, nullptr};
+  int32_t* qi[2] = {nullptr, nullptr};
+  BucketRec* brecs = nullptr;
+  double *ox = nullptr, *ov = nullptr, *om = nullptr;
+  int32_t* oi = nullptr;
+  unsigned* ocount = nullptr;
+  unsigned* abort_word = nullptr;
+  unsigned* offs = nullptr;
+  int mode = 0;          // 0: compact sorted sets (half drift pending), 1: buckets
+  int lay = 0;           // layout holding the sheets in bucket mode
+  int qsel = 0;          // splitter array defining the next layout
+  double pending_dt = 0; // dt of the half drift the bucket layout was routed for
+  bool out_valid = false;  // x_out / v_out hold the last call's output
+  int grid_bucket = 0;
   // physics
   uint64_t T_lo = 0, T_hi = 0;
   int E = 0;
@@ -165,6 +190,7 @@ void free_sim(wg_sim* s) {
   if (!s) return;
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->big) cudaFree(s->big);
+  if (s->bk) cudaFree(s->bk);
   if (s->small) cudaFree(s->small);
   if (s->stage) cudaFree(s->stage);
   if (s->h_t) cudaFreeHost(s->h_t);
@@ -242,10 +268,63 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
     set_error("memset failed");
     return fail(WG_ERR_CUDA);
   }
+  // bucket layout: two layouts of nb buckets x capacity, counts, splitters,
+  // look-back records, the overflow list
+  s->nb = (n + kBucketTarget - 1) / kBucketTarget;
+  const int64_t nb = s->nb;
+  const size_t slots = (size_t)nb * kBucketCap;
+  const size_t bk_b = 2 * (3 * al(slots * 8) + al(slots * 4)) + 2 * al(4 * (size_t)nb) +
+                      2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
+                      al(sizeof(BucketRec) * (size_t)nb) + 3 * nd + ni + al(64) +
+                      al(4 * (size_t)nb);
+  e = cudaMalloc(&s->bk, bk_b);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaMalloc of %zu bytes for the bucket layout failed: %s", bk_b,
+              cudaGetErrorString(e));
+    return fail(WG_ERR_NOMEM);
+  }
+  p = static_cast<char*>(s->bk);
+  for (int k = 0; k < 2; ++k) {
+    s->bx[k] = reinterpret_cast<double*>(p); p += al(slots * 8);
+    s->bv[k] = reinterpret_cast<double*>(p); p += al(slots * 8);
+    s->bm[k] = reinterpret_cast<double*>(p); p += al(slots * 8);
+    s->bi[k] = reinterpret_cast<int32_t*>(p); p += al(slots * 4);
+  }
+  for (int k = 0; k < 2; ++k) {
+    s->bcnt[k] = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)nb);
+  }
+  for (int k = 0; k < 2; ++k) {
+    s->qk[k] = reinterpret_cast<uint64_t*>(p); p += al(8 * (size_t)(nb + 1));
+    s->qi[k] = reinterpret_cast<int32_t*>(p); p += al(4 * (size_t)(nb + 1));
+  }
+  s->brecs = reinterpret_cast<BucketRec*>(p); p += al(sizeof(BucketRec) * (size_t)nb);
+  s->ox = reinterpret_cast<double*>(p); p += nd;
+  s->ov = reinterpret_cast<double*>(p); p += nd;
+  s->om = reinterpret_cast<double*>(p); p += nd;
+  s->oi = reinterpret_cast<int32_t*>(p); p += ni;
+  s->ocount = reinterpret_cast<unsigned*>(p);
+  s->abort_word = s->ocount + 1;
+  p += al(64);
+  s->offs = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)nb);
+  if (cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)nb, s->stream) != cudaSuccess ||
+      cudaMemsetAsync(s->bcnt[0], 0, 4 * (size_t)nb, s->stream) != cudaSuccess ||
+      cudaMemsetAsync(s->bcnt[1], 0, 4 * (size_t)nb, s->stream) != cudaSuccess) {
+    set_error("memset failed");
+    return fail(WG_ERR_CUDA);
+  }
+  {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    per_sm = 2;
+    int64_t g = (int64_t)sms * per_sm;
+    s->grid_bucket = (int)(nb < g ? nb : g);
+  }
   rc = alloc_call_arrays(s, 64);
   if (rc != WG_OK) return fail(rc);
   s->st.n = n;
-  s->st.device_bytes = (int64_t)(total);
+  s->st.device_bytes = (int64_t)(total + bk_b);
   *out = s;
   return WG_OK;
 }
@@ -284,13 +363,13 @@ int validate_sheets(int64_t n, const double* x, const double* v, const double* m
 }
 
 // Read the device error word and the per-sub-step flags of the last call.
-int finish_call(wg_sim* s, int nleap) {
+int finish_call(wg_sim* s, int nleap, bool count_sorts = true) {
   unsigned err = 0;
   WG_CUDA(cudaMemcpyAsync(&err, s->err, 4, cudaMemcpyDeviceToHost, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(StepFlags) * (nleap + 1),
                           cudaMemcpyDeviceToHost, s->stream));
   WG_CUDA(cudaStreamSynchronize(s->stream));
-  for (int i = 0; i < nleap; ++i) {
+  for (int i = 0; i < nleap && count_sorts; ++i) {
     if (s->h_flags[i].unsorted)
       s->st.sorts_full++;
     else
@@ -348,6 +427,63 @@ int enqueue_step(wg_sim* s, double dt, int nleap, bool want_accel, double dt_las
   }
   WG_CUDA(cudaGetLastError());
   return WG_OK;
+}
+
+// Bucket layout `lay` (+ overflow list) -> compact, unsorted sheets in the
+// current sorted-state set.
+void bucket_to_compact(wg_sim* s, int lay) {
+  launch_compact(s->table, s->nb, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay], s->bcnt[lay],
+                 s->offs, s->ox, s->ov, s->om, s->oi, s->ocount, s->n, s->stream);
+  s->st.launches += 2;
+}
+
+BucketStepArgs bucket_args(wg_sim* s, int i, int nleap, double dt, double pre) {
+  BucketStepArgs a;
+  const int in = s->lay, out = 1 - s->lay;
+  a.xin = s->bx[in];
+  a.vin = s->bv[in];
+  a.min = s->bm[in];
+  a.iin = s->bi[in];
+  a.cnt_in = s->bcnt[in];
+  a.xout = s->bx[out];
+  a.vout = s->bv[out];
+  a.mout = s->bm[out];
+  a.iout = s->bi[out];
+  a.cnt_out = s->bcnt[out];
+  a.q_dest_key = s->qk[s->qsel];
+  a.q_dest_idx = s->qi[s->qsel];
+  a.q_new_key = s->qk[1 - s->qsel];
+  a.q_new_idx = s->qi[1 - s->qsel];
+  a.n = s->n;
+  a.nb = s->nb;
+  a.target = kBucketTarget;
+  a.recs = s->brecs;
+  a.epochs = s->epochs;
+  a.sub = i;
+  a.ticket = s->tickets + i;
+  a.T_lo = s->T_lo;
+  a.T_hi = s->T_hi;
+  a.E = s->E;
+  a.has_omega = s->omega2 >= 0;
+  a.omega2 = s->omega2;
+  a.ext = s->ext;
+  a.t_seq = s->t_seq;
+  const bool last = i == nleap - 1;
+  a.pre_dt = i == 0 ? pre : 0.0;
+  a.dt_kick = dt;
+  a.dt_drift = last ? dt / 2. : dt;
+  a.dest_dt = last ? dt / 2. : 0.0;
+  a.x_orig = last ? s->x_out : nullptr;
+  a.v_orig = last ? s->v_out : nullptr;
+  a.ox = s->ox;
+  a.ov = s->ov;
+  a.om = s->om;
+  a.oi = s->oi;
+  a.ocount = s->ocount;
+  a.abort = s->abort_word;
+  a.err = s->err;
+  a.flag_out = &s->flags[i + 1];
+  return a;
 }
 
 void fill_times(wg_sim* s, double dt, int nleap, double* t0) {
@@ -478,11 +614,98 @@ int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
   int rc = alloc_call_arrays(s, nleap);
   if (rc) return rc;
   fill_times(s, dt, nleap, t0);
+  for (int i = 0; i < nleap; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
+  s->epoch += (unsigned)nleap;
+  if (s->epoch > (1u << 29)) {
+    WG_CUDA(cudaMemsetAsync(s->recs, 0, sizeof(TileRec) * (size_t)s->n_tiles, s->stream));
+    WG_CUDA(cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)s->nb, s->stream));
+    s->epoch = 1;
+    for (int i = 0; i < nleap; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
+    s->epoch += (unsigned)nleap;
+  }
   WG_CUDA(cudaEventRecord(s->ev0, s->stream));
-  rc = enqueue_step(s, dt, nleap, false, dt / 2.);
-  if (rc) return rc;
+  WG_CUDA(cudaMemcpyAsync(s->t_seq, s->h_t, 8 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->epochs, s->h_ep, 4 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemsetAsync(s->flags, 0, sizeof(StepFlags) * (nleap + 1), s->stream));
+  WG_CUDA(cudaMemsetAsync(s->tickets, 0, 4 * (size_t)nleap, s->stream));
+  WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));  // overflow count and abort word
+  if (s->mode == 1 && dt != s->pending_dt) {
+    // routed for another dt: back to compact state, the half drift still pending
+    bucket_to_compact(s, s->lay);
+    s->mode = 0;
+  }
+  double pre = 0.0;
+  if (s->mode == 0) {
+    launch_drift(s->table, s->n, dt / 2., &s->flags[0], s->stream);
+    radix_sort_state(s->table, s->n, &s->radix, &s->flags[0], s->err, s->stream);
+    s->lay = 0;
+    s->qsel = 0;
+    launch_bucketize(s->table, s->n, kBucketTarget, s->nb, s->bx[0], s->bv[0], s->bm[0],
+                     s->bi[0], s->bcnt[0], s->qk[0], s->qi[0], s->bcnt[1], s->stream);
+    s->st.launches += 2 + kRadixLaunches;
+    s->st.sorts_full += 1;
+  } else {
+    pre = dt / 2.;
+  }
+  const int lay0 = s->lay;
+  for (int i = 0; i < nleap; ++i) {
+    const BucketStepArgs a = bucket_args(s, i, nleap, dt, pre);
+    launch_bucket_step(a, s->grid_bucket, s->stream);
+    s->lay = 1 - s->lay;
+    s->qsel = 1 - s->qsel;
+  }
+  s->st.launches += nleap;
+  WG_CUDA(cudaGetLastError());
+  unsigned ab[2] = {0, 0};
+  WG_CUDA(cudaMemcpyAsync(ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaStreamSynchronize(s->stream));
+  s->out_valid = true;
+  s->mode = 1;
+  s->pending_dt = dt;
+  if (ab[1] != 0) {
+    // sub-step k overflowed a bucket: its sheets are complete in the layout it
+    // wrote plus the overflow list.  Re-sort from scratch and finish the call
+    // on the compact path.
+    const int k = (int)ab[1] - 1;
+    s->st.sorts_full += 1;
+    const int lay_k = (k % 2 == 0) ? 1 - lay0 : lay0;
+    bucket_to_compact(s, lay_k);
+    s->mode = 0;
+    if (k < nleap - 1) {
+      ForceArgs f;
+      f.table = s->table;
+      f.n = s->n;
+      f.T_lo = s->T_lo;
+      f.T_hi = s->T_hi;
+      f.E = s->E;
+      f.has_omega = s->omega2 >= 0;
+      f.omega2 = s->omega2;
+      f.ext = s->ext;
+      f.t_seq = s->t_seq;
+      f.epochs = s->epochs;
+      f.recs = s->recs;
+      f.err = s->err;
+      f.a_out = nullptr;
+      StepFlags one{1u, 0u, 0ull};
+      for (int i = k + 1; i < nleap; ++i) {
+        WG_CUDA(cudaMemcpyAsync(&s->flags[i], &one, sizeof(one), cudaMemcpyHostToDevice,
+                                s->stream));
+        radix_sort_state(s->table, s->n, &s->radix, &s->flags[i], s->err, s->stream);
+        f.sub = i;
+        f.dt_kick = dt;
+        f.dt_drift = (i == nleap - 1) ? dt / 2. : dt;
+        f.ticket = s->tickets + i;
+        f.flag_out = &s->flags[i + 1];
+        launch_force(f, s->n_tiles, s->stream);
+        WG_CUDA(cudaStreamSynchronize(s->stream));  // pageable `one` stays valid
+      }
+      s->st.launches += (int64_t)(nleap - k - 1) * (1 + kRadixLaunches);
+      s->out_valid = false;
+    }
+  }
+  s->st.sorts_window += ab[1] ? (int64_t)ab[1] : (int64_t)nleap;
   WG_CUDA(cudaEventRecord(s->ev1, s->stream));
-  rc = finish_call(s, nleap);
+  rc = finish_call(s, nleap, false);
   float ms = 0;
   cudaEventElapsedTime(&ms, s->ev0, s->ev1);
   if (time_elapsed) *time_elapsed = ms * 1e-3;
@@ -501,7 +724,10 @@ int wg_download(wg_sim* s, double* x, double* v) {
     set_error("null simulation");
     return WG_ERR_ARG;
   }
-  launch_desort(s->table, s->n, s->x_out, s->v_out, s->stream);
+  if (!s->out_valid) {
+    launch_desort(s->table, s->n, s->x_out, s->v_out, s->stream);
+    s->out_valid = true;
+  }
   if (x) WG_CUDA(cudaMemcpyAsync(x, s->x_out, 8 * s->n, cudaMemcpyDeviceToHost, s->stream));
   if (v) WG_CUDA(cudaMemcpyAsync(v, s->v_out, 8 * s->n, cudaMemcpyDeviceToHost, s->stream));
   WG_CUDA(cudaStreamSynchronize(s->stream));
@@ -523,8 +749,13 @@ int wg_destroy(wg_sim* s) {
 }
 
 int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
-  if (!s || reps < 1 || !avg_seconds || (what != WG_PROF_FORCE && what != WG_PROF_SORT)) {
+  if (!s || reps < 1 || !avg_seconds ||
+      (what != WG_PROF_FORCE && what != WG_PROF_SORT && what != WG_PROF_BUCKET)) {
     set_error("bad arguments to wg_profile");
+    return WG_ERR_ARG;
+  }
+  if (what == WG_PROF_BUCKET && s->mode != 1) {
+    set_error("wg_profile(WG_PROF_BUCKET) needs the bucket layout: run wg_step first");
     return WG_ERR_ARG;
   }
   int rc = alloc_call_arrays(s, reps);
@@ -558,10 +789,25 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   a.dt_kick = 0.0;
   a.dt_drift = 0.0;
   a.flag_out = &s->flags[s->cap];  // scratch slot
+  WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));
   WG_CUDA(cudaStreamSynchronize(s->stream));
+  const int lay_start = s->lay;
   WG_CUDA(cudaEventRecord(s->ev0, s->stream));
   for (int i = 0; i < reps; ++i) {
-    if (what == WG_PROF_FORCE) {
+    if (what == WG_PROF_BUCKET) {
+      // dt = 0 keeps x and v; routing by x + (pending_dt / 2) v keeps the
+      // layout's meaning, so the handle stays ready for the next wg_step
+      BucketStepArgs b = bucket_args(s, i, reps, 0.0, 0.0);
+      b.dt_kick = 0.0;
+      b.dt_drift = 0.0;
+      b.dest_dt = s->pending_dt / 2.;
+      b.x_orig = nullptr;
+      b.v_orig = nullptr;
+      b.flag_out = &s->flags[s->cap];
+      launch_bucket_step(b, s->grid_bucket, s->stream);
+      s->lay = 1 - s->lay;
+      s->qsel = 1 - s->qsel;
+    } else if (what == WG_PROF_FORCE) {
       a.sub = i;
       a.ticket = s->tickets + i;
       launch_force(a, s->n_tiles, s->stream);
@@ -575,7 +821,14 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   float ms = 0;
   WG_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
   *avg_seconds = ms * 1e-3 / reps;
-  s->st.launches += what == WG_PROF_FORCE ? reps : (int64_t)reps * kRadixLaunches;
+  s->st.launches += what == WG_PROF_SORT ? (int64_t)reps * kRadixLaunches : reps;
+  unsigned ab[2] = {0, 0};
+  WG_CUDA(cudaMemcpy(ab, s->ocount, 8, cudaMemcpyDeviceToHost));
+  if (ab[1]) {
+    // a bucket overflowed while profiling: fall back to the compact state
+    bucket_to_compact(s, ((ab[1] - 1) % 2 == 0) ? 1 - lay_start : lay_start);
+    s->mode = 0;
+  }
   unsigned err = 0;
   WG_CUDA(cudaMemcpy(&err, s->err, 4, cudaMemcpyDeviceToHost));
   if (err) {
