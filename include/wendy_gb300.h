@@ -131,6 +131,26 @@ int wg_nbody_approx_onestep(int n, wg_sheet *xi, double *x, double *v, const dou
                             double omega2, int ext_kind, const double *ext_params,
                             int n_ext_params, int *err, double *time_elapsed);
 
+/* Allocation-free force evaluation (no counterpart in the reference).
+   For callers that cannot call cudaMalloc themselves or let this library do
+   so: an application whose device memory belongs to another framework's
+   allocator and budget, code that must not trigger the device-wide
+   synchronisation cudaMalloc and cudaFree imply, or a latency-critical loop
+   that may not allocate.  Same result as wg_accel, but x, m, a and perm are
+   DEVICE pointers the caller owns (a or perm may be NULL), the work runs on
+   `stream` (a cudaStream_t; NULL = legacy default stream), and the call
+   returns after that stream has finished it.  All intermediates live in one
+   fixed __device__ array of this library (8 MiB, held by every GPU that loads
+   the library until the process exits), so n is limited to
+   WG_NOALLOC_MAX_SHEETS; larger n returns WG_ERR_ARG.  The first call on a
+   device looks up the array's device address (cudaGetSymbolAddress): make
+   that first call before any stream capture.  All calls share the array:
+   calls that overlap on the GPU (other streams or host threads) race. */
+#define WG_NOALLOC_MAX_SHEETS 65536
+int wg_accel_noalloc(int64_t n, const double *x, const double *m, double totmass,
+                     double omega2, int ext_kind, const double *ext_params, int n_ext_params,
+                     double t, double *a, int32_t *perm, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,7 +23,11 @@ EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH = 0, 1, 2
 # Every symbol include/wendy_gb300.h declares.
 EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", "wg_create",
            "wg_step", "wg_download", "wg_get_stats", "wg_destroy", "wg_accel",
-           "wg_nbody_approx_onestep", "wg_profile", "wg_host_register", "wg_host_unregister")
+           "wg_nbody_approx_onestep", "wg_profile", "wg_host_register", "wg_host_unregister",
+           "wg_accel_noalloc")
+
+# Largest n wg_accel_noalloc accepts (its fixed device scratch array).
+NOALLOC_MAX_SHEETS = 65536
 
 
 class WgSheet(ctypes.Structure):
@@ -92,6 +96,7 @@ def lib():
     L.wg_profile.argtypes = [_P, _I, _I, ctypes.POINTER(_D)]
     L.wg_host_register.argtypes = [_P, _I64]
     L.wg_host_unregister.argtypes = [_P]
+    L.wg_accel_noalloc.argtypes = [_I64, _P, _P, _D, _D, _I, _F64, _I, _D, _P, _P, _P]
     for name in EXPORTS:
         if name not in ("wg_status_string", "wg_last_error"):
             getattr(L, name).restype = _I

@@ -18,7 +18,13 @@ namespace {
 
 thread_local char g_last_error[512] = "";
 
+}  // namespace
 
+void wg::record_last_error(const char* msg) {
+  std::snprintf(g_last_error, sizeof(g_last_error), "%s", msg);
+}
+
+namespace {
 
 void set_error(const char* fmt, ...) {
   va_list ap;

@@ -90,6 +90,9 @@ void launch_scatter_accel(const StateTable* table, int64_t n, const double* a_so
                           double* a_orig, cudaStream_t s);
 void launch_init_state(StateTable* table, int64_t n, cudaStream_t s);
 
+// Record a message for wg_last_error() (wg_api.cu).
+void record_last_error(const char* msg);
+
 // --- launchers (wg_radix.cu) ---
 constexpr int kRadixLaunches = 13;  // kernels radix_sort_state enqueues (hist, plan, 8 passes,
                                     // gather, ties, flip)
