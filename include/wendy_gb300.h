@@ -131,6 +131,37 @@ int wg_nbody_approx_onestep(int n, wg_sheet *xi, double *x, double *v, const dou
                             double omega2, int ext_kind, const double *ext_params,
                             int n_ext_params, int *err, double *time_elapsed);
 
+/* ---- ensembles: many simulations resident on one GPU -------------------
+   A pool holds any number of simulations (sheets, bucket layouts and
+   look-back state of each in its own device allocation) and advances any
+   subset of them by one output interval with one launch of the fused
+   sub-step kernel per leapfrog sub-step.  Each simulation's arithmetic is
+   that of _wendy_nbody_approx_onestep (wendy/wendy.c:385-418) and its result
+   is bit-identical to running it alone; the reference itself has no
+   ensemble API.  Simulations can be added and removed between steps
+   (continuous batching). */
+typedef struct wg_pool wg_pool;
+
+/* Device bytes a simulation of n sheets holds in a pool (admission control). */
+int64_t wg_pool_sim_bytes(int64_t n);
+/* budget_bytes > 0 caps the bytes of all simulations (wg_pool_add returns
+   WG_ERR_BUDGET beyond it); 0 = no cap. */
+int wg_pool_create(int64_t budget_bytes, wg_pool **out);
+/* Same inputs as wg_create; returns the simulation's id. */
+int wg_pool_add(wg_pool *p, int64_t n, const double *x, const double *v, const double *m,
+                double totmass, double omega2, int ext_kind, const double *ext_params,
+                int n_ext_params, int *sim_id);
+int wg_pool_remove(wg_pool *p, int sim_id);
+/* Advance the `count` simulations ids[] by nleap sub-steps each (dt[k] is
+   simulation k's dt_leap; t0[k] advances as in wg_step; t0 may be NULL). */
+int wg_pool_step(wg_pool *p, int count, const int *ids, const double *dt, int nleap, double *t0,
+                 double *time_elapsed);
+/* Positions and velocities of the last step, original order. */
+int wg_pool_download(wg_pool *p, int sim_id, double *x, double *v);
+int wg_pool_info(wg_pool *p, int64_t *used_bytes, int64_t *budget_bytes, int *n_sims,
+                 int64_t *launches);
+int wg_pool_destroy(wg_pool *p);
+
 /* Allocation-free force evaluation (no counterpart in the reference).
    For callers that cannot call cudaMalloc themselves or let this library do
    so: an application whose device memory belongs to another framework's

@@ -1,0 +1,102 @@
+"""Ensembles on one GPU: each simulation bit-identical to its solo run."""
+import ctypes
+
+import numpy
+import pytest
+
+import wendy_gb300
+from oracle import oracle as O
+from wendy_gb300 import ics
+from wendy_gb300.ensemble import Pool
+from wendy_gb300.extforce import Harmonic, PulseTanh
+
+pytestmark = pytest.mark.gpu
+
+CASES = [  # (n, family, seed, dt_leap, omega, ext)
+    (1, "gaussian", 1, 0.01, None, None),
+    (7, "sech2", 2, 0.004, 1.1, None),
+    (500, "tophat", 3, 0.001, None, PulseTanh(0.3, 5.0, 1.0, 0.5)),
+    (3000, "gaussian", 4, 0.002, 0.5, None),
+    (20000, "sech2", 5, 0.003, None, Harmonic(0.7)),
+    (70001, "sech2", 6, 0.001, 1.1, None),
+]
+
+
+def _solo(n, fam, seed, dt, omega, ext, nleap, nout):
+    x, v, m = ics.FAMILIES[fam](n, seed=seed)
+    omega2 = -1. if omega is None else omega ** 2
+    sim = wendy_gb300.Simulation(x, v, m, numpy.sum(m), omega2, ext)
+    t = ctypes.c_double(4.0)
+    outs = []
+    for _ in range(nout):
+        sim.step(dt, nleap, t)
+        gx, gv = numpy.empty(n), numpy.empty(n)
+        sim.download(gx, gv)
+        outs.append((gx, gv))
+    return outs, t.value
+
+
+def test_ensemble_matches_solo_bit_for_bit():
+    nleap, nout = 5, 3
+    with Pool() as pool:
+        ids = []
+        for n, fam, seed, dt, omega, ext in CASES:
+            x, v, m = ics.FAMILIES[fam](n, seed=seed)
+            ids.append(pool.add(x, v, m, omega=omega, ext_force=ext))
+        dts = numpy.array([c[3] for c in CASES])
+        t0 = numpy.full(len(CASES), 4.0)
+        got = [[] for _ in CASES]
+        for _ in range(nout):
+            pool.step(ids, dts, nleap, t0)
+            for k, sid in enumerate(ids):
+                got[k].append(pool.download(sid))
+    for k, (n, fam, seed, dt, omega, ext) in enumerate(CASES):
+        solo, tsolo = _solo(n, fam, seed, dt, omega, ext, nleap, nout)
+        assert t0[k] == tsolo
+        for (gx, gv), (sx, sv) in zip(got[k], solo):
+            assert numpy.array_equal(gx, sx) and numpy.array_equal(gv, sv), (n, fam)
+
+
+def test_ensemble_matches_oracle():
+    n, dt, nleap = 4000, 0.002, 8
+    x, v, m = ics.sech2_disk(n, seed=11, masses="lognormal")
+    with Pool() as pool:
+        a = pool.add(x, v, m, omega=1.1)
+        b = pool.add(x[:900], v[:900], m[:900])
+        pool.step([a, b], [dt, dt], nleap)
+        gx, gv = pool.download(a)
+    r = O.nbody_approx(x, v, m, dt * nleap, nleap, omega=1.1)
+    rx, rv = next(r)
+    assert numpy.max(numpy.abs(gx - rx)) <= 1e-10
+    assert numpy.max(numpy.abs(gv - rv)) <= 1e-10
+
+
+def test_members_join_and_leave_without_changing_results():
+    nleap = 4
+    x, v, m = ics.sech2_disk(12000, seed=21)
+    xo, vo, mo = ics.top_hat(5000, seed=22)
+    with Pool() as alone, Pool() as mixed:
+        a = alone.add(x, v, m)
+        b = mixed.add(x, v, m)
+        other = mixed.add(xo, vo, mo)
+        for k in range(4):
+            alone.step([a], [0.002], nleap)
+            if k == 1:
+                mixed.remove(other)
+                other = mixed.add(xo[:3000], vo[:3000], mo[:3000])
+            ids = [other, b] if k % 2 else [b, other]
+            mixed.step(ids, [0.002, 0.002], nleap)
+            ax, av = alone.download(a)
+            bx, bv = mixed.download(b)
+            assert numpy.array_equal(ax, bx) and numpy.array_equal(av, bv), k
+
+
+def test_budget_is_enforced():
+    need = Pool.sim_bytes(10000)
+    with Pool(budget_bytes=int(need * 1.5)) as pool:
+        x, v, m = ics.sech2_disk(10000, seed=3)
+        pool.add(x, v, m)
+        with pytest.raises(wendy_gb300._lib.WendyGPUError) as e:
+            pool.add(x, v, m)
+        assert e.value.status == -6
+        assert pool.info()["sims"] == 1

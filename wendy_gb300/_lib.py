@@ -24,7 +24,9 @@ EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH = 0, 1, 2
 EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", "wg_create",
            "wg_step", "wg_download", "wg_get_stats", "wg_destroy", "wg_accel",
            "wg_nbody_approx_onestep", "wg_profile", "wg_host_register", "wg_host_unregister",
-           "wg_accel_noalloc")
+           "wg_accel_noalloc", "wg_pool_sim_bytes", "wg_pool_create", "wg_pool_add",
+           "wg_pool_remove", "wg_pool_step", "wg_pool_download", "wg_pool_info",
+           "wg_pool_destroy")
 
 # Largest n wg_accel_noalloc accepts (its fixed device scratch array).
 NOALLOC_MAX_SHEETS = 65536
@@ -97,9 +99,20 @@ def lib():
     L.wg_host_register.argtypes = [_P, _I64]
     L.wg_host_unregister.argtypes = [_P]
     L.wg_accel_noalloc.argtypes = [_I64, _P, _P, _D, _D, _I, _F64, _I, _D, _P, _P, _P]
+    L.wg_pool_sim_bytes.argtypes = [_I64]
+    L.wg_pool_create.argtypes = [_I64, ctypes.POINTER(_P)]
+    L.wg_pool_add.argtypes = [_P, _I64, _F64, _F64, _F64, _D, _D, _I, _F64, _I,
+                              ctypes.POINTER(_I)]
+    L.wg_pool_remove.argtypes = [_P, _I]
+    L.wg_pool_step.argtypes = [_P, _I, _P, _P, _I, _P, ctypes.POINTER(_D)]
+    L.wg_pool_download.argtypes = [_P, _I, _P, _P]
+    L.wg_pool_info.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                               ctypes.POINTER(_I), ctypes.POINTER(_I64)]
+    L.wg_pool_destroy.argtypes = [_P]
     for name in EXPORTS:
         if name not in ("wg_status_string", "wg_last_error"):
             getattr(L, name).restype = _I
+    L.wg_pool_sim_bytes.restype = _I64
     _lib = L
     return L
 

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_wendy_gb300.so")
 BUILD_DIR = os.path.join(HERE, "_build")
-SOURCES = ["wg_kernels.cu", "wg_radix.cu", "wg_bucket.cu", "wg_api.cu", "wg_noalloc.cu"]
+SOURCES = ["wg_kernels.cu", "wg_radix.cu", "wg_bucket.cu", "wg_api.cu", "wg_pool.cu", "wg_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

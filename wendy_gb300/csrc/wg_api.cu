@@ -141,6 +141,9 @@ struct wg_sim {
   double pending_dt = 0; // dt of the half drift the bucket layout was routed for
   bool out_valid = false;  // x_out / v_out hold the last call's output
   int grid_bucket = 0;
+  SimDev dev{};                  // host copy of the kernel's view of this simulation
+  SimDev* d_dev = nullptr;       // device copy (one entry)
+  BucketTask* d_tasks = nullptr; // [nb]: (0, b)
   // physics
   uint64_t T_lo = 0, T_hi = 0;
   int E = 0;
@@ -282,7 +285,7 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
   const size_t bk_b = 2 * (3 * al(slots * 8) + al(slots * 4)) + 2 * al(4 * (size_t)nb) +
                       2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
                       al(sizeof(BucketRec) * (size_t)nb) + 3 * nd + ni + al(64) +
-                      al(4 * (size_t)nb);
+                      al(4 * (size_t)nb) + al(sizeof(SimDev)) + al(sizeof(BucketTask) * (size_t)nb);
   e = cudaMalloc(&s->bk, bk_b);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -313,6 +316,17 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
   s->abort_word = s->ocount + 1;
   p += al(64);
   s->offs = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)nb);
+  s->d_dev = reinterpret_cast<SimDev*>(p); p += al(sizeof(SimDev));
+  s->d_tasks = reinterpret_cast<BucketTask*>(p); p += al(sizeof(BucketTask) * (size_t)nb);
+  {
+    std::vector<BucketTask> tasks((size_t)nb);
+    for (int64_t b = 0; b < nb; ++b) tasks[(size_t)b] = BucketTask{0, (int)b};
+    if (cudaMemcpy(s->d_tasks, tasks.data(), sizeof(BucketTask) * (size_t)nb,
+                   cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("upload of the bucket task list failed");
+      return fail(WG_ERR_CUDA);
+    }
+  }
   if (cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)nb, s->stream) != cudaSuccess ||
       cudaMemsetAsync(s->bcnt[0], 0, 4 * (size_t)nb, s->stream) != cudaSuccess ||
       cudaMemsetAsync(s->bcnt[1], 0, 4 * (size_t)nb, s->stream) != cudaSuccess) {
@@ -323,9 +337,8 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    per_sm = 2;
-    int64_t g = (int64_t)sms * per_sm;
-    s->grid_bucket = (int)(nb < g ? nb : g);
+    (void)per_sm;
+    s->grid_bucket = bucket_step_grid(sms);
   }
   rc = alloc_call_arrays(s, 64);
   if (rc != WG_OK) return fail(rc);
@@ -443,53 +456,54 @@ void bucket_to_compact(wg_sim* s, int lay) {
   s->st.launches += 2;
 }
 
-BucketStepArgs bucket_args(wg_sim* s, int i, int nleap, double dt, double pre) {
-  BucketStepArgs a;
-  const int in = s->lay, out = 1 - s->lay;
-  a.xin = s->bx[in];
-  a.vin = s->bv[in];
-  a.min = s->bm[in];
-  a.iin = s->bi[in];
-  a.cnt_in = s->bcnt[in];
-  a.xout = s->bx[out];
-  a.vout = s->bv[out];
-  a.mout = s->bm[out];
-  a.iout = s->bi[out];
-  a.cnt_out = s->bcnt[out];
-  a.q_dest_key = s->qk[s->qsel];
-  a.q_dest_idx = s->qi[s->qsel];
-  a.q_new_key = s->qk[1 - s->qsel];
-  a.q_new_idx = s->qi[1 - s->qsel];
-  a.n = s->n;
-  a.nb = s->nb;
-  a.target = kBucketTarget;
-  a.recs = s->brecs;
-  a.epochs = s->epochs;
-  a.sub = i;
-  a.ticket = s->tickets + i;
-  a.T_lo = s->T_lo;
-  a.T_hi = s->T_hi;
-  a.E = s->E;
-  a.has_omega = s->omega2 >= 0;
-  a.omega2 = s->omega2;
-  a.ext = s->ext;
-  a.t_seq = s->t_seq;
-  const bool last = i == nleap - 1;
-  a.pre_dt = i == 0 ? pre : 0.0;
-  a.dt_kick = dt;
-  a.dt_drift = last ? dt / 2. : dt;
-  a.dest_dt = last ? dt / 2. : 0.0;
-  a.x_orig = last ? s->x_out : nullptr;
-  a.v_orig = last ? s->v_out : nullptr;
-  a.ox = s->ox;
-  a.ov = s->ov;
-  a.om = s->om;
-  a.oi = s->oi;
-  a.ocount = s->ocount;
-  a.abort = s->abort_word;
-  a.err = s->err;
-  a.flag_out = &s->flags[i + 1];
-  return a;
+// The kernel's view of this simulation for the coming call.
+void fill_dev(wg_sim* s, double dt, double pre) {
+  SimDev& d = s->dev;
+  for (int k = 0; k < 2; ++k) {
+    d.bx[k] = s->bx[k];
+    d.bv[k] = s->bv[k];
+    d.bm[k] = s->bm[k];
+    d.bi[k] = s->bi[k];
+    d.bcnt[k] = s->bcnt[k];
+    d.qk[k] = s->qk[k];
+    d.qi[k] = s->qi[k];
+  }
+  d.recs = s->brecs;
+  d.ox = s->ox;
+  d.ov = s->ov;
+  d.om = s->om;
+  d.oi = s->oi;
+  d.ocount = s->ocount;
+  d.x_out = s->x_out;
+  d.v_out = s->v_out;
+  d.flags = s->flags;
+  d.t_seq = s->t_seq;
+  d.n = s->n;
+  d.nb = s->nb;
+  d.T_lo = s->T_lo;
+  d.T_hi = s->T_hi;
+  d.E = s->E;
+  d.has_omega = s->omega2 >= 0;
+  d.omega2 = s->omega2;
+  d.ext = s->ext;
+  d.dt = dt;
+  d.pre_dt = pre;
+  d.lay0 = s->lay;
+  d.qsel0 = s->qsel;
+}
+
+StepLaunch step_launch(wg_sim* s, int i, int nleap, int profile) {
+  StepLaunch L;
+  L.sims = s->d_dev;
+  L.tasks = s->d_tasks;
+  L.ntasks = (int)s->nb;
+  L.sub = i;
+  L.nleap = nleap;
+  L.epochs = s->epochs;
+  L.ticket = s->tickets + i;
+  L.err = s->err;
+  L.profile = profile;
+  return L;
 }
 
 void fill_times(wg_sim* s, double dt, int nleap, double* t0) {
@@ -654,12 +668,11 @@ int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
     pre = dt / 2.;
   }
   const int lay0 = s->lay;
-  for (int i = 0; i < nleap; ++i) {
-    const BucketStepArgs a = bucket_args(s, i, nleap, dt, pre);
-    launch_bucket_step(a, s->grid_bucket, s->stream);
-    s->lay = 1 - s->lay;
-    s->qsel = 1 - s->qsel;
-  }
+  fill_dev(s, dt, pre);
+  WG_CUDA(cudaMemcpyAsync(s->d_dev, &s->dev, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream));
+  for (int i = 0; i < nleap; ++i) launch_bucket_step(step_launch(s, i, nleap, 0), s->grid_bucket, s->stream);
+  s->lay = (lay0 + nleap) & 1;
+  s->qsel = (s->qsel + nleap) & 1;
   s->st.launches += nleap;
   WG_CUDA(cudaGetLastError());
   unsigned ab[2] = {0, 0};
@@ -693,6 +706,8 @@ int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
       f.err = s->err;
       f.a_out = nullptr;
       StepFlags one{1u, 0u, 0ull};
+      // the bucket launches of these sub-steps consumed their tickets
+      WG_CUDA(cudaMemsetAsync(s->tickets + k + 1, 0, 4 * (size_t)(nleap - k - 1), s->stream));
       for (int i = k + 1; i < nleap; ++i) {
         WG_CUDA(cudaMemcpyAsync(&s->flags[i], &one, sizeof(one), cudaMemcpyHostToDevice,
                                 s->stream));
@@ -798,21 +813,15 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));
   WG_CUDA(cudaStreamSynchronize(s->stream));
   const int lay_start = s->lay;
+  if (what == WG_PROF_BUCKET) {
+    fill_dev(s, 0.0, 0.0);
+    WG_CUDA(cudaMemcpyAsync(s->d_dev, &s->dev, sizeof(SimDev), cudaMemcpyHostToDevice,
+                            s->stream));
+  }
   WG_CUDA(cudaEventRecord(s->ev0, s->stream));
   for (int i = 0; i < reps; ++i) {
     if (what == WG_PROF_BUCKET) {
-      // dt = 0 keeps x and v; routing by x + (pending_dt / 2) v keeps the
-      // layout's meaning, so the handle stays ready for the next wg_step
-      BucketStepArgs b = bucket_args(s, i, reps, 0.0, 0.0);
-      b.dt_kick = 0.0;
-      b.dt_drift = 0.0;
-      b.dest_dt = s->pending_dt / 2.;
-      b.x_orig = nullptr;
-      b.v_orig = nullptr;
-      b.flag_out = &s->flags[s->cap];
-      launch_bucket_step(b, s->grid_bucket, s->stream);
-      s->lay = 1 - s->lay;
-      s->qsel = 1 - s->qsel;
+      launch_bucket_step(step_launch(s, i, reps, 1), s->grid_bucket, s->stream);
     } else if (what == WG_PROF_FORCE) {
       a.sub = i;
       a.ticket = s->tickets + i;
@@ -828,12 +837,19 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   WG_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
   *avg_seconds = ms * 1e-3 / reps;
   s->st.launches += what == WG_PROF_SORT ? (int64_t)reps * kRadixLaunches : reps;
-  unsigned ab[2] = {0, 0};
-  WG_CUDA(cudaMemcpy(ab, s->ocount, 8, cudaMemcpyDeviceToHost));
-  if (ab[1]) {
-    // a bucket overflowed while profiling: fall back to the compact state
-    bucket_to_compact(s, ((ab[1] - 1) % 2 == 0) ? 1 - lay_start : lay_start);
+  if (what == WG_PROF_BUCKET) {
+    // dt = 0 kept every sheet in place, but the layout is now routed by the
+    // stored positions rather than by the pending half drift: hand the
+    // sheets back to the compact state so the next wg_step re-sorts them
+    unsigned ab[2] = {0, 0};
+    WG_CUDA(cudaMemcpy(ab, s->ocount, 8, cudaMemcpyDeviceToHost));
+    const int lay_end = ab[1] ? (((ab[1] - 1) % 2 == 0) ? 1 - lay_start : lay_start)
+                              : ((lay_start + reps) & 1);
+    bucket_to_compact(s, lay_end);
+    s->lay = lay_end;
+    s->qsel = (s->qsel + reps) & 1;
     s->mode = 0;
+    WG_CUDA(cudaStreamSynchronize(s->stream));
   }
   unsigned err = 0;
   WG_CUDA(cudaMemcpy(&err, s->err, 4, cudaMemcpyDeviceToHost));

@@ -1,25 +1,33 @@
 // wg_bucket.cu -- the fused sub-step on bucketed state.
 //
-// Between sub-steps the sheets live in B buckets of fixed capacity; bucket b
-// holds exactly the sheets whose (position key, index) lies in
-// [Q_b, Q_{b+1}), in arbitrary order inside the bucket.  One kernel launch
-// per sub-step then does, per bucket (one CTA, persistent over buckets):
+// Between sub-steps the sheets of a simulation live in B buckets of fixed
+// capacity; bucket b holds exactly the sheets whose (position key, index)
+// lies in [Q_b, Q_{b+1}), in arbitrary order inside the bucket.  One kernel
+// launch per sub-step then does, per bucket (one CTA, persistent over a list
+// of (simulation, bucket) tasks):
 //
 //   load the bucket into shared memory (optionally applying the half drift
-//     a call starts with)
-//   sort it by (key, index) in shared memory: the bounded-window fix-up,
-//     since a bucket only ever receives sheets from nearby buckets
-//   exact fixed-point prefix sum of the masses plus a count prefix, with a
-//     decoupled look-back across buckets (the count gives global ranks)
-//   a = [ext(x,t) +] (totmass - 2 C - m [- omega^2 x]); kick; drift
+//     a call starts with), summing its fixed-point mass and count
+//   decoupled look-back over the earlier buckets of the same simulation for
+//     the exclusive (mass, count) prefix -- before the sort, since the sums
+//     do not depend on the order inside the bucket
+//   sort the bucket by (key, index) in shared memory: the bounded-window
+//     fix-up, since a bucket only ever receives sheets from nearby buckets
+//     (one counting-sort pass on a 12-bit order-preserving offset, equal
+//     offsets ordered by the full key; a multi-pass radix sort when the keys
+//     are too clustered for that)
+//   exact prefix of the masses in sorted order, a = [ext(x,t) +]
+//     (totmass - 2 C - m [- omega^2 x]); kick; drift
 //   publish new splitters: the keys at global ranks j*T (quantiles)
 //   route every sheet to the bucket of the next layout that covers its new
 //     key (splitters computed by the previous sub-step) and append it there
 //
 // so a sub-step reads and writes each sheet once (28 B in, 28 B out).  A
-// bucket that would overflow its capacity, or a sheet that left the search
-// window, is still placed (overflow list, global search) and the sub-step
-// is flagged so that the host re-sorts from scratch; no sheet is ever lost.
+// bucket that would overflow its capacity sends the sheet to an overflow
+// list and flags the simulation, whose host side then re-sorts from scratch;
+// no sheet is ever lost.  Simulations never interact: every sum, sort and
+// splitter is per simulation, so a simulation gives the same bits alone and
+// in an ensemble.
 //
 // Reference: _nbody_force and leapfrog_leappq, wendy/wendy.c:324-384; the
 // argsort at wendy/wendy.c:341-357 is what the bucket sort replaces.
@@ -33,11 +41,18 @@ namespace {
 
 constexpr int BT = kBucketThreads;  // 256
 constexpr int CAP = kBucketCap;     // 2048
-constexpr int ITEMS = CAP / BT;     // 8
+constexpr int MAXI = CAP / BT;      // 8 sheets per thread at most
 constexpr int WARPS = BT / 32;
-constexpr int RWIN = kSplitterWindow;  // splitters searched in shared memory on each side
+constexpr int RWIN = kSplitterWindow;
+constexpr int QB = 12;              // bits of the counting-sort offset
+constexpr int NBIN = 1 << QB;       // 4096 bins
+constexpr int MAXBIN = 48;          // a fuller bin sends the bucket to the radix sort
+// Bins are padded with one word per 32 so that a thread scanning 16
+// consecutive bins and its 31 neighbours hit 32 different banks.
+constexpr int NBIN_PAD = NBIN + NBIN / 32 + 1;
+__device__ __forceinline__ int binp(int b) { return b + (b >> 5); }
 
-struct SortSmem {
+struct LsdSmem {
   uint32_t q[2][CAP];
   uint16_t p[2][CAP];
   uint32_t hist[WARPS][256];
@@ -49,24 +64,27 @@ struct StepSmem {
   double m[CAP];
   uint64_t key[CAP];
   int32_t idx[CAP];
-  SortSmem sort;
+  uint16_t perm[CAP];  // sorted position -> slot
+  union {
+    uint32_t bins[NBIN_PAD];
+    LsdSmem lsd;
+  } u;
   uint64_t wkey[2 * RWIN + 2];
   int32_t widx[2 * RWIN + 2];
   uint32_t dcount[2 * RWIN + 2];
   uint32_t dbase[2 * RWIN + 2];
   u128 warp_mass[WARPS];
   uint32_t warp_cnt[WARPS];
+  uint32_t scan_tmp[WARPS];
   u128 prefix_mass;
   uint32_t prefix_cnt;
   uint64_t red_min[WARPS], red_max[WARPS];
-  unsigned bucket;
-  int n;
+  unsigned task;
+  int sim;
+  int64_t bucket;
   int win_lo, win_hi;
-  int any_tie;
-  int perm_buf;
   double amp;
   unsigned epoch;
-  unsigned flags;
   unsigned long long maxv;
 };
 
@@ -74,117 +92,191 @@ __device__ __forceinline__ bool pair_less(uint64_t k1, int32_t i1, uint64_t k2, 
   return k1 < k2 || (k1 == k2 && i1 < i2);
 }
 
-// Sort the n <= CAP sheets of the bucket by (key, idx).  Keys are first
-// mapped to 32-bit order-preserving offsets ((key - kmin) >> shift) and
-// radix-sorted, stable, 8 bits per pass, only over the bits that differ;
-// equal offsets are then ordered by the full (key, idx) pair.  Leaves the
-// permutation (sorted position -> slot) in sort.p[*perm_buf].
-__device__ void bucket_sort(StepSmem& S, int n, uint64_t kmin, uint64_t kmax) {
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and (through total) the block total.  Contains barriers.
+__device__ __forceinline__ uint32_t block_excl_scan(StepSmem& S, uint32_t v, uint32_t& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) S.scan_tmp[warp] = incl;
+  __syncthreads();
+  uint32_t pre = 0;
+  total = 0;
+#pragma unroll
+  for (int w = 0; w < WARPS; ++w) {
+    const uint32_t t = S.scan_tmp[w];
+    pre += (w < warp) ? t : 0u;
+    total += t;
+  }
+  __syncthreads();
+  return pre + incl - v;
+}
+
+// Multi-pass fallback: stable LSD radix sort of 32-bit order-preserving
+// offsets, 8 bits per pass over the bits that differ, then exact tie order.
+__device__ void lsd_sort(StepSmem& S, int n, uint64_t kmin, uint64_t kmax) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t span = kmax - kmin;
   const int bits = span ? 64 - __clzll((long long)span) : 0;
   const int shift = bits > 32 ? bits - 32 : 0;
   const int passes = (bits - shift + 7) / 8;
+  LsdSmem& L = S.u.lsd;
+  __syncthreads();  // the union was just used as counting-sort bins
   for (int j = tid; j < n; j += BT) {
-    S.sort.q[0][j] = (uint32_t)((S.key[j] - kmin) >> shift);
-    S.sort.p[0][j] = (uint16_t)j;
+    L.q[0][j] = (uint32_t)((S.key[j] - kmin) >> shift);
+    L.p[0][j] = (uint16_t)j;
   }
   int cur = 0;
   __syncthreads();
   for (int pass = 0; pass < passes; ++pass) {
     const int ds = 8 * pass;
-    for (int i = lane; i < 256; i += 32) S.sort.hist[warp][i] = 0;
+    for (int i = lane; i < 256; i += 32) L.hist[warp][i] = 0;
     __syncwarp();
-    uint32_t rank[ITEMS];
-    unsigned dig[ITEMS];
+    uint32_t rank[MAXI];
+    unsigned dig[MAXI];
 #pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      const int j = warp * (32 * ITEMS) + i * 32 + lane;
+    for (int i = 0; i < MAXI; ++i) {
+      const int j = warp * (32 * MAXI) + i * 32 + lane;
       const bool ok = j < n;
-      const unsigned d = ok ? ((S.sort.q[cur][j] >> ds) & 255u) : (256u + lane);
+      const unsigned d = ok ? ((L.q[cur][j] >> ds) & 255u) : (256u + lane);
       dig[i] = d;
       const unsigned peers = __match_any_sync(0xffffffffu, d);
       uint32_t old = 0;
       if (ok) {
-        old = S.sort.hist[warp][d];
+        old = L.hist[warp][d];
         rank[i] = old + __popc(peers & lanemask_lt());
       }
       __syncwarp();
-      if (ok && lane == __ffs(peers) - 1) S.sort.hist[warp][d] = old + __popc(peers);
+      if (ok && lane == __ffs(peers) - 1) L.hist[warp][d] = old + __popc(peers);
       __syncwarp();
     }
     __syncthreads();
-    {
-      // thread tid owns digit tid: offsets of the warps inside the digit,
-      // then an exclusive scan of the digit totals across threads
-      uint32_t run = 0;
+    uint32_t run = 0;
 #pragma unroll
-      for (int w = 0; w < WARPS; ++w) {
-        const uint32_t c = S.sort.hist[w][tid];
-        S.sort.hist[w][tid] = run;
-        run += c;
-      }
-      uint32_t incl = run;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      __shared__ uint32_t s_wsum[WARPS];
-      if (lane == 31) s_wsum[warp] = incl;
-      __syncthreads();
-      uint32_t base = incl - run;
-      for (int w = 0; w < warp; ++w) base += s_wsum[w];
-#pragma unroll
-      for (int w = 0; w < WARPS; ++w) S.sort.hist[w][tid] += base;
+    for (int w = 0; w < WARPS; ++w) {
+      const uint32_t c = L.hist[w][tid];
+      L.hist[w][tid] = run;
+      run += c;
     }
+    uint32_t total;
+    const uint32_t base = block_excl_scan(S, run, total);
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) L.hist[w][tid] += base;
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      const int j = warp * (32 * ITEMS) + i * 32 + lane;
+    for (int i = 0; i < MAXI; ++i) {
+      const int j = warp * (32 * MAXI) + i * 32 + lane;
       if (j < n) {
-        const uint32_t dst = S.sort.hist[warp][dig[i]] + rank[i];
-        S.sort.q[1 - cur][dst] = S.sort.q[cur][j];
-        S.sort.p[1 - cur][dst] = S.sort.p[cur][j];
+        const uint32_t dst = L.hist[warp][dig[i]] + rank[i];
+        L.q[1 - cur][dst] = L.q[cur][j];
+        L.p[1 - cur][dst] = L.p[cur][j];
       }
     }
     __syncthreads();
     cur = 1 - cur;
   }
-  // equal 32-bit offsets: order by the full (key, idx)
-  bool tie = false;
-  for (int j = tid; j + 1 < n; j += BT)
-    if (S.sort.q[cur][j] == S.sort.q[cur][j + 1]) tie = true;
-  if (__syncthreads_or(tie)) {
-    for (int j = tid; j + 1 < n; j += BT) {
-      const uint32_t qj = S.sort.q[cur][j];
-      if (qj != S.sort.q[cur][j + 1] || (j > 0 && S.sort.q[cur][j - 1] == qj)) continue;
-      int e = j + 1;
-      while (e + 1 < n && S.sort.q[cur][e + 1] == qj) ++e;
-      uint16_t* p = S.sort.p[cur];
-      for (int a = j + 1; a <= e; ++a) {
-        const uint16_t s = p[a];
-        const uint64_t ks = S.key[s];
-        const int32_t is = S.idx[s];
-        int b = a - 1;
-        while (b >= j && pair_less(ks, is, S.key[p[b]], S.idx[p[b]])) {
-          p[b + 1] = p[b];
-          --b;
-        }
-        p[b + 1] = s;
+  for (int j = tid; j < n; j += BT) S.perm[j] = L.p[cur][j];
+  __syncthreads();
+  // equal offsets: order by the full (key, idx)
+  for (int j = tid; j + 1 < n; j += BT) {
+    const uint32_t qj = L.q[cur][j];
+    if (qj != L.q[cur][j + 1] || (j > 0 && L.q[cur][j - 1] == qj)) continue;
+    int e = j + 1;
+    while (e + 1 < n && L.q[cur][e + 1] == qj) ++e;
+    for (int a = j + 1; a <= e; ++a) {
+      const uint16_t s = S.perm[a];
+      const uint64_t ks = S.key[s];
+      const int32_t is = S.idx[s];
+      int b = a - 1;
+      while (b >= j && pair_less(ks, is, S.key[S.perm[b]], S.idx[S.perm[b]])) {
+        S.perm[b + 1] = S.perm[b];
+        --b;
       }
+      S.perm[b + 1] = s;
     }
-    __syncthreads();
   }
-  if (tid == 0) S.perm_buf = cur;
+  __syncthreads();
+}
+
+// Sort the n <= CAP sheets of the bucket by (key, idx) into S.perm.
+__device__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin, uint64_t kmax) {
+  const int tid = threadIdx.x;
+  const uint64_t span = kmax - kmin;
+  const int bits = span ? 64 - __clzll((long long)span) : 0;
+  const int shift = bits > QB ? bits - QB : 0;
+  uint32_t* bins = S.u.bins;
+  for (int j = tid; j < NBIN_PAD; j += BT) bins[j] = 0;
+  __syncthreads();
+  uint16_t qv[MAXI], rk[MAXI];
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i) {
+    const int j = tid + i * BT;
+    if (i < ipt && j < n) {
+      qv[i] = (uint16_t)((S.key[j] - kmin) >> shift);
+      rk[i] = (uint16_t)atomicAdd(&bins[binp(qv[i])], 1u);
+    }
+  }
+  __syncthreads();
+  // exclusive scan of the bins: thread t owns bins [16 t, 16 t + 16)
+  constexpr int PER = NBIN / BT;
+  uint32_t c[PER];
+  uint32_t run = 0, mx = 0;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    c[k] = bins[binp(tid * PER + k)];
+    mx = c[k] > mx ? c[k] : mx;
+    run += c[k];
+  }
+  const int too_full = __syncthreads_or(mx > (uint32_t)MAXBIN);
+  if (too_full) {
+    lsd_sort(S, n, kmin, kmax);
+    return;
+  }
+  uint32_t total;
+  uint32_t off = block_excl_scan(S, run, total);
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    bins[binp(tid * PER + k)] = off;
+    off += c[k];
+  }
+  if (tid == 0) bins[binp(NBIN)] = (uint32_t)n;
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i) {
+    const int j = tid + i * BT;
+    if (i < ipt && j < n) S.perm[bins[binp(qv[i])] + rk[i]] = (uint16_t)j;
+  }
+  __syncthreads();
+  // the order inside a bin came from atomics: sort each bin by (key, idx)
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int q = tid * PER + k;
+    const uint32_t lo = bins[binp(q)], hi = bins[binp(q + 1)];
+    if (hi - lo < 2) continue;
+    for (uint32_t a = lo + 1; a < hi; ++a) {
+      const uint16_t s = S.perm[a];
+      const uint64_t ks = S.key[s];
+      const int32_t is = S.idx[s];
+      int b = (int)a - 1;
+      while (b >= (int)lo && pair_less(ks, is, S.key[S.perm[b]], S.idx[S.perm[b]])) {
+        S.perm[b + 1] = S.perm[b];
+        --b;
+      }
+      S.perm[b + 1] = s;
+    }
+  }
   __syncthreads();
 }
 
 // Look-back over earlier buckets of the same simulation for the exclusive
-// (mass, count) prefix; all lanes of warp 0 call it.
-__device__ void bucket_lookback(const BucketStepArgs& a, int64_t b, u128 mass, uint32_t cnt,
-                                unsigned ep, int lane, u128& pmass, uint32_t& pcnt) {
-  BucketRec* recs = a.recs;
+// (mass, count) prefix; all lanes of warp 0 call it.  Bounded waits.
+__device__ void bucket_lookback(BucketRec* recs, int64_t b, u128 mass, uint32_t cnt,
+                                unsigned ep, int lane, unsigned* err, u128& pmass,
+                                uint32_t& pcnt) {
   BucketRec* me = recs + b;
   pmass = 0;
   pcnt = 0;
@@ -216,11 +308,11 @@ __device__ void bucket_lookback(const BucketStepArgs& a, int64_t b, u128 mass, u
         f = ld_acquire_u32(&r->flag);
         if ((f >> 2) == ep && (f & 3u)) break;
         if (++spins > kSpinLimit) {
-          atomicOr(a.err, DEV_ERR_LOOKBACK_TIMEOUT);
+          atomicOr(err, DEV_ERR_LOOKBACK_TIMEOUT);
           f = 0;
           break;
         }
-        __nanosleep(32);
+        __nanosleep(20);
       }
       status = ((f >> 2) == ep) ? (f & 3u) : 0u;
       if (status == 2u) {
@@ -252,28 +344,30 @@ __device__ void bucket_lookback(const BucketStepArgs& a, int64_t b, u128 mass, u
 }
 
 // Bucket of the next layout covering (k, i): the largest j with Q_j <= (k, i).
-__device__ int dest_bucket(const BucketStepArgs& a, const StepSmem& S, uint64_t k, int32_t i,
-                           bool& far) {
-  // window [win_lo, win_hi] of splitter indices is in shared memory
-  const int lo = S.win_lo, hi = S.win_hi;
-  far = false;
-  if (!pair_less(k, i, S.wkey[0], S.widx[0]) &&
-      pair_less(k, i, S.wkey[hi - lo], S.widx[hi - lo])) {
-    int l = 0, h = hi - lo;  // Q_{lo+l} <= (k,i) < Q_{lo+h}
-    while (h - l > 1) {
-      const int mid = (l + h) >> 1;
-      if (pair_less(k, i, S.wkey[mid], S.widx[mid]))
-        h = mid;
-      else
-        l = mid;
+// (k, i) >= splitter j of the window (keys first; indices only on a tie)
+__device__ __forceinline__ bool win_ge(const StepSmem& S, int j, uint64_t k, int32_t i) {
+  const uint64_t K = S.wkey[j];
+  return k > K || (k == K && i >= S.widx[j]);
+}
+
+__device__ __forceinline__ int dest_bucket(const StepSmem& S, const uint64_t* qk,
+                                           const int32_t* qi, int64_t nb, uint64_t k,
+                                           int32_t i) {
+  const int lo = S.win_lo, w = S.win_hi - S.win_lo;
+  if (win_ge(S, 0, k, i) && !win_ge(S, w, k, i)) {
+    int l = 0, len = w;  // Q_{lo+l} <= (k,i) < Q_{lo+l+len}
+    while (len > 1) {
+      const int half = len >> 1;
+      const bool ge = win_ge(S, l + half, k, i);
+      l = ge ? l + half : l;
+      len = ge ? len - half : half;
     }
     return lo + l;
   }
-  far = true;
-  int l = 0, h = (int)a.nb;  // Q_0 = -inf <= (k,i) < Q_nb = +inf
+  int l = 0, h = (int)nb;  // Q_0 = -inf <= (k,i) < Q_nb = +inf
   while (h - l > 1) {
     const int mid = (l + h) >> 1;
-    if (pair_less(k, i, __ldg(&a.q_dest_key[mid]), __ldg(&a.q_dest_idx[mid])))
+    if (pair_less(k, i, __ldg(&qk[mid]), __ldg(&qi[mid])))
       h = mid;
     else
       l = mid;
@@ -281,59 +375,86 @@ __device__ int dest_bucket(const BucketStepArgs& a, const StepSmem& S, uint64_t 
   return l;
 }
 
-__global__ void __launch_bounds__(BT, 2) k_bucket_step(const BucketStepArgs a) {
+__global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   StepSmem& S = *reinterpret_cast<StepSmem*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  {
-    const unsigned ab = *(volatile const unsigned*)a.abort;
-    if (ab != 0 && (int)ab <= a.sub) return;  // an earlier sub-step of this call failed
-  }
-  if (tid == 0) {
-    S.epoch = a.epochs[a.sub];
-    S.amp = (a.ext.kind == EXT_PULSE_TANH) ? pulse_amplitude(a.ext, a.t_seq[a.sub]) : 0.0;
-    S.maxv = 0;
-    S.flags = 0;
-  }
-  const i128 T = (i128)((((u128)a.T_hi) << 64) | a.T_lo);
+  const int sub = L.sub;
+  const bool last = sub == L.nleap - 1;
+  if (tid == 0) S.epoch = L.epochs[sub];
   for (;;) {
     __syncthreads();
     if (tid == 0) {
-      S.bucket = atomicAdd(a.ticket, 1u);
-      S.n = S.bucket < a.nb ? (int)a.cnt_in[S.bucket] : 0;
+      S.task = atomicAdd(L.ticket, 1u);
+      if (S.task < (unsigned)L.ntasks) {
+        const BucketTask t = L.tasks[S.task];
+        S.sim = t.sim;
+        S.bucket = t.bucket;
+      }
     }
     __syncthreads();
+    if (S.task >= (unsigned)L.ntasks) break;
+    const SimDev& D = L.sims[S.sim];
+    {
+      // an earlier sub-step of this call overflowed this simulation: its
+      // host side finishes the call on the compact path
+      const unsigned ab = *(volatile const unsigned*)(D.ocount + 1);
+      if (ab != 0 && (int)ab <= sub) continue;
+    }
     const int64_t b = S.bucket;
-    if (b >= a.nb) break;
-    const int n = S.n < CAP ? S.n : CAP;
+    const int lay = (D.lay0 + sub) & 1, qs = (D.qsel0 + sub) & 1;
+    const double* xin = D.bx[lay];
+    const double* vin = D.bv[lay];
+    const double* min = D.bm[lay];
+    const int32_t* iin = D.bi[lay];
+    unsigned* cnt_in = D.bcnt[lay];
+    const uint64_t* qdk = D.qk[qs];
+    const int32_t* qdi = D.qi[qs];
     const int64_t base = b * CAP;
-    if (tid == 0) a.cnt_in[b] = 0;  // this count buffer is the target two sub-steps on
-    // ---- load (applying the opening half drift of a call, if any)
+    int n = (int)cnt_in[b];
+    n = n < CAP ? n : CAP;
+    const int ipt = (n + BT - 1) / BT;
+    const double pre = sub == 0 ? D.pre_dt : 0.0;
+    const int E = D.E;
+    __syncthreads();  // every thread has read cnt_in[b]
+    if (tid == 0) {
+      cnt_in[b] = 0;  // this count buffer is the target two sub-steps on
+      S.amp = (D.ext.kind == EXT_PULSE_TANH) ? pulse_amplitude(D.ext, D.t_seq[sub]) : 0.0;
+    }
+    // ---- load, with the bucket's mass and count
     uint64_t kmin = ~0ull, kmax = 0;
-    for (int j = tid; j < n; j += BT) {
-      const double v = a.vin[base + j];
-      double x = a.xin[base + j];
-      if (a.pre_dt != 0.0) x = fma(a.pre_dt, v, x);
-      const uint64_t k = key_of(x);
-      S.x[j] = x;
-      S.v[j] = v;
-      S.m[j] = a.min[base + j];
-      S.idx[j] = a.iin[base + j];
-      S.key[j] = k;
-      kmin = k < kmin ? k : kmin;
-      kmax = k > kmax ? k : kmax;
+    u128 msum = 0;
+#pragma unroll
+    for (int i = 0; i < MAXI; ++i) {
+      const int j = tid + i * BT;
+      if (i < ipt && j < n) {
+        const double v = vin[base + j];
+        double x = xin[base + j];
+        if (pre != 0.0) x = fma(pre, v, x);
+        const uint64_t k = key_of(x);
+        const double mj = min[base + j];
+        S.x[j] = x;
+        S.v[j] = v;
+        S.m[j] = mj;
+        S.idx[j] = iin[base + j];
+        S.key[j] = k;
+        kmin = k < kmin ? k : kmin;
+        kmax = k > kmax ? k : kmax;
+        msum += mass_to_fixed(mj, E);
+      }
     }
     // splitter window of the next layout around this bucket
     const int wlo = (int)(b > RWIN ? b - RWIN : 0);
-    const int whi = (int)((b + RWIN + 1) < a.nb ? (b + RWIN + 1) : a.nb);
+    const int whi = (int)((b + RWIN + 1) < D.nb ? (b + RWIN + 1) : D.nb);
     for (int j = tid; j <= whi - wlo; j += BT) {
-      S.wkey[j] = a.q_dest_key[wlo + j];
-      S.widx[j] = a.q_dest_idx[wlo + j];
+      S.wkey[j] = qdk[wlo + j];
+      S.widx[j] = qdi[wlo + j];
       S.dcount[j] = 0;
     }
     if (tid == 0) {
       S.win_lo = wlo;
       S.win_hi = whi;
+      S.maxv = 0;
     }
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) {
@@ -342,11 +463,23 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const BucketStepArgs a) {
       kmin = o1 < kmin ? o1 : kmin;
       kmax = o2 > kmax ? o2 : kmax;
     }
+    msum = warp_sum_u128(msum);
     if (lane == 0) {
       S.red_min[warp] = kmin;
       S.red_max[warp] = kmax;
+      S.warp_mass[warp] = msum;
     }
     __syncthreads();
+    if (warp == 0) {
+      const u128 bm = warp_sum_u128(lane < WARPS ? S.warp_mass[lane] : (u128)0);
+      u128 pm;
+      uint32_t pc;
+      bucket_lookback(D.recs, b, bm, (uint32_t)n, S.epoch, lane, L.err, pm, pc);
+      if (lane == 0) {
+        S.prefix_mass = pm;
+        S.prefix_cnt = pc;
+      }
+    }
     kmin = ~0ull;
     kmax = 0;
 #pragma unroll
@@ -354,33 +487,22 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const BucketStepArgs a) {
       kmin = S.red_min[w] < kmin ? S.red_min[w] : kmin;
       kmax = S.red_max[w] > kmax ? S.red_max[w] : kmax;
     }
+    // ---- sort the bucket (barriers inside wait for the look-back warp)
     if (n > 1) {
-      bucket_sort(S, n, kmin, kmax);
+      bucket_sort(S, n, ipt, kmin, kmax);
     } else {
-      if (tid == 0) {
-        S.sort.p[0][0] = 0;
-        S.perm_buf = 0;
-      }
+      if (tid == 0) S.perm[0] = 0;
       __syncthreads();
     }
-    const uint16_t* perm = S.sort.p[S.perm_buf];
 
-    // ---- exact prefix of the masses (blocked: ITEMS sorted positions per thread)
-    const int j0 = tid * ITEMS;
-    u128 cex[ITEMS];
-    u128 run = 0;
-    int nv = 0;
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      cex[i] = run;
-      if (j0 + i < n) {
-        run += mass_to_fixed(S.m[perm[j0 + i]], a.E);
-        ++nv;
-      }
-    }
-    const u128 tot = run;
+    // ---- exact prefix of the masses in sorted order: thread tid holds the
+    // sorted positions [tid * ipt, tid * ipt + ipt)
+    const int j0 = tid * ipt;
+    const int nmine = (j0 < n) ? ((n - j0) < ipt ? (n - j0) : ipt) : 0;
+    u128 tot = 0;
+    for (int i = 0; i < nmine; ++i) tot += mass_to_fixed(S.m[S.perm[j0 + i]], E);
     const u128 incl = warp_inclusive_scan_u128(tot, lane);
-    uint32_t cin = (uint32_t)nv;
+    uint32_t cin = (uint32_t)nmine;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t y = __shfl_up_sync(0xffffffffu, cin, o);
@@ -391,114 +513,99 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const BucketStepArgs a) {
       S.warp_cnt[warp] = cin;
     }
     __syncthreads();
-    if (warp == 0) {
-      const u128 wm = lane < WARPS ? S.warp_mass[lane] : (u128)0;
-      const uint32_t wc = lane < WARPS ? S.warp_cnt[lane] : 0u;
-      const u128 wmi = warp_inclusive_scan_u128(wm, lane);
-      uint32_t wci = wc;
+    u128 C = S.prefix_mass;
+    uint32_t rank0 = S.prefix_cnt;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, wci, o);
-        if (lane >= o) wci += y;
-      }
-      const u128 bm = shfl_u128(wmi, WARPS - 1);
-      const uint32_t bc = __shfl_sync(0xffffffffu, wci, WARPS - 1);
-      if (lane < WARPS) {
-        S.warp_mass[lane] = wmi - wm;
-        S.warp_cnt[lane] = wci - wc;
-      }
-      u128 pm;
-      uint32_t pc;
-      bucket_lookback(a, b, bm, bc, S.epoch, lane, pm, pc);
-      if (lane == 0) {
-        S.prefix_mass = pm;
-        S.prefix_cnt = pc;
+    for (int w = 0; w < WARPS; ++w) {
+      if (w < warp) {
+        C += S.warp_mass[w];
+        rank0 += S.warp_cnt[w];
       }
     }
-    __syncthreads();
-    const u128 tpm = S.prefix_mass + S.warp_mass[warp] + (incl - tot);
-    const uint32_t rank0 = S.prefix_cnt + S.warp_cnt[warp] + (cin - (uint32_t)nv);
+    C += incl - tot;
+    rank0 += cin - (uint32_t)nmine;
 
     // ---- splitters of the layout after next: keys at global ranks j*T
+    uint64_t* qnk = D.qk[1 - qs];
+    int32_t* qni = D.qi[1 - qs];
     if (b == 0 && tid == 0) {
-      a.q_new_key[0] = 0ull;
-      a.q_new_idx[0] = (int32_t)0x80000000;
-      a.q_new_key[a.nb] = ~0ull;
-      a.q_new_idx[a.nb] = 0x7fffffff;
+      qnk[0] = 0ull;
+      qni[0] = (int32_t)0x80000000;
+      qnk[D.nb] = ~0ull;
+      qni[D.nb] = 0x7fffffff;
     }
-    // ---- force, kick, drift, routing
+    // ---- force, kick, drift, routing; new x, v go back to their slots and
+    // the destination of every slot to the (now free) sort area
+    int32_t* sdst = reinterpret_cast<int32_t*>(S.u.bins);          // [CAP]
+    uint16_t* srank = reinterpret_cast<uint16_t*>(sdst + CAP);     // [CAP]
+    const double dt = L.profile ? 0.0 : D.dt;
+    const double dt_drift = last ? dt / 2. : dt;
+    const double dest_dt = (last && !L.profile) ? dt / 2. : 0.0;
+    const i128 T = (i128)((((u128)D.T_hi) << 64) | D.T_lo);
     unsigned long long maxv = 0;
-    double xr[ITEMS], vr[ITEMS];
-    int dst[ITEMS];
-    uint32_t drank[ITEMS];
-    bool dfar[ITEMS];
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      dst[i] = -1;
-      if (j0 + i >= n) continue;
-      const int s = perm[j0 + i];
+    for (int i = 0; i < nmine; ++i) {
+      const int s = S.perm[j0 + i];
       const uint32_t r = rank0 + (uint32_t)i;
-      if (r != 0 && (r % (uint32_t)a.target) == 0) {
-        a.q_new_key[r / a.target] = S.key[s];
-        a.q_new_idx[r / a.target] = S.idx[s];
+      const uint64_t key = S.key[s];
+      const int32_t id = S.idx[s];
+      if (r != 0 && (r % (uint32_t)kBucketTarget) == 0) {
+        qnk[r / kBucketTarget] = key;
+        qni[r / kBucketTarget] = id;
       }
       const double x = S.x[s], v = S.v[s];
-      const u128 M = (i + 1 < ITEMS ? cex[i + 1] : tot) - cex[i];
-      const i128 C = (i128)(tpm + cex[i]);
-      const i128 A = T - 2 * C - (i128)M;
-      double acc = fixed_to_double(A, a.E);
-      if (a.has_omega) acc = fma(-a.omega2, x, acc);
-      if (a.ext.kind != EXT_NONE) acc = ext_force_at(a.ext, S.amp, x) + acc;
-      const double vn = fma(a.dt_kick, acc, v);
-      const double xn = fma(a.dt_drift, vn, x);
-      xr[i] = xn;
-      vr[i] = vn;
+      const u128 M = mass_to_fixed(S.m[s], E);
+      const i128 A = T - 2 * (i128)C - (i128)M;
+      C += M;
+      double acc = fixed_to_double(A, E);
+      if (D.has_omega) acc = fma(-D.omega2, x, acc);
+      if (D.ext.kind != EXT_NONE) acc = ext_force_at(D.ext, S.amp, x) + acc;
+      const double vn = fma(dt, acc, v);
+      const double xn = fma(dt_drift, vn, x);
+      S.x[s] = xn;
+      S.v[s] = vn;
       const unsigned long long av =
           (unsigned long long)__double_as_longlong(vn) & 0x7FFFFFFFFFFFFFFFull;
       maxv = av > maxv ? av : maxv;
-      if (a.x_orig) {
-        a.x_orig[S.idx[s]] = xn;
-        a.v_orig[S.idx[s]] = vn;
+      if (last && !L.profile) {
+        D.x_out[id] = xn;
+        D.v_out[id] = vn;
       }
-      const double xd = a.dest_dt != 0.0 ? fma(a.dest_dt, vn, xn) : xn;
-      bool far;
-      const int d = dest_bucket(a, S, key_of(xd), S.idx[s], far);
-      dst[i] = d;
-      dfar[i] = far;
-      if (!far) drank[i] = atomicAdd(&S.dcount[d - S.win_lo], 1u);
+      const double xd = dest_dt != 0.0 ? fma(dest_dt, vn, xn) : xn;
+      const int d = dest_bucket(S, qdk, qdi, D.nb, key_of(xd), id);
+      sdst[s] = d;
+      srank[s] = (d >= S.win_lo && d < S.win_hi)
+                     ? (uint16_t)atomicAdd(&S.dcount[d - S.win_lo], 1u)
+                     : (uint16_t)0xffffu;
     }
     __syncthreads();
-    for (int j = tid; j <= S.win_hi - S.win_lo; j += BT) {
+    for (int j = tid; j < S.win_hi - S.win_lo; j += BT) {
       const uint32_t c = S.dcount[j];
-      S.dbase[j] = c ? atomicAdd(&a.cnt_out[S.win_lo + j], c) : 0u;
+      S.dbase[j] = c ? atomicAdd(&D.bcnt[1 - lay][S.win_lo + j], c) : 0u;
     }
     __syncthreads();
-    unsigned fl = 0;
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      if (dst[i] < 0) continue;
-      const int s = perm[j0 + i];
-      const int d = dst[i];
-      uint32_t slot;
-      if (dfar[i]) {
-        slot = atomicAdd(&a.cnt_out[d], 1u);
-        fl |= 1u;
-      } else {
-        slot = S.dbase[d - S.win_lo] + drank[i];
-      }
+    double* xout = D.bx[1 - lay];
+    double* vout = D.bv[1 - lay];
+    double* mout = D.bm[1 - lay];
+    int32_t* iout = D.bi[1 - lay];
+    bool overflow = false;
+    for (int j = tid; j < n; j += BT) {
+      const int d = sdst[j];
+      const uint16_t rk = srank[j];
+      const uint32_t slot = rk == 0xffffu ? atomicAdd(&D.bcnt[1 - lay][d], 1u)
+                                          : S.dbase[d - S.win_lo] + rk;
       if (slot < (uint32_t)CAP) {
         const int64_t o = (int64_t)d * CAP + slot;
-        a.xout[o] = xr[i];
-        a.vout[o] = vr[i];
-        a.mout[o] = S.m[s];
-        a.iout[o] = S.idx[s];
+        xout[o] = S.x[j];
+        vout[o] = S.v[j];
+        mout[o] = S.m[j];
+        iout[o] = S.idx[j];
       } else {
-        const uint32_t o = atomicAdd(a.ocount, 1u);
-        a.ox[o] = xr[i];
-        a.ov[o] = vr[i];
-        a.om[o] = S.m[s];
-        a.oi[o] = S.idx[s];
-        fl |= 2u;
+        const uint32_t o = atomicAdd(D.ocount, 1u);
+        D.ox[o] = S.x[j];
+        D.ov[o] = S.v[j];
+        D.om[o] = S.m[j];
+        D.oi[o] = S.idx[j];
+        overflow = true;
       }
     }
 #pragma unroll
@@ -507,13 +614,9 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const BucketStepArgs a) {
       maxv = o > maxv ? o : maxv;
     }
     if (lane == 0 && maxv) atomicMax(&S.maxv, maxv);
-    if (fl) atomicOr(&S.flags, fl);
-  }
-  __syncthreads();
-  if (tid == 0) {
-    if (S.maxv) atomicMax(&a.flag_out->max_v, S.maxv);
-    if (S.flags & 1u) atomicAdd(&a.flag_out->pad, 1u);  // sheets found by the global search
-    if (S.flags & 2u) atomicCAS(a.abort, 0u, (unsigned)(a.sub + 1));  // overflow: re-sort
+    if (overflow) atomicCAS(D.ocount + 1, 0u, (unsigned)(sub + 1));
+    __syncthreads();
+    if (tid == 0 && S.maxv) atomicMax(&D.flags[sub + 1].max_v, S.maxv);
   }
 }
 
@@ -606,15 +709,17 @@ __global__ void k_count_offsets(const unsigned* cnt, int64_t nb, unsigned* offs)
 
 }  // namespace
 
-size_t bucket_step_smem() { return sizeof(StepSmem); }
+int bucket_step_grid(int sm_count) { return 2 * sm_count; }
 
-void launch_bucket_step(const BucketStepArgs& a, int grid, cudaStream_t s) {
+void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_bucket_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sizeof(StepSmem));
     attr = true;
   }
+  if (grid > a.ntasks) grid = a.ntasks;
+  if (grid < 1) grid = 1;
   k_bucket_step<<<grid, BT, sizeof(StepSmem), s>>>(a);
 }
 

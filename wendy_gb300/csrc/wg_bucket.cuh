@@ -1,4 +1,10 @@
 // wg_bucket.cuh -- bucketed sheet layout and the fused sub-step kernel.
+//
+// A launch of the sub-step kernel serves any number of simulations at once:
+// each simulation has its own arrays (described by a SimDev entry) and the
+// launch walks a list of (simulation, bucket) tasks in order, so one launch
+// per sub-step advances a whole ensemble.  A single simulation is an ensemble
+// of one.
 #pragma once
 #include <cstdint>
 
@@ -13,63 +19,66 @@ constexpr int kSplitterWindow = 64;   // buckets searched in shared memory on ea
 
 // Decoupled look-back record of one bucket (48 bytes).
 struct __align__(16) BucketRec {
-  uint64_t agg_lo, agg_hi;  // bucket's fixed-point mass
-  uint64_t inc_lo, inc_hi;  // inclusive mass prefix
+  uint64_t agg_lo, agg_hi;    // bucket's fixed-point mass
+  uint64_t inc_lo, inc_hi;    // inclusive mass prefix
   uint32_t agg_cnt, inc_cnt;  // sheet count, inclusive count prefix
   unsigned flag;              // (epoch << 2) | {1: aggregate, 2: inclusive}
   unsigned pad;
 };
 
-struct BucketStepArgs {
-  // layout read by this sub-step (bucket b = slots [b*cap, b*cap + cnt_in[b]))
-  const double* xin;
-  const double* vin;
-  const double* min;
-  const int32_t* iin;
-  unsigned* cnt_in;        // zeroed after reading (reused two sub-steps later)
-  // layout written by this sub-step
-  double* xout;
-  double* vout;
-  double* mout;
-  int32_t* iout;
-  unsigned* cnt_out;       // zero on entry, appended to
-  const uint64_t* q_dest_key;  // [nb + 1] splitters of the written layout
-  const int32_t* q_dest_idx;
-  uint64_t* q_new_key;     // [nb + 1] quantiles of this sub-step's sorted keys
-  int32_t* q_new_idx;
+// One simulation as the sub-step kernel sees it.  Arrays are the
+// simulation's own; layouts, counts and splitters come in pairs used
+// alternately from sub-step to sub-step, starting at lay0 / qsel0.
+struct SimDev {
+  double* bx[2];
+  double* bv[2];
+  double* bm[2];
+  int32_t* bi[2];
+  unsigned* bcnt[2];     // per-bucket sheet counts of each layout
+  uint64_t* qk[2];       // [nb + 1] splitter keys (Q_0 = -inf, Q_nb = +inf)
+  int32_t* qi[2];        // [nb + 1] splitter indices
+  BucketRec* recs;       // [nb]
+  double* ox;            // overflow list
+  double* ov;
+  double* om;
+  int32_t* oi;
+  unsigned* ocount;      // [0] sheets in the overflow list, [1] 1 + sub-step that overflowed
+  double* x_out;         // output of the call's last sub-step, original order
+  double* v_out;
+  StepFlags* flags;      // [nleap + 1] of this call
+  const double* t_seq;   // [nleap] times of this call's force evaluations
   int64_t n;
   int64_t nb;
-  int target;
-  BucketRec* recs;
-  const unsigned* epochs;
-  int sub;
-  unsigned* ticket;
-  // physics
-  uint64_t T_lo, T_hi;
+  uint64_t T_lo, T_hi;   // totmass in fixed point
   int E;
   int has_omega;
   double omega2;
   ExtForce ext;
-  const double* t_seq;
-  double pre_dt;    // drift applied on load (a call's opening half drift) or 0
-  double dt_kick;
-  double dt_drift;
-  double dest_dt;   // routing uses x + dest_dt v (the next call's opening half drift) or 0
-  double* x_orig;   // if set: new x, v written in original order (the call's output)
-  double* v_orig;
-  // overflow list (sheets that found their bucket full)
-  double* ox;
-  double* ov;
-  double* om;
-  int32_t* oi;
-  unsigned* ocount;
-  unsigned* abort;  // 1 + first sub-step of the call that overflowed, or 0
-  unsigned* err;
-  StepFlags* flag_out;
+  double dt;             // leapfrog step of this call
+  double pre_dt;         // half drift applied while loading the first sub-step (or 0)
+  int lay0;              // layout read by the call's first sub-step
+  int qsel0;             // splitter array defining the layout the first sub-step writes
 };
 
-size_t bucket_step_smem();
-void launch_bucket_step(const BucketStepArgs& a, int grid, cudaStream_t s);
+struct BucketTask {
+  int sim;
+  int bucket;
+};
+
+struct StepLaunch {
+  const SimDev* sims;
+  const BucketTask* tasks;
+  int ntasks;
+  int sub;               // sub-step index within the call
+  int nleap;
+  const unsigned* epochs;
+  unsigned* ticket;      // zero before the launch
+  unsigned* err;
+  int profile;           // 1: dt = 0 and no outputs (timing harness)
+};
+
+void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s);
+int bucket_step_grid(int sm_count);
 void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, double* x,
                       double* v, double* m, int32_t* idx, unsigned* cnt, uint64_t* qk,
                       int32_t* qi, unsigned* cnt_other, cudaStream_t s);

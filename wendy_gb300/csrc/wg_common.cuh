@@ -66,17 +66,19 @@ __device__ __forceinline__ u128 mass_to_fixed(double m, int E) {
 
 // Signed 128-bit integer A times 2^-E, rounded to nearest even.  The normal
 // range is handled with integer operations only (FP64 issue slots are the
-// scarce resource on this part); an out-of-range exponent falls back to
-// ldexp.
-__device__ __forceinline__ double fixed_to_double(i128 A, int E) {
-  if (A == 0) return 0.0;
+// scarce resource on this part): the top 64 bits of |A| are normalised with
+// one count-leading-zeros, the mantissa is their top 53 bits and the rest
+// (plus a sticky bit for everything below) decides the rounding.  Values
+// below 2^64 units or outside the normal exponent range take ldexp.
+static __device__ __noinline__ double fixed_to_double_slow(i128 A, int E) {
   const bool neg = A < 0;
   const u128 u = neg ? (u128)(-A) : (u128)A;
+  if (u == 0) return 0.0;
   const uint64_t hi = (uint64_t)(u >> 64), lo = (uint64_t)u;
   const int lz = hi ? __clzll((long long)hi) : 64 + __clzll((long long)lo);
-  const int p = 127 - lz;  // index of the leading one
+  const int p = 127 - lz;
   uint64_t mant;
-  int e2;  // |A| ~= mant * 2^e2, mant in [2^52, 2^53)
+  int e2;
   if (p <= 52) {
     mant = lo << (52 - p);
     e2 = p - 52;
@@ -94,11 +96,29 @@ __device__ __forceinline__ double fixed_to_double(i128 A, int E) {
     }
     e2 = sh;
   }
-  const int bexp = e2 - E + 52 + 1023;
-  if (bexp <= 0 || bexp >= 2047) {
-    const double r = ldexp((double)mant, e2 - E);
-    return neg ? -r : r;
+  const double r = ldexp((double)mant, e2 - E);
+  return neg ? -r : r;
+}
+
+__device__ __forceinline__ double fixed_to_double(i128 A, int E) {
+  const bool neg = A < 0;
+  const u128 u = neg ? (u128)(-A) : (u128)A;
+  const uint64_t hi = (uint64_t)(u >> 64), lo = (uint64_t)u;
+  if (hi == 0) return fixed_to_double_slow(A, E);
+  const int lz = __clzll((long long)hi);
+  const uint64_t t = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;  // top 64 bits
+  const uint64_t rest = lo << lz;                                  // bits below t
+  uint64_t mant = t >> 11;
+  const uint64_t r = t & 0x7FFull;
+  int bexp = 127 - lz - E + 1023;
+  if (r > 0x400ull || (r == 0x400ull && (rest != 0 || (mant & 1ull)))) {
+    ++mant;
+    if (mant == (1ull << 53)) {
+      mant >>= 1;
+      ++bexp;
+    }
   }
+  if (bexp <= 0 || bexp >= 2047) return fixed_to_double_slow(A, E);
   const uint64_t bits = ((uint64_t)bexp << 52) | (mant & 0xFFFFFFFFFFFFFull) |
                         (neg ? 0x8000000000000000ull : 0ull);
   return __longlong_as_double((long long)bits);

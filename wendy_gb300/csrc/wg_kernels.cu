@@ -107,6 +107,10 @@ __global__ void __launch_bounds__(THREADS, 2) k_force_kick_drift(const ForceArgs
   const int64_t tile = s_tile;
   const int64_t base = tile * TILE;
   const int64_t n = a.n;
+  if (base >= n) {  // only with a ticket counter that was not reset: do nothing
+    if (tid == 0) atomicOr(a.err, DEV_ERR_BAD_STATE);
+    return;
+  }
   const StateRef st = a.table->cur;
   const int64_t i0 = base + (int64_t)tid * ITEMS;
   const bool full = base + TILE <= n;

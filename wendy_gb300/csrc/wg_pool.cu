@@ -1,0 +1,666 @@
+// wg_pool.cu -- many simulations resident on one GPU, advanced together.
+//
+// A pool owns any number of simulations (each with its own bucket layouts,
+// look-back records and splitters, allocated with the stream-ordered
+// allocator) and one shared workspace (compact sheet sets, radix-sort
+// buffers) sized for the largest of them.  wg_pool_step advances any subset
+// of the simulations by one output interval with ONE launch of the fused
+// bucket kernel per leapfrog sub-step: the launch walks the concatenated
+// bucket lists of all chosen simulations, and every look-back, sort and
+// splitter stays inside its own simulation, so each result is bit-identical
+// to the same simulation run alone.  Simulations can be added and removed
+// between steps, which is what continuous batching needs.
+//
+// Per simulation the arithmetic is that of wendy's approximate step
+// (wendy/wendy.c:385-418); the reference has no ensemble API.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/wendy_gb300.h"
+#include "wg_bucket.cuh"
+#include "wg_internal.cuh"
+
+using namespace wg;
+
+namespace {
+
+size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+int pool_fail(int code, const char* fmt, ...) {
+  char msg[320];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(msg, sizeof(msg), fmt, ap);
+  va_end(ap);
+  record_last_error(msg);
+  return code;
+}
+
+#define PC(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return pool_fail(e_ == cudaErrorMemoryAllocation ? WG_ERR_NOMEM : WG_ERR_CUDA,    \
+                       "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                       __LINE__);                                                       \
+  } while (0)
+
+u128 fixed_of(double m, int E) {
+  uint64_t b;
+  std::memcpy(&b, &m, 8);
+  int ex = (int)((b >> 52) & 0x7FF);
+  uint64_t mant = b & 0xFFFFFFFFFFFFFull;
+  if (ex == 0) {
+    if (mant == 0) return 0;
+    ex = 1;
+  } else {
+    mant |= 1ull << 52;
+  }
+  const int s = ex - 1075 + E;
+  if (s >= 0) return ((u128)mant) << s;
+  const int r = -s;
+  if (r > 54) return 0;
+  return (u128)((mant + (1ull << (r - 1))) >> r);
+}
+
+// Persistent device memory of one simulation, in one allocation.
+struct PoolSim {
+  int64_t n = 0, nb = 0;
+  void* mem = nullptr;
+  size_t bytes = 0;
+  double* bx[2];
+  double* bv[2];
+  double* bm[2];
+  int32_t* bi[2];
+  unsigned* bcnt[2];
+  uint64_t* qk[2];
+  int32_t* qi[2];
+  BucketRec* recs;
+  double *ox, *ov, *om;  // overflow list; also the compact (unsorted) store in mode 0
+  int32_t* oi;
+  double *x_out, *v_out;
+  uint64_t T_lo = 0, T_hi = 0;
+  int E = 0;
+  double totmass = 0, omega2 = -1;
+  ExtForce ext{};
+  int mode = 0;  // 0: sheets compact in ox..oi, half drift pending; 1: bucket layout
+  int lay = 0, qsel = 0;
+  double pending_dt = 0;
+  bool fresh = false;      // just bucketized: the opening half drift is already applied
+  bool out_valid = false;  // x_out / v_out hold the last output
+};
+
+size_t sim_bytes(int64_t n) {
+  const int64_t nb = (n + kBucketTarget - 1) / kBucketTarget;
+  const size_t slots = (size_t)nb * kBucketCap;
+  return 2 * (3 * al(slots * 8) + al(slots * 4)) + 2 * al(4 * (size_t)nb) +
+         2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
+         al(sizeof(BucketRec) * (size_t)nb) + 3 * al(8 * (size_t)n) + al(4 * (size_t)n) +
+         2 * al(8 * (size_t)n);
+}
+
+void carve(PoolSim* s) {
+  const size_t slots = (size_t)s->nb * kBucketCap;
+  char* p = static_cast<char*>(s->mem);
+  for (int k = 0; k < 2; ++k) {
+    s->bx[k] = reinterpret_cast<double*>(p); p += al(slots * 8);
+    s->bv[k] = reinterpret_cast<double*>(p); p += al(slots * 8);
+    s->bm[k] = reinterpret_cast<double*>(p); p += al(slots * 8);
+    s->bi[k] = reinterpret_cast<int32_t*>(p); p += al(slots * 4);
+  }
+  for (int k = 0; k < 2; ++k) {
+    s->bcnt[k] = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)s->nb);
+  }
+  for (int k = 0; k < 2; ++k) {
+    s->qk[k] = reinterpret_cast<uint64_t*>(p); p += al(8 * (size_t)(s->nb + 1));
+    s->qi[k] = reinterpret_cast<int32_t*>(p); p += al(4 * (size_t)(s->nb + 1));
+  }
+  s->recs = reinterpret_cast<BucketRec*>(p); p += al(sizeof(BucketRec) * (size_t)s->nb);
+  s->ox = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
+  s->ov = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
+  s->om = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
+  s->oi = reinterpret_cast<int32_t*>(p); p += al(4 * (size_t)s->n);
+  s->x_out = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
+  s->v_out = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
+}
+
+__global__ void k_set_table(StateTable* t, StateRef cur, StateRef other) {
+  t->cur = cur;
+  t->other = other;
+}
+
+__global__ void k_iota_i32(int32_t* p, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    p[i] = (int32_t)i;
+}
+
+// Copy the current compact set into a simulation's compact store.
+__global__ void k_store_compact(const StateTable* t, int64_t n, double* x, double* v,
+                                double* m, int32_t* idx) {
+  const StateRef c = t->cur;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    x[i] = c.x[i];
+    v[i] = c.v[i];
+    m[i] = c.m[i];
+    idx[i] = c.idx[i];
+  }
+}
+
+}  // namespace
+
+struct wg_pool {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int sms = 152;
+  int64_t budget = 0;  // bytes, 0 = no limit
+  int64_t used = 0;
+  std::vector<PoolSim*> sims;
+  // shared workspace for the compact path, sized for ws_n sheets
+  int64_t ws_n = 0;
+  void* ws = nullptr;
+  StateRef set[2];
+  TileRec* trecs = nullptr;
+  RadixWork radix;
+  unsigned* offs = nullptr;
+  // small per-call arrays (device) and their pinned mirrors
+  void* small = nullptr;
+  int cap_sims = 0, cap_leap = 0;
+  int64_t cap_tasks = 0;
+  StateTable* table = nullptr;
+  unsigned* err = nullptr;
+  StepFlags* wflags = nullptr;    // [cap_leap + 1] for the compact path
+  unsigned* tickets = nullptr;    // [cap_leap]
+  unsigned* epochs = nullptr;     // [cap_leap]
+  SimDev* d_dev = nullptr;        // [cap_sims]
+  StepFlags* flags = nullptr;     // [cap_sims * (cap_leap + 1)]
+  double* t_seq = nullptr;        // [cap_sims * cap_leap]
+  unsigned* ocount = nullptr;     // [cap_sims * 2]
+  BucketTask* tasks = nullptr;    // [cap_tasks]
+  SimDev* h_dev = nullptr;
+  double* h_t = nullptr;
+  unsigned* h_ep = nullptr;
+  unsigned* h_oc = nullptr;
+  BucketTask* h_tasks = nullptr;
+  unsigned epoch = 1;
+  int64_t launches = 0;
+};
+
+namespace {
+
+void free_small(wg_pool* p) {
+  if (p->small) cudaFree(p->small);
+  if (p->h_dev) cudaFreeHost(p->h_dev);
+  if (p->h_t) cudaFreeHost(p->h_t);
+  if (p->h_ep) cudaFreeHost(p->h_ep);
+  if (p->h_oc) cudaFreeHost(p->h_oc);
+  if (p->h_tasks) cudaFreeHost(p->h_tasks);
+  p->small = nullptr;
+  p->h_dev = nullptr;
+  p->h_t = nullptr;
+  p->h_ep = nullptr;
+  p->h_oc = nullptr;
+  p->h_tasks = nullptr;
+}
+
+int ensure_small(wg_pool* p, int nsims, int nleap, int64_t ntasks) {
+  if (nsims <= p->cap_sims && nleap <= p->cap_leap && ntasks <= p->cap_tasks && p->small)
+    return WG_OK;
+  PC(cudaStreamSynchronize(p->stream));
+  int cs = p->cap_sims > 16 ? p->cap_sims : 16, cl = p->cap_leap > 64 ? p->cap_leap : 64;
+  int64_t ct = p->cap_tasks > 1024 ? p->cap_tasks : 1024;
+  while (cs < nsims) cs *= 2;
+  while (cl < nleap) cl *= 2;
+  while (ct < ntasks) ct *= 2;
+  free_small(p);
+  const size_t b = al(sizeof(StateTable)) + al(64) + al(sizeof(StepFlags) * (cl + 1)) +
+                   2 * al(4 * (size_t)cl) + al(sizeof(SimDev) * (size_t)cs) +
+                   al(sizeof(StepFlags) * (size_t)cs * (cl + 1)) + al(8 * (size_t)cs * cl) +
+                   al(8 * (size_t)cs) + al(sizeof(BucketTask) * (size_t)ct);
+  PC(cudaMalloc(&p->small, b));
+  char* q = static_cast<char*>(p->small);
+  p->table = reinterpret_cast<StateTable*>(q); q += al(sizeof(StateTable));
+  p->err = reinterpret_cast<unsigned*>(q); q += al(64);
+  p->wflags = reinterpret_cast<StepFlags*>(q); q += al(sizeof(StepFlags) * (cl + 1));
+  p->tickets = reinterpret_cast<unsigned*>(q); q += al(4 * (size_t)cl);
+  p->epochs = reinterpret_cast<unsigned*>(q); q += al(4 * (size_t)cl);
+  p->d_dev = reinterpret_cast<SimDev*>(q); q += al(sizeof(SimDev) * (size_t)cs);
+  p->flags = reinterpret_cast<StepFlags*>(q); q += al(sizeof(StepFlags) * (size_t)cs * (cl + 1));
+  p->t_seq = reinterpret_cast<double*>(q); q += al(8 * (size_t)cs * cl);
+  p->ocount = reinterpret_cast<unsigned*>(q); q += al(8 * (size_t)cs);
+  p->tasks = reinterpret_cast<BucketTask*>(q); q += al(sizeof(BucketTask) * (size_t)ct);
+  PC(cudaMemsetAsync(p->small, 0, b, p->stream));
+  PC(cudaMallocHost(&p->h_dev, sizeof(SimDev) * (size_t)cs));
+  PC(cudaMallocHost(&p->h_t, 8 * (size_t)cs * cl));
+  PC(cudaMallocHost(&p->h_ep, 4 * (size_t)cl));
+  PC(cudaMallocHost(&p->h_oc, 8 * (size_t)cs));
+  PC(cudaMallocHost(&p->h_tasks, sizeof(BucketTask) * (size_t)ct));
+  p->cap_sims = cs;
+  p->cap_leap = cl;
+  p->cap_tasks = ct;
+  return WG_OK;
+}
+
+int ensure_workspace(wg_pool* p, int64_t n) {
+  if (n <= p->ws_n && p->ws) return WG_OK;
+  PC(cudaStreamSynchronize(p->stream));
+  if (p->ws) cudaFree(p->ws);
+  p->ws = nullptr;
+  const size_t nd = al((size_t)n * 8), ni = al((size_t)n * 4);
+  const int64_t tiles = (n + kForceTile - 1) / kForceTile;
+  const int64_t nb = (n + kBucketTarget - 1) / kBucketTarget;
+  const size_t b = 2 * (3 * nd + ni) + al(sizeof(TileRec) * (size_t)tiles) + radix_bytes(n) +
+                   al(4 * (size_t)nb);
+  PC(cudaMalloc(&p->ws, b));
+  char* q = static_cast<char*>(p->ws);
+  for (int k = 0; k < 2; ++k) {
+    p->set[k].x = reinterpret_cast<double*>(q); q += nd;
+    p->set[k].v = reinterpret_cast<double*>(q); q += nd;
+    p->set[k].m = reinterpret_cast<double*>(q); q += nd;
+    p->set[k].idx = reinterpret_cast<int32_t*>(q); q += ni;
+  }
+  p->trecs = reinterpret_cast<TileRec*>(q); q += al(sizeof(TileRec) * (size_t)tiles);
+  radix_bind(&p->radix, q, n);
+  q += radix_bytes(n);
+  p->offs = reinterpret_cast<unsigned*>(q);
+  PC(cudaMemsetAsync(p->trecs, 0, sizeof(TileRec) * (size_t)tiles, p->stream));
+  p->ws_n = n;
+  return WG_OK;
+}
+
+int grid_1d(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  if (g > 152 * 8) g = 152 * 8;
+  return (int)(g < 1 ? 1 : g);
+}
+
+// Bring a mode-0 simulation to its bucket layout: half drift of dt/2 on the
+// compact store, full radix sort, bucketize.  Uses the shared workspace.
+int to_buckets(wg_pool* p, PoolSim* s, double dt) {
+  int rc = ensure_workspace(p, s->n);
+  if (rc) return rc;
+  StateRef own{s->ox, s->ov, s->om, s->oi};
+  k_set_table<<<1, 1, 0, p->stream>>>(p->table, own, p->set[1]);
+  launch_drift(p->table, s->n, dt / 2., &p->wflags[0], p->stream);  // also marks "unsorted"
+  radix_sort_state(p->table, s->n, &p->radix, &p->wflags[0], p->err, p->stream);
+  launch_bucketize(p->table, s->n, kBucketTarget, s->nb, s->bx[0], s->bv[0], s->bm[0],
+                   s->bi[0], s->bcnt[0], s->qk[0], s->qi[0], s->bcnt[1], p->stream);
+  p->launches += 3 + kRadixLaunches;
+  s->lay = 0;
+  s->qsel = 0;
+  s->mode = 1;
+  s->pending_dt = dt;
+  return WG_OK;
+}
+
+// Bucket layout `lay` of s (+ the overflow entries counted in oc) -> the
+// workspace's first set, unsorted.
+void buckets_to_workspace(wg_pool* p, PoolSim* s, int lay, const unsigned* oc) {
+  k_set_table<<<1, 1, 0, p->stream>>>(p->table, p->set[0], p->set[1]);
+  launch_compact(p->table, s->nb, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay], s->bcnt[lay],
+                 p->offs, s->ox, s->ov, s->om, s->oi, oc, s->n, p->stream);
+  p->launches += 3;
+}
+
+void store_compact(wg_pool* p, PoolSim* s) {
+  k_store_compact<<<grid_1d(s->n), 256, 0, p->stream>>>(p->table, s->n, s->ox, s->ov, s->om,
+                                                          s->oi);
+  p->launches += 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t wg_pool_sim_bytes(int64_t n) { return n < 1 ? 0 : (int64_t)sim_bytes(n); }
+
+int wg_pool_create(int64_t budget_bytes, wg_pool** out) {
+  if (!out) return pool_fail(WG_ERR_ARG, "null output handle");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return pool_fail(WG_ERR_NODEV, "no CUDA device visible");
+  }
+  wg_pool* p = new wg_pool();
+  p->budget = budget_bytes > 0 ? budget_bytes : 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess) {
+    delete p;
+    return pool_fail(WG_ERR_CUDA, "stream/event creation failed");
+  }
+  int rc = ensure_small(p, 16, 64, 1024);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return WG_OK;
+}
+
+int wg_pool_add(wg_pool* p, int64_t n, const double* x, const double* v, const double* m,
+                double totmass, double omega2, int ext_kind, const double* ext_params,
+                int n_ext_params, int* sim_id) {
+  if (!p || !sim_id) return pool_fail(WG_ERR_ARG, "null argument");
+  if (n < 1 || n >= (1ll << 30)) return pool_fail(WG_ERR_ARG, "n outside [1, 2^30)");
+  if (!x || !v || !m) return pool_fail(WG_ERR_ARG, "null array");
+  if (!std::isfinite(totmass) || totmass < 0 || !std::isfinite(omega2))
+    return pool_fail(WG_ERR_ARG, "totmass must be finite and >= 0, omega2 finite");
+  double mmax = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!(m[i] >= 0) || !std::isfinite(m[i]) || !std::isfinite(x[i]) || !std::isfinite(v[i]))
+      return pool_fail(WG_ERR_ARG, "sheet %lld: non-finite value or negative mass", (long long)i);
+    if (m[i] > mmax) mmax = m[i];
+  }
+  if (mmax > 2 * totmass)
+    return pool_fail(WG_ERR_ARG, "a single mass exceeds twice totmass");
+  ExtForce ext;
+  ext.kind = ext_kind;
+  for (int i = 0; i < 4; ++i) ext.p[i] = 0.0;
+  const int need = ext_kind == WG_EXT_NONE ? 0 : ext_kind == WG_EXT_HARMONIC ? 1
+                 : ext_kind == WG_EXT_PULSE_TANH ? 4 : -1;
+  if (need < 0 || n_ext_params < need || (need > 0 && !ext_params))
+    return pool_fail(WG_ERR_EXT, "unknown external force %d or too few parameters", ext_kind);
+  for (int i = 0; i < need; ++i) ext.p[i] = ext_params[i];
+  if (ext_kind == WG_EXT_PULSE_TANH && (ext.p[2] == 0.0 || ext.p[3] == 0.0))
+    return pool_fail(WG_ERR_EXT, "pulsed force needs tau != 0 and h != 0");
+  const size_t bytes = sim_bytes(n);
+  if (p->budget && p->used + (int64_t)bytes > p->budget)
+    return pool_fail(WG_ERR_BUDGET, "simulation of %lld sheets needs %zu bytes; %lld of %lld in use",
+                     (long long)n, bytes, (long long)p->used, (long long)p->budget);
+  PoolSim* s = new PoolSim();
+  s->n = n;
+  s->nb = (n + kBucketTarget - 1) / kBucketTarget;
+  s->bytes = bytes;
+  cudaError_t e = cudaMallocAsync(&s->mem, bytes, p->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete s;
+    return pool_fail(WG_ERR_NOMEM, "allocation of %zu bytes failed: %s", bytes,
+                     cudaGetErrorString(e));
+  }
+  carve(s);
+  s->totmass = totmass;
+  s->omega2 = omega2;
+  s->ext = ext;
+  if (totmass > 0) {
+    int eT = 0;
+    std::frexp(totmass, &eT);
+    s->E = 123 - eT;
+  }
+  const u128 T = fixed_of(totmass, s->E);
+  s->T_lo = (uint64_t)T;
+  s->T_hi = (uint64_t)(T >> 64);
+  PC(cudaMemsetAsync(s->recs, 0, sizeof(BucketRec) * (size_t)s->nb, p->stream));
+  PC(cudaMemcpyAsync(s->ox, x, 8 * (size_t)n, cudaMemcpyHostToDevice, p->stream));
+  PC(cudaMemcpyAsync(s->ov, v, 8 * (size_t)n, cudaMemcpyHostToDevice, p->stream));
+  PC(cudaMemcpyAsync(s->om, m, 8 * (size_t)n, cudaMemcpyHostToDevice, p->stream));
+  k_iota_i32<<<grid_1d(n), 256, 0, p->stream>>>(s->oi, n);
+  PC(cudaStreamSynchronize(p->stream));
+  p->used += (int64_t)bytes;
+  int id = -1;
+  for (size_t i = 0; i < p->sims.size(); ++i)
+    if (!p->sims[i]) {
+      id = (int)i;
+      break;
+    }
+  if (id < 0) {
+    id = (int)p->sims.size();
+    p->sims.push_back(nullptr);
+  }
+  p->sims[(size_t)id] = s;
+  *sim_id = id;
+  return WG_OK;
+}
+
+int wg_pool_remove(wg_pool* p, int sim_id) {
+  if (!p || sim_id < 0 || (size_t)sim_id >= p->sims.size() || !p->sims[(size_t)sim_id])
+    return pool_fail(WG_ERR_ARG, "no simulation %d in the pool", sim_id);
+  PoolSim* s = p->sims[(size_t)sim_id];
+  cudaFreeAsync(s->mem, p->stream);
+  p->used -= (int64_t)s->bytes;
+  delete s;
+  p->sims[(size_t)sim_id] = nullptr;
+  return WG_OK;
+}
+
+int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nleap, double* t0,
+                 double* time_elapsed) {
+  if (!p || count < 1 || !ids || !dt || nleap < 1)
+    return pool_fail(WG_ERR_ARG, "bad arguments to wg_pool_step");
+  std::vector<PoolSim*> act((size_t)count);
+  int64_t ntasks = 0;
+  for (int k = 0; k < count; ++k) {
+    if (ids[k] < 0 || (size_t)ids[k] >= p->sims.size() || !p->sims[(size_t)ids[k]])
+      return pool_fail(WG_ERR_ARG, "no simulation %d in the pool", ids[k]);
+    if (!std::isfinite(dt[k])) return pool_fail(WG_ERR_ARG, "dt of simulation %d", ids[k]);
+    for (int j = 0; j < k; ++j)
+      if (ids[j] == ids[k]) return pool_fail(WG_ERR_ARG, "simulation %d listed twice", ids[k]);
+    act[(size_t)k] = p->sims[(size_t)ids[k]];
+    ntasks += act[(size_t)k]->nb;
+  }
+  if (ntasks >= (1ll << 31)) return pool_fail(WG_ERR_ARG, "too many buckets in one step");
+  int rc = ensure_small(p, count, nleap, ntasks);
+  if (rc) return rc;
+  const int L1 = p->cap_leap;
+  // times (the reference's lagged, repeatedly added t) and epochs
+  for (int k = 0; k < count; ++k) {
+    double t = t0 ? t0[k] : 0.0;
+    for (int i = 0; i < nleap; ++i) {
+      p->h_t[(size_t)k * L1 + i] = t;
+      if (act[(size_t)k]->ext.kind != EXT_NONE) t += dt[k];
+    }
+    if (t0) t0[k] = t;
+  }
+  if (p->epoch + (unsigned)nleap + 2 > (1u << 29)) {
+    // restart epochs: forget every look-back record
+    for (PoolSim* s : p->sims)
+      if (s) PC(cudaMemsetAsync(s->recs, 0, sizeof(BucketRec) * (size_t)s->nb, p->stream));
+    if (p->ws)
+      PC(cudaMemsetAsync(p->trecs, 0,
+                         sizeof(TileRec) * (size_t)((p->ws_n + kForceTile - 1) / kForceTile),
+                         p->stream));
+    p->epoch = 1;
+  }
+  for (int i = 0; i < nleap; ++i) p->h_ep[i] = p->epoch + (unsigned)i;
+  p->epoch += (unsigned)nleap;
+  PC(cudaEventRecord(p->ev0, p->stream));
+  PC(cudaMemcpyAsync(p->t_seq, p->h_t, 8 * (size_t)count * L1, cudaMemcpyHostToDevice,
+                     p->stream));
+  PC(cudaMemcpyAsync(p->epochs, p->h_ep, 4 * (size_t)nleap, cudaMemcpyHostToDevice, p->stream));
+  PC(cudaMemsetAsync(p->tickets, 0, 4 * (size_t)nleap, p->stream));
+  PC(cudaMemsetAsync(p->ocount, 0, 8 * (size_t)count, p->stream));
+  PC(cudaMemsetAsync(p->flags, 0, sizeof(StepFlags) * (size_t)count * (L1 + 1), p->stream));
+  // simulations that are compact, or routed for another dt, re-sort first
+  for (int k = 0; k < count; ++k) {
+    PoolSim* s = act[(size_t)k];
+    if (s->mode == 1 && dt[k] != s->pending_dt) {
+      rc = ensure_workspace(p, s->n);
+      if (rc) return rc;
+      buckets_to_workspace(p, s, s->lay, p->ocount + 2 * k);
+      store_compact(p, s);
+      s->mode = 0;
+    }
+    if (s->mode == 0) {
+      PC(cudaMemsetAsync(&p->wflags[0], 0, sizeof(StepFlags), p->stream));
+      rc = to_buckets(p, s, dt[k]);
+      if (rc) return rc;
+      s->fresh = true;
+    }
+  }
+  // the kernel's view of every simulation, and the task list
+  int64_t t = 0;
+  for (int k = 0; k < count; ++k) {
+    PoolSim* s = act[(size_t)k];
+    SimDev& d = p->h_dev[k];
+    for (int j = 0; j < 2; ++j) {
+      d.bx[j] = s->bx[j];
+      d.bv[j] = s->bv[j];
+      d.bm[j] = s->bm[j];
+      d.bi[j] = s->bi[j];
+      d.bcnt[j] = s->bcnt[j];
+      d.qk[j] = s->qk[j];
+      d.qi[j] = s->qi[j];
+    }
+    d.recs = s->recs;
+    d.ox = s->ox;
+    d.ov = s->ov;
+    d.om = s->om;
+    d.oi = s->oi;
+    d.ocount = p->ocount + 2 * k;
+    d.x_out = s->x_out;
+    d.v_out = s->v_out;
+    d.flags = p->flags + (size_t)k * (L1 + 1);
+    d.t_seq = p->t_seq + (size_t)k * L1;
+    d.n = s->n;
+    d.nb = s->nb;
+    d.T_lo = s->T_lo;
+    d.T_hi = s->T_hi;
+    d.E = s->E;
+    d.has_omega = s->omega2 >= 0;
+    d.omega2 = s->omega2;
+    d.ext = s->ext;
+    d.dt = dt[k];
+    d.pre_dt = s->fresh ? 0.0 : dt[k] / 2.;
+    d.lay0 = s->lay;
+    d.qsel0 = s->qsel;
+    for (int64_t b = 0; b < s->nb; ++b) p->h_tasks[t++] = BucketTask{k, (int)b};
+  }
+  PC(cudaMemcpyAsync(p->d_dev, p->h_dev, sizeof(SimDev) * (size_t)count, cudaMemcpyHostToDevice,
+                     p->stream));
+  PC(cudaMemcpyAsync(p->tasks, p->h_tasks, sizeof(BucketTask) * (size_t)ntasks,
+                     cudaMemcpyHostToDevice, p->stream));
+  const int grid = bucket_step_grid(p->sms);
+  for (int i = 0; i < nleap; ++i) {
+    StepLaunch L;
+    L.sims = p->d_dev;
+    L.tasks = p->tasks;
+    L.ntasks = (int)ntasks;
+    L.sub = i;
+    L.nleap = nleap;
+    L.epochs = p->epochs;
+    L.ticket = p->tickets + i;
+    L.err = p->err;
+    L.profile = 0;
+    launch_bucket_step(L, grid, p->stream);
+  }
+  p->launches += nleap;
+  PC(cudaGetLastError());
+  PC(cudaMemcpyAsync(p->h_oc, p->ocount, 8 * (size_t)count, cudaMemcpyDeviceToHost, p->stream));
+  PC(cudaStreamSynchronize(p->stream));
+  // bookkeeping, and recovery of simulations that overflowed a bucket
+  for (int k = 0; k < count; ++k) {
+    PoolSim* s = act[(size_t)k];
+    const int lay0 = s->lay;
+    s->lay = (lay0 + nleap) & 1;
+    s->qsel = (s->qsel + nleap) & 1;
+    s->mode = 1;
+    s->pending_dt = dt[k];
+    s->fresh = false;
+    s->out_valid = true;
+    const unsigned ab = p->h_oc[2 * k + 1];
+    if (!ab) continue;
+    const int kk = (int)ab - 1;  // sub-step that overflowed
+    const int lay_k = (kk % 2 == 0) ? 1 - lay0 : lay0;
+    rc = ensure_workspace(p, s->n);
+    if (rc) return rc;
+    buckets_to_workspace(p, s, lay_k, p->ocount + 2 * k);
+    if (kk < nleap - 1) {
+      ForceArgs f;
+      f.table = p->table;
+      f.n = s->n;
+      f.T_lo = s->T_lo;
+      f.T_hi = s->T_hi;
+      f.E = s->E;
+      f.has_omega = s->omega2 >= 0;
+      f.omega2 = s->omega2;
+      f.ext = s->ext;
+      f.t_seq = p->t_seq + (size_t)k * L1;
+      f.epochs = p->epochs;
+      f.recs = p->trecs;
+      f.err = p->err;
+      f.a_out = nullptr;
+      const int64_t tiles = (s->n + kForceTile - 1) / kForceTile;
+      PC(cudaMemsetAsync(p->tickets, 0, 4 * (size_t)nleap, p->stream));
+      for (int i = kk + 1; i < nleap; ++i) {
+        const StepFlags one{1u, 0u, 0ull};
+        PC(cudaMemcpyAsync(&p->wflags[i], &one, sizeof(one), cudaMemcpyHostToDevice, p->stream));
+        radix_sort_state(p->table, s->n, &p->radix, &p->wflags[i], p->err, p->stream);
+        f.sub = i;
+        f.dt_kick = dt[k];
+        f.dt_drift = (i == nleap - 1) ? dt[k] / 2. : dt[k];
+        f.ticket = p->tickets + i;
+        f.flag_out = &p->wflags[i + 1];
+        launch_force(f, tiles, p->stream);
+        PC(cudaStreamSynchronize(p->stream));
+      }
+      launch_desort(p->table, s->n, s->x_out, s->v_out, p->stream);
+      p->launches += (int64_t)(nleap - kk - 1) * (1 + kRadixLaunches) + 1;
+    }
+    store_compact(p, s);
+    s->mode = 0;
+  }
+  PC(cudaEventRecord(p->ev1, p->stream));
+  unsigned err = 0;
+  PC(cudaMemcpyAsync(&err, p->err, 4, cudaMemcpyDeviceToHost, p->stream));
+  PC(cudaStreamSynchronize(p->stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+  if (time_elapsed) *time_elapsed = ms * 1e-3;
+  if (err) {
+    cudaMemsetAsync(p->err, 0, 4, p->stream);
+    return pool_fail(WG_ERR_DEVICE, "device error word 0x%x", err);
+  }
+  return WG_OK;
+}
+
+int wg_pool_download(wg_pool* p, int sim_id, double* x, double* v) {
+  if (!p || sim_id < 0 || (size_t)sim_id >= p->sims.size() || !p->sims[(size_t)sim_id])
+    return pool_fail(WG_ERR_ARG, "no simulation %d in the pool", sim_id);
+  PoolSim* s = p->sims[(size_t)sim_id];
+  if (!s->out_valid) return pool_fail(WG_ERR_ARG, "simulation %d has not been stepped", sim_id);
+  if (x) PC(cudaMemcpyAsync(x, s->x_out, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->stream));
+  if (v) PC(cudaMemcpyAsync(v, s->v_out, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->stream));
+  PC(cudaStreamSynchronize(p->stream));
+  return WG_OK;
+}
+
+int wg_pool_info(wg_pool* p, int64_t* used_bytes, int64_t* budget_bytes, int* n_sims,
+                 int64_t* launches) {
+  if (!p) return pool_fail(WG_ERR_ARG, "null pool");
+  int c = 0;
+  for (PoolSim* s : p->sims) c += s ? 1 : 0;
+  if (used_bytes) *used_bytes = p->used;
+  if (budget_bytes) *budget_bytes = p->budget;
+  if (n_sims) *n_sims = c;
+  if (launches) *launches = p->launches;
+  return WG_OK;
+}
+
+int wg_pool_destroy(wg_pool* p) {
+  if (!p) return WG_OK;
+  cudaStreamSynchronize(p->stream);
+  for (PoolSim* s : p->sims)
+    if (s) {
+      cudaFreeAsync(s->mem, p->stream);
+      delete s;
+    }
+  cudaStreamSynchronize(p->stream);
+  if (p->ws) cudaFree(p->ws);
+  free_small(p);
+  if (p->ev0) cudaEventDestroy(p->ev0);
+  if (p->ev1) cudaEventDestroy(p->ev1);
+  if (p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+  return WG_OK;
+}
+
+}  // extern "C"
