@@ -86,6 +86,7 @@ struct StepSmem {
   double amp;
   unsigned epoch;
   unsigned long long maxv;
+  uint64_t mbar;  // completion of the bucket's bulk copies
 };
 
 __device__ __forceinline__ bool pair_less(uint64_t k1, int32_t i1, uint64_t k2, int32_t i2) {
@@ -251,22 +252,25 @@ __device__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin, uint64_t
     if (i < ipt && j < n) S.perm[bins[binp(qv[i])] + rk[i]] = (uint16_t)j;
   }
   __syncthreads();
-  // the order inside a bin came from atomics: sort each bin by (key, idx)
+  // The order inside a bin came from atomics: sort each bin with two or more
+  // sheets by (key, idx).  The sheet that arrived second in a bin does it,
+  // so only occupied bins cost anything.
 #pragma unroll
-  for (int k = 0; k < PER; ++k) {
-    const int q = tid * PER + k;
-    const uint32_t lo = bins[binp(q)], hi = bins[binp(q + 1)];
-    if (hi - lo < 2) continue;
-    for (uint32_t a = lo + 1; a < hi; ++a) {
-      const uint16_t s = S.perm[a];
-      const uint64_t ks = S.key[s];
-      const int32_t is = S.idx[s];
-      int b = (int)a - 1;
-      while (b >= (int)lo && pair_less(ks, is, S.key[S.perm[b]], S.idx[S.perm[b]])) {
-        S.perm[b + 1] = S.perm[b];
-        --b;
+  for (int i = 0; i < MAXI; ++i) {
+    const int j = tid + i * BT;
+    if (i < ipt && j < n && rk[i] == 1) {
+      const uint32_t lo = bins[binp(qv[i])], hi = bins[binp(qv[i] + 1)];
+      for (uint32_t a = lo + 1; a < hi; ++a) {
+        const uint16_t s = S.perm[a];
+        const uint64_t ks = S.key[s];
+        const int32_t is = S.idx[s];
+        int b = (int)a - 1;
+        while (b >= (int)lo && pair_less(ks, is, S.key[S.perm[b]], S.idx[S.perm[b]])) {
+          S.perm[b + 1] = S.perm[b];
+          --b;
+        }
+        S.perm[b + 1] = s;
       }
-      S.perm[b + 1] = s;
     }
   }
   __syncthreads();
@@ -381,7 +385,12 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int sub = L.sub;
   const bool last = sub == L.nleap - 1;
-  if (tid == 0) S.epoch = L.epochs[sub];
+  if (tid == 0) {
+    S.epoch = L.epochs[sub];
+    mbar_init(&S.mbar, 1);
+    fence_proxy_async_smem();
+  }
+  unsigned parity = 0;
   for (;;) {
     __syncthreads();
     if (tid == 0) {
@@ -421,27 +430,35 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       cnt_in[b] = 0;  // this count buffer is the target two sub-steps on
       S.amp = (D.ext.kind == EXT_PULSE_TANH) ? pulse_amplitude(D.ext, D.t_seq[sub]) : 0.0;
     }
-    // ---- load, with the bucket's mass and count
+    // ---- load: the bucket's four arrays arrive by bulk copy (sizes rounded
+    // up to 4 sheets, which stays inside the bucket's capacity), then its
+    // keys, key range, mass and count are formed from shared memory
+    const int n4 = (n + 3) & ~3;
+    if (n4 > 0) {
+      if (tid == 0) {
+        fence_proxy_async_smem();  // earlier generic accesses to these buffers are done
+        mbar_expect_tx(&S.mbar, (uint32_t)n4 * 28u);
+        bulk_g2s(S.x, xin + base, (uint32_t)n4 * 8u, &S.mbar);
+        bulk_g2s(S.v, vin + base, (uint32_t)n4 * 8u, &S.mbar);
+        bulk_g2s(S.m, min + base, (uint32_t)n4 * 8u, &S.mbar);
+        bulk_g2s(S.idx, iin + base, (uint32_t)n4 * 4u, &S.mbar);
+      }
+      if (!mbar_wait(&S.mbar, parity) && tid == 0) atomicOr(L.err, DEV_ERR_BAD_STATE);
+      parity ^= 1u;
+    }
     uint64_t kmin = ~0ull, kmax = 0;
     u128 msum = 0;
-#pragma unroll
-    for (int i = 0; i < MAXI; ++i) {
-      const int j = tid + i * BT;
-      if (i < ipt && j < n) {
-        const double v = vin[base + j];
-        double x = xin[base + j];
-        if (pre != 0.0) x = fma(pre, v, x);
-        const uint64_t k = key_of(x);
-        const double mj = min[base + j];
+    for (int j = tid; j < n; j += BT) {
+      double x = S.x[j];
+      if (pre != 0.0) {
+        x = fma(pre, S.v[j], x);
         S.x[j] = x;
-        S.v[j] = v;
-        S.m[j] = mj;
-        S.idx[j] = iin[base + j];
-        S.key[j] = k;
-        kmin = k < kmin ? k : kmin;
-        kmax = k > kmax ? k : kmax;
-        msum += mass_to_fixed(mj, E);
       }
+      const uint64_t k = key_of(x);
+      S.key[j] = k;
+      kmin = k < kmin ? k : kmin;
+      kmax = k > kmax ? k : kmax;
+      msum += mass_to_fixed(S.m[j], E);
     }
     // splitter window of the next layout around this bucket
     const int wlo = (int)(b > RWIN ? b - RWIN : 0);
