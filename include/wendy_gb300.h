@@ -102,6 +102,22 @@ int wg_destroy(wg_sim *s);
 #define WG_PROF_BUCKET 2
 int wg_profile(wg_sim *s, int what, int reps, double *avg_seconds);
 
+/* Tuning of the fused bucket sub-step by simulation size.  Row i applies to
+   simulations of n >= n_min[i] sheets (rows ascending in n_min) created after
+   the call: sheets per bucket after a re-sort (64..1024), splitter window
+   (1..64 buckets each side), counting-sort bits (8..12), persistent CTAs per
+   SM (1..2).  Written by the autotuner (wendy_gb300/autotune.py); no
+   reference counterpart. */
+typedef struct wg_tuning {
+  int64_t n_min;
+  int target;
+  int window;
+  int sort_bits;
+  int ctas_per_sm;
+} wg_tuning;
+int wg_set_tuning(const wg_tuning *rows, int nrows);
+int wg_get_tuning(int64_t n, wg_tuning *out);
+
 /* Page-lock (or release) caller memory so that downloads and uploads run
    at full link speed.  No reference counterpart (wendy's buffers are plain
    numpy arrays). */

@@ -26,7 +26,7 @@ EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", 
            "wg_nbody_approx_onestep", "wg_profile", "wg_host_register", "wg_host_unregister",
            "wg_accel_noalloc", "wg_pool_sim_bytes", "wg_pool_create", "wg_pool_add",
            "wg_pool_remove", "wg_pool_step", "wg_pool_download", "wg_pool_info",
-           "wg_pool_destroy")
+           "wg_pool_destroy", "wg_set_tuning", "wg_get_tuning")
 
 # Largest n wg_accel_noalloc accepts (its fixed device scratch array).
 NOALLOC_MAX_SHEETS = 65536
@@ -47,6 +47,11 @@ class WgStats(ctypes.Structure):
                 ("sorts_full", ctypes.c_int64), ("sorts_skipped", ctypes.c_int64),
                 ("sorts_window", ctypes.c_int64), ("last_max_disp", ctypes.c_double),
                 ("device_bytes", ctypes.c_int64), ("launches", ctypes.c_int64)]
+
+
+class WgTuning(ctypes.Structure):
+    _fields_ = [("n_min", ctypes.c_int64), ("target", ctypes.c_int), ("window", ctypes.c_int),
+                ("sort_bits", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
 
 
 class WendyGPUError(RuntimeError):
@@ -109,11 +114,16 @@ def lib():
     L.wg_pool_info.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                ctypes.POINTER(_I), ctypes.POINTER(_I64)]
     L.wg_pool_destroy.argtypes = [_P]
+    L.wg_set_tuning.argtypes = [_P, _I]
+    L.wg_get_tuning.argtypes = [_I64, ctypes.POINTER(WgTuning)]
     for name in EXPORTS:
         if name not in ("wg_status_string", "wg_last_error"):
             getattr(L, name).restype = _I
     L.wg_pool_sim_bytes.restype = _I64
     _lib = L
+    # the tuning table measured on a GB300 that ships with the package
+    from . import autotune
+    autotune.apply_shipped()
     return L
 
 

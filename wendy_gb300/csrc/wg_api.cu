@@ -141,6 +141,7 @@ struct wg_sim {
   double pending_dt = 0; // dt of the half drift the bucket layout was routed for
   bool out_valid = false;  // x_out / v_out hold the last call's output
   int grid_bucket = 0;
+  BucketTuning tune;             // bucket size, window, sort bits, CTAs per SM
   SimDev dev{};                  // host copy of the kernel's view of this simulation
   SimDev* d_dev = nullptr;       // device copy (one entry)
   BucketTask* d_tasks = nullptr; // [nb]: (0, b)
@@ -279,7 +280,8 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
   }
   // bucket layout: two layouts of nb buckets x capacity, counts, splitters,
   // look-back records, the overflow list
-  s->nb = (n + kBucketTarget - 1) / kBucketTarget;
+  s->tune = tuning_for(n);
+  s->nb = (n + s->tune.target - 1) / s->tune.target;
   const int64_t nb = s->nb;
   const size_t slots = (size_t)nb * kBucketCap;
   const size_t bk_b = 2 * (3 * al(slots * 8) + al(slots * 4)) + 2 * al(4 * (size_t)nb) +
@@ -338,7 +340,7 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     (void)per_sm;
-    s->grid_bucket = bucket_step_grid(sms);
+    s->grid_bucket = s->tune.ctas_per_sm * sms;
   }
   rc = alloc_call_arrays(s, 64);
   if (rc != WG_OK) return fail(rc);
@@ -480,6 +482,9 @@ void fill_dev(wg_sim* s, double dt, double pre) {
   d.t_seq = s->t_seq;
   d.n = s->n;
   d.nb = s->nb;
+  d.target = s->tune.target;
+  d.window = s->tune.window;
+  d.sort_bits = s->tune.sort_bits;
   d.T_lo = s->T_lo;
   d.T_hi = s->T_hi;
   d.E = s->E;
@@ -660,7 +665,7 @@ int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
     radix_sort_state(s->table, s->n, &s->radix, &s->flags[0], s->err, s->stream);
     s->lay = 0;
     s->qsel = 0;
-    launch_bucketize(s->table, s->n, kBucketTarget, s->nb, s->bx[0], s->bv[0], s->bm[0],
+    launch_bucketize(s->table, s->n, s->tune.target, s->nb, s->bx[0], s->bv[0], s->bm[0],
                      s->bi[0], s->bcnt[0], s->qk[0], s->qi[0], s->bcnt[1], s->stream);
     s->st.launches += 2 + kRadixLaunches;
     s->st.sorts_full += 1;
@@ -858,6 +863,47 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
     cudaMemset(s->err, 0, 4);
     return WG_ERR_DEVICE;
   }
+  return WG_OK;
+}
+
+int wg_set_tuning(const wg_tuning* rows, int nrows) {
+  if (nrows < 0 || (nrows > 0 && !rows)) {
+    set_error("bad tuning table");
+    return WG_ERR_ARG;
+  }
+  std::vector<std::pair<int64_t, BucketTuning>> t;
+  for (int i = 0; i < nrows; ++i) {
+    const wg_tuning& r = rows[i];
+    if (r.target < 64 || r.target > kBucketCap / 2 || r.window < 1 ||
+        r.window > kSplitterWindow || r.sort_bits < 8 || r.sort_bits > kSortBitsMax ||
+        r.ctas_per_sm < 1 || r.ctas_per_sm > 2 || (i > 0 && r.n_min < rows[i - 1].n_min)) {
+      set_error("tuning row %d out of range (target 64..%d, window 1..%d, sort_bits 8..%d, "
+                "ctas_per_sm 1..2, n_min ascending)", i, kBucketCap / 2, kSplitterWindow,
+                kSortBitsMax);
+      return WG_ERR_ARG;
+    }
+    BucketTuning b;
+    b.target = r.target;
+    b.window = r.window;
+    b.sort_bits = r.sort_bits;
+    b.ctas_per_sm = r.ctas_per_sm;
+    t.emplace_back(r.n_min, b);
+  }
+  set_tuning(t);
+  return WG_OK;
+}
+
+int wg_get_tuning(int64_t n, wg_tuning* out) {
+  if (!out) {
+    set_error("null output");
+    return WG_ERR_ARG;
+  }
+  const BucketTuning b = tuning_for(n);
+  out->n_min = 0;
+  out->target = b.target;
+  out->window = b.window;
+  out->sort_bits = b.sort_bits;
+  out->ctas_per_sm = b.ctas_per_sm;
   return WG_OK;
 }
 

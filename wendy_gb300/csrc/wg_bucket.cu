@@ -32,6 +32,9 @@
 // Reference: _nbody_force and leapfrog_leappq, wendy/wendy.c:324-384; the
 // argsort at wendy/wendy.c:341-357 is what the bucket sort replaces.
 #include <cstdint>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 #include "wg_bucket.cuh"
 
@@ -44,8 +47,7 @@ constexpr int CAP = kBucketCap;     // 2048
 constexpr int MAXI = CAP / BT;      // 8 sheets per thread at most
 constexpr int WARPS = BT / 32;
 constexpr int RWIN = kSplitterWindow;
-constexpr int QB = 12;              // bits of the counting-sort offset
-constexpr int NBIN = 1 << QB;       // 4096 bins
+constexpr int NBIN = 1 << kSortBitsMax;  // bins the shared memory is sized for
 constexpr int MAXBIN = 48;          // a fuller bin sends the bucket to the radix sort
 // Bins are padded with one word per 32 so that a thread scanning 16
 // consecutive bins and its 31 neighbours hit 32 different banks.
@@ -204,13 +206,16 @@ __device__ void lsd_sort(StepSmem& S, int n, uint64_t kmin, uint64_t kmax) {
 }
 
 // Sort the n <= CAP sheets of the bucket by (key, idx) into S.perm.
-__device__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin, uint64_t kmax) {
+__device__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin, uint64_t kmax,
+                            int qb) {
   const int tid = threadIdx.x;
   const uint64_t span = kmax - kmin;
   const int bits = span ? 64 - __clzll((long long)span) : 0;
-  const int shift = bits > QB ? bits - QB : 0;
+  const int shift = bits > qb ? bits - qb : 0;
+  const int nbin = 1 << qb;
+  const int per = nbin / BT;  // bins per thread in the scan (1..16)
   uint32_t* bins = S.u.bins;
-  for (int j = tid; j < NBIN_PAD; j += BT) bins[j] = 0;
+  for (int j = tid; j < binp(nbin) + 1; j += BT) bins[j] = 0;
   __syncthreads();
   uint16_t qv[MAXI], rk[MAXI];
 #pragma unroll
@@ -223,12 +228,12 @@ __device__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin, uint64_t
   }
   __syncthreads();
   // exclusive scan of the bins: thread t owns bins [16 t, 16 t + 16)
-  constexpr int PER = NBIN / BT;
-  uint32_t c[PER];
+  constexpr int PERMAX = NBIN / BT;
+  uint32_t c[PERMAX];
   uint32_t run = 0, mx = 0;
 #pragma unroll
-  for (int k = 0; k < PER; ++k) {
-    c[k] = bins[binp(tid * PER + k)];
+  for (int k = 0; k < PERMAX; ++k) {
+    c[k] = k < per ? bins[binp(tid * per + k)] : 0u;
     mx = c[k] > mx ? c[k] : mx;
     run += c[k];
   }
@@ -240,11 +245,11 @@ __device__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin, uint64_t
   uint32_t total;
   uint32_t off = block_excl_scan(S, run, total);
 #pragma unroll
-  for (int k = 0; k < PER; ++k) {
-    bins[binp(tid * PER + k)] = off;
+  for (int k = 0; k < PERMAX; ++k) {
+    if (k < per) bins[binp(tid * per + k)] = off;
     off += c[k];
   }
-  if (tid == 0) bins[binp(NBIN)] = (uint32_t)n;
+  if (tid == 0) bins[binp(nbin)] = (uint32_t)n;
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
@@ -443,11 +448,29 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
         bulk_g2s(S.m, min + base, (uint32_t)n4 * 8u, &S.mbar);
         bulk_g2s(S.idx, iin + base, (uint32_t)n4 * 4u, &S.mbar);
       }
+    }
+    // splitter window of the next layout around this bucket, fetched while
+    // the bulk copies are in flight
+    const int rw = D.window;
+    const int wlo = (int)(b > rw ? b - rw : 0);
+    const int whi = (int)((b + rw + 1) < D.nb ? (b + rw + 1) : D.nb);
+    for (int j = tid; j <= whi - wlo; j += BT) {
+      S.wkey[j] = qdk[wlo + j];
+      S.widx[j] = qdi[wlo + j];
+      S.dcount[j] = 0;
+    }
+    if (tid == 0) {
+      S.win_lo = wlo;
+      S.win_hi = whi;
+      S.maxv = 0;
+    }
+    if (n4 > 0) {
       if (!mbar_wait(&S.mbar, parity) && tid == 0) atomicOr(L.err, DEV_ERR_BAD_STATE);
       parity ^= 1u;
     }
     uint64_t kmin = ~0ull, kmax = 0;
     u128 msum = 0;
+#pragma unroll 4
     for (int j = tid; j < n; j += BT) {
       double x = S.x[j];
       if (pre != 0.0) {
@@ -459,19 +482,6 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       kmin = k < kmin ? k : kmin;
       kmax = k > kmax ? k : kmax;
       msum += mass_to_fixed(S.m[j], E);
-    }
-    // splitter window of the next layout around this bucket
-    const int wlo = (int)(b > RWIN ? b - RWIN : 0);
-    const int whi = (int)((b + RWIN + 1) < D.nb ? (b + RWIN + 1) : D.nb);
-    for (int j = tid; j <= whi - wlo; j += BT) {
-      S.wkey[j] = qdk[wlo + j];
-      S.widx[j] = qdi[wlo + j];
-      S.dcount[j] = 0;
-    }
-    if (tid == 0) {
-      S.win_lo = wlo;
-      S.win_hi = whi;
-      S.maxv = 0;
     }
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) {
@@ -506,7 +516,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     }
     // ---- sort the bucket (barriers inside wait for the look-back warp)
     if (n > 1) {
-      bucket_sort(S, n, ipt, kmin, kmax);
+      bucket_sort(S, n, ipt, kmin, kmax, D.sort_bits);
     } else {
       if (tid == 0) S.perm[0] = 0;
       __syncthreads();
@@ -560,39 +570,75 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     const double dest_dt = (last && !L.profile) ? dt / 2. : 0.0;
     const i128 T = (i128)((((u128)D.T_hi) << 64) | D.T_lo);
     unsigned long long maxv = 0;
-    for (int i = 0; i < nmine; ++i) {
-      const int s = S.perm[j0 + i];
-      const uint32_t r = rank0 + (uint32_t)i;
-      const uint64_t key = S.key[s];
-      const int32_t id = S.idx[s];
-      if (r != 0 && (r % (uint32_t)kBucketTarget) == 0) {
-        qnk[r / kBucketTarget] = key;
-        qni[r / kBucketTarget] = id;
+    // two sheets at a time, interleaved, so that their shared-memory and
+    // FP64 latencies overlap; the window searches run in lock-step
+    const int wlen = S.win_hi - S.win_lo;
+    int top = 1;
+    while ((top << 1) < wlen) top <<= 1;
+    for (int i0 = 0; i0 < nmine; i0 += 2) {
+      const bool ok1 = i0 + 1 < nmine;
+      int sl[2];
+      uint64_t kd[2];
+      int32_t idv[2];
+      bool live[2] = {true, ok1};
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        sl[u] = S.perm[j0 + (live[u] ? i0 + u : i0)];
+        idv[u] = S.idx[sl[u]];
       }
-      const double x = S.x[s], v = S.v[s];
-      const u128 M = mass_to_fixed(S.m[s], E);
-      const i128 A = T - 2 * (i128)C - (i128)M;
-      C += M;
-      double acc = fixed_to_double(A, E);
-      if (D.has_omega) acc = fma(-D.omega2, x, acc);
-      if (D.ext.kind != EXT_NONE) acc = ext_force_at(D.ext, S.amp, x) + acc;
-      const double vn = fma(dt, acc, v);
-      const double xn = fma(dt_drift, vn, x);
-      S.x[s] = xn;
-      S.v[s] = vn;
-      const unsigned long long av =
-          (unsigned long long)__double_as_longlong(vn) & 0x7FFFFFFFFFFFFFFFull;
-      maxv = av > maxv ? av : maxv;
-      if (last && !L.profile) {
-        D.x_out[id] = xn;
-        D.v_out[id] = vn;
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (!live[u]) {
+          kd[u] = 0;
+          continue;
+        }
+        const int sidx = sl[u];
+        const uint32_t r = rank0 + (uint32_t)(i0 + u);
+        const uint64_t key = S.key[sidx];
+        if (r != 0 && (r % (uint32_t)D.target) == 0) {
+          qnk[r / (uint32_t)D.target] = key;
+          qni[r / (uint32_t)D.target] = idv[u];
+        }
+        const double x = S.x[sidx], v = S.v[sidx];
+        const u128 M = mass_to_fixed(S.m[sidx], E);
+        const i128 A = T - 2 * (i128)C - (i128)M;
+        C += M;
+        double acc = fixed_to_double(A, E);
+        if (D.has_omega) acc = fma(-D.omega2, x, acc);
+        if (D.ext.kind != EXT_NONE) acc = ext_force_at(D.ext, S.amp, x) + acc;
+        const double vn = fma(dt, acc, v);
+        const double xn = fma(dt_drift, vn, x);
+        S.x[sidx] = xn;
+        S.v[sidx] = vn;
+        const unsigned long long av =
+            (unsigned long long)__double_as_longlong(vn) & 0x7FFFFFFFFFFFFFFFull;
+        maxv = av > maxv ? av : maxv;
+        if (last && !L.profile) {
+          D.x_out[idv[u]] = xn;
+          D.v_out[idv[u]] = vn;
+        }
+        kd[u] = key_of(dest_dt != 0.0 ? fma(dest_dt, vn, xn) : xn);
       }
-      const double xd = dest_dt != 0.0 ? fma(dest_dt, vn, xn) : xn;
-      const int d = dest_bucket(S, qdk, qdi, D.nb, key_of(xd), id);
-      sdst[s] = d;
-      srank[s] = (d >= S.win_lo && d < S.win_hi)
-                     ? (uint16_t)atomicAdd(&S.dcount[d - S.win_lo], 1u)
-                     : (uint16_t)0xffffu;
+      // routing: binary lifting over the window, both sheets in lock-step
+      int l[2] = {0, 0};
+      bool inw[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+        inw[u] = live[u] && win_ge(S, 0, kd[u], idv[u]) && !win_ge(S, wlen, kd[u], idv[u]);
+      for (int step = top; step >= 1; step >>= 1) {
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          if (l[u] + step < wlen && win_ge(S, l[u] + step, kd[u], idv[u])) l[u] += step;
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (!live[u]) continue;
+        const int d = inw[u] ? S.win_lo + l[u] : dest_bucket(S, qdk, qdi, D.nb, kd[u], idv[u]);
+        sdst[sl[u]] = d;
+        srank[sl[u]] = (d >= S.win_lo && d < S.win_hi)
+                           ? (uint16_t)atomicAdd(&S.dcount[d - S.win_lo], 1u)
+                           : (uint16_t)0xffffu;
+      }
     }
     __syncthreads();
     for (int j = tid; j < S.win_hi - S.win_lo; j += BT) {
@@ -605,6 +651,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     double* mout = D.bm[1 - lay];
     int32_t* iout = D.bi[1 - lay];
     bool overflow = false;
+#pragma unroll 4
     for (int j = tid; j < n; j += BT) {
       const int d = sdst[j];
       const uint16_t rk = srank[j];
@@ -728,13 +775,35 @@ __global__ void k_count_offsets(const unsigned* cnt, int64_t nb, unsigned* offs)
 
 int bucket_step_grid(int sm_count) { return 2 * sm_count; }
 
-void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s) {
+namespace {
+std::mutex g_tune_mu;
+std::vector<std::pair<int64_t, BucketTuning>> g_tune;  // rows sorted by n_min
+}  // namespace
+
+BucketTuning tuning_for(int64_t n) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  BucketTuning t;
+  for (const auto& row : g_tune)
+    if (row.first <= n) t = row.second;
+  return t;
+}
+
+void set_tuning(const std::vector<std::pair<int64_t, BucketTuning>>& rows) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune = rows;
+}
+
+void bucket_step_prepare() {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_bucket_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sizeof(StepSmem));
     attr = true;
   }
+}
+
+void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s) {
+  bucket_step_prepare();
   if (grid > a.ntasks) grid = a.ntasks;
   if (grid < 1) grid = 1;
   k_bucket_step<<<grid, BT, sizeof(StepSmem), s>>>(a);

@@ -14,8 +14,23 @@ namespace wg {
 
 constexpr int kBucketThreads = 256;
 constexpr int kBucketCap = 2048;      // sheets a bucket can hold
-constexpr int kBucketTarget = 1024;   // sheets per bucket right after a re-sort
-constexpr int kSplitterWindow = 64;   // buckets searched in shared memory on each side
+constexpr int kSplitterWindow = 64;   // largest splitter window (buckets on each side)
+constexpr int kSortBitsMax = 12;      // largest counting-sort offset (bits)
+
+// Tunables of the fused sub-step, chosen per simulation size by the
+// autotuner (wendy_gb300/autotune.py) or left at their defaults.
+struct BucketTuning {
+  int target = 1024;      // sheets per bucket right after a re-sort (<= kBucketCap / 2)
+  int window = 64;        // splitters searched in shared memory on each side
+  int sort_bits = 12;     // counting-sort bins = 2^sort_bits (8..12)
+  int ctas_per_sm = 2;    // persistent CTAs per SM (1 or 2)
+};
+BucketTuning tuning_for(int64_t n);
+}  // namespace wg
+#include <utility>
+#include <vector>
+namespace wg {
+void set_tuning(const std::vector<std::pair<int64_t, BucketTuning>>& rows);
 
 // Decoupled look-back record of one bucket (48 bytes).
 struct __align__(16) BucketRec {
@@ -49,6 +64,10 @@ struct SimDev {
   const double* t_seq;   // [nleap] times of this call's force evaluations
   int64_t n;
   int64_t nb;
+  int target;            // sheets per bucket at a re-sort (splitters at ranks j * target)
+  int window;            // splitter window half-width (<= kSplitterWindow)
+  int sort_bits;         // counting-sort offset bits (8..12)
+  int pad0;
   uint64_t T_lo, T_hi;   // totmass in fixed point
   int E;
   int has_omega;
@@ -78,6 +97,8 @@ struct StepLaunch {
 };
 
 void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s);
+// One-time kernel attribute set-up; call before any stream capture.
+void bucket_step_prepare();
 int bucket_step_grid(int sm_count);
 void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, double* x,
                       double* v, double* m, int32_t* idx, unsigned* cnt, uint64_t* qk,

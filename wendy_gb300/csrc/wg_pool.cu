@@ -92,10 +92,12 @@ struct PoolSim {
   double pending_dt = 0;
   bool fresh = false;      // just bucketized: the opening half drift is already applied
   bool out_valid = false;  // x_out / v_out hold the last output
+  BucketTuning tune;
 };
 
 size_t sim_bytes(int64_t n) {
-  const int64_t nb = (n + kBucketTarget - 1) / kBucketTarget;
+  const BucketTuning t = tuning_for(n);
+  const int64_t nb = (n + t.target - 1) / t.target;
   const size_t slots = (size_t)nb * kBucketCap;
   return 2 * (3 * al(slots * 8) + al(slots * 4)) + 2 * al(4 * (size_t)nb) +
          2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
@@ -189,6 +191,13 @@ struct wg_pool {
   BucketTask* h_tasks = nullptr;
   unsigned epoch = 1;
   int64_t launches = 0;
+  // the per-call device sequence (copies in, nleap sub-step launches, copy
+  // back) captured once per (simulations, buckets, nleap) and replayed
+  cudaGraphExec_t gexec = nullptr;
+  int g_count = -1, g_nleap = -1;
+  int64_t g_ntasks = -1;
+  void* g_small = nullptr;
+  int64_t graph_builds = 0;
 };
 
 namespace {
@@ -253,7 +262,7 @@ int ensure_workspace(wg_pool* p, int64_t n) {
   p->ws = nullptr;
   const size_t nd = al((size_t)n * 8), ni = al((size_t)n * 4);
   const int64_t tiles = (n + kForceTile - 1) / kForceTile;
-  const int64_t nb = (n + kBucketTarget - 1) / kBucketTarget;
+  const int64_t nb = n;  // compaction offsets: at most one bucket per sheet
   const size_t b = 2 * (3 * nd + ni) + al(sizeof(TileRec) * (size_t)tiles) + radix_bytes(n) +
                    al(4 * (size_t)nb);
   PC(cudaMalloc(&p->ws, b));
@@ -288,7 +297,7 @@ int to_buckets(wg_pool* p, PoolSim* s, double dt) {
   k_set_table<<<1, 1, 0, p->stream>>>(p->table, own, p->set[1]);
   launch_drift(p->table, s->n, dt / 2., &p->wflags[0], p->stream);  // also marks "unsorted"
   radix_sort_state(p->table, s->n, &p->radix, &p->wflags[0], p->err, p->stream);
-  launch_bucketize(p->table, s->n, kBucketTarget, s->nb, s->bx[0], s->bv[0], s->bm[0],
+  launch_bucketize(p->table, s->n, s->tune.target, s->nb, s->bx[0], s->bv[0], s->bm[0],
                    s->bi[0], s->bcnt[0], s->qk[0], s->qi[0], s->bcnt[1], p->stream);
   p->launches += 3 + kRadixLaunches;
   s->lay = 0;
@@ -342,6 +351,7 @@ int wg_pool_create(int64_t budget_bytes, wg_pool** out) {
     delete p;
     return rc;
   }
+  bucket_step_prepare();
   *out = p;
   return WG_OK;
 }
@@ -378,7 +388,8 @@ int wg_pool_add(wg_pool* p, int64_t n, const double* x, const double* v, const d
                      (long long)n, bytes, (long long)p->used, (long long)p->budget);
   PoolSim* s = new PoolSim();
   s->n = n;
-  s->nb = (n + kBucketTarget - 1) / kBucketTarget;
+  s->tune = tuning_for(n);
+  s->nb = (n + s->tune.target - 1) / s->tune.target;
   s->bytes = bytes;
   cudaError_t e = cudaMallocAsync(&s->mem, bytes, p->stream);
   if (e != cudaSuccess) {
@@ -473,12 +484,7 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
   for (int i = 0; i < nleap; ++i) p->h_ep[i] = p->epoch + (unsigned)i;
   p->epoch += (unsigned)nleap;
   PC(cudaEventRecord(p->ev0, p->stream));
-  PC(cudaMemcpyAsync(p->t_seq, p->h_t, 8 * (size_t)count * L1, cudaMemcpyHostToDevice,
-                     p->stream));
-  PC(cudaMemcpyAsync(p->epochs, p->h_ep, 4 * (size_t)nleap, cudaMemcpyHostToDevice, p->stream));
-  PC(cudaMemsetAsync(p->tickets, 0, 4 * (size_t)nleap, p->stream));
   PC(cudaMemsetAsync(p->ocount, 0, 8 * (size_t)count, p->stream));
-  PC(cudaMemsetAsync(p->flags, 0, sizeof(StepFlags) * (size_t)count * (L1 + 1), p->stream));
   // simulations that are compact, or routed for another dt, re-sort first
   for (int k = 0; k < count; ++k) {
     PoolSim* s = act[(size_t)k];
@@ -522,6 +528,9 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
     d.t_seq = p->t_seq + (size_t)k * L1;
     d.n = s->n;
     d.nb = s->nb;
+    d.target = s->tune.target;
+    d.window = s->tune.window;
+    d.sort_bits = s->tune.sort_bits;
     d.T_lo = s->T_lo;
     d.T_hi = s->T_hi;
     d.E = s->E;
@@ -534,27 +543,61 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
     d.qsel0 = s->qsel;
     for (int64_t b = 0; b < s->nb; ++b) p->h_tasks[t++] = BucketTask{k, (int)b};
   }
-  PC(cudaMemcpyAsync(p->d_dev, p->h_dev, sizeof(SimDev) * (size_t)count, cudaMemcpyHostToDevice,
-                     p->stream));
-  PC(cudaMemcpyAsync(p->tasks, p->h_tasks, sizeof(BucketTask) * (size_t)ntasks,
-                     cudaMemcpyHostToDevice, p->stream));
-  const int grid = bucket_step_grid(p->sms);
-  for (int i = 0; i < nleap; ++i) {
-    StepLaunch L;
-    L.sims = p->d_dev;
-    L.tasks = p->tasks;
-    L.ntasks = (int)ntasks;
-    L.sub = i;
-    L.nleap = nleap;
-    L.epochs = p->epochs;
-    L.ticket = p->tickets + i;
-    L.err = p->err;
-    L.profile = 0;
-    launch_bucket_step(L, grid, p->stream);
+  // device sequence of the call, captured in a CUDA graph and replayed while
+  // the number of simulations, buckets and sub-steps stays the same
+  const bool rebuild = !p->gexec || p->g_count != count || p->g_nleap != nleap ||
+                       p->g_ntasks != ntasks || p->g_small != p->small;
+  if (rebuild) {
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    p->gexec = nullptr;
+    cudaGraph_t g = nullptr;
+    PC(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    cudaMemcpyAsync(p->t_seq, p->h_t, 8 * (size_t)count * L1, cudaMemcpyHostToDevice,
+                    p->stream);
+    cudaMemcpyAsync(p->epochs, p->h_ep, 4 * (size_t)nleap, cudaMemcpyHostToDevice, p->stream);
+    cudaMemsetAsync(p->tickets, 0, 4 * (size_t)nleap, p->stream);
+    cudaMemsetAsync(p->flags, 0, sizeof(StepFlags) * (size_t)count * (L1 + 1), p->stream);
+    cudaMemcpyAsync(p->d_dev, p->h_dev, sizeof(SimDev) * (size_t)count, cudaMemcpyHostToDevice,
+                    p->stream);
+    cudaMemcpyAsync(p->tasks, p->h_tasks, sizeof(BucketTask) * (size_t)ntasks,
+                    cudaMemcpyHostToDevice, p->stream);
+    int cps = 1;
+    int64_t nmax = 0;
+    for (PoolSim* a : act)
+      if (a->n > nmax) {
+        nmax = a->n;
+        cps = a->tune.ctas_per_sm;
+      }
+    const int grid = cps * p->sms;
+    for (int i = 0; i < nleap; ++i) {
+      StepLaunch L;
+      L.sims = p->d_dev;
+      L.tasks = p->tasks;
+      L.ntasks = (int)ntasks;
+      L.sub = i;
+      L.nleap = nleap;
+      L.epochs = p->epochs;
+      L.ticket = p->tickets + i;
+      L.err = p->err;
+      L.profile = 0;
+      launch_bucket_step(L, grid, p->stream);
+    }
+    cudaMemcpyAsync(p->h_oc, p->ocount, 8 * (size_t)count, cudaMemcpyDeviceToHost, p->stream);
+    PC(cudaStreamEndCapture(p->stream, &g));
+    const cudaError_t ie = cudaGraphInstantiate(&p->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      p->gexec = nullptr;
+      return pool_fail(WG_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ie));
+    }
+    p->g_count = count;
+    p->g_nleap = nleap;
+    p->g_ntasks = ntasks;
+    p->g_small = p->small;
+    p->graph_builds++;
   }
+  PC(cudaGraphLaunch(p->gexec, p->stream));
   p->launches += nleap;
-  PC(cudaGetLastError());
-  PC(cudaMemcpyAsync(p->h_oc, p->ocount, 8 * (size_t)count, cudaMemcpyDeviceToHost, p->stream));
   PC(cudaStreamSynchronize(p->stream));
   // bookkeeping, and recovery of simulations that overflowed a bucket
   for (int k = 0; k < count; ++k) {
@@ -655,6 +698,7 @@ int wg_pool_destroy(wg_pool* p) {
     }
   cudaStreamSynchronize(p->stream);
   if (p->ws) cudaFree(p->ws);
+  if (p->gexec) cudaGraphExecDestroy(p->gexec);
   free_small(p);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);

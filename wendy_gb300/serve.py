@@ -24,8 +24,24 @@ from dataclasses import dataclass, field
 
 import numpy
 
+from . import _lib
 from .ensemble import Pool
 from .wendy import Simulation
+
+
+class _Pinned:
+    """Output buffers of one request, page-locked for the stream of downloads."""
+
+    def __init__(self, n):
+        self.x = numpy.empty(n)
+        self.v = numpy.empty(n)
+        self._L = _lib.lib()
+        for a in (self.x, self.v):
+            _lib.check(self._L.wg_host_register(a.ctypes.data, a.nbytes), "wg_host_register")
+
+    def release(self):
+        for a in (self.x, self.v):
+            self._L.wg_host_unregister(a.ctypes.data)
 
 
 @dataclass
@@ -84,7 +100,7 @@ class Server:
                 sid = self.pool.add(r.x, r.v, r.m, omega=r.omega, ext_force=r.ext_force,
                                     twopiG=1.)
                 r.admitted_at = now
-                active[sid] = [r, r.noutputs, r.t0]
+                active[sid] = [r, r.noutputs, r.t0, _Pinned(r.n)]
                 used += need
                 i += 1
             if not active:
@@ -95,7 +111,7 @@ class Server:
                 continue
             # one round: every resident simulation advances one output interval
             by_nleap = {}
-            for sid, (r, left, t) in active.items():
+            for sid, (r, left, t, buf) in active.items():
                 by_nleap.setdefault(r.nleap, []).append(sid)
             for nleap, ids in by_nleap.items():
                 dts = numpy.array([active[s][0].dt / nleap for s in ids])
@@ -106,17 +122,18 @@ class Server:
             self.rounds += 1
             now = clock() - start
             for sid in list(active):
-                r, left, t = active[sid]
-                x, v = self.pool.download(sid)
+                r, left, t, buf = active[sid]
+                x, v = self.pool.download(sid, buf.x, buf.v)
                 if r.keep_outputs:
-                    r.outputs.append((x, v))
+                    r.outputs.append((x.copy(), v.copy()))
                 if self.on_output:
                     self.on_output(r, x, v)
                 left -= 1
                 active[sid][1] = left
                 if left == 0:
-                    r.last_x, r.last_v = x, v
+                    r.last_x, r.last_v = x.copy(), v.copy()
                     r.done_at = clock() - start
+                    buf.release()
                     self.pool.remove(sid)
                     used -= Pool.sim_bytes(r.n)
                     del active[sid]
@@ -138,7 +155,8 @@ def serve_one_at_a_time(requests, clock=time.perf_counter):
         omega2 = -1. if r.omega is None else r.omega ** 2.
         sim = Simulation(r.x, r.v, r.m, float(numpy.sum(r.m)), omega2, r.ext_force)
         t = ctypes.c_double(r.t0)
-        x, v = numpy.empty(r.n), numpy.empty(r.n)
+        buf = _Pinned(r.n)
+        x, v = buf.x, buf.v
         for _ in range(r.noutputs):
             sim.step(r.dt / r.nleap, r.nleap, t)
             sim.download(x, v)
@@ -146,6 +164,7 @@ def serve_one_at_a_time(requests, clock=time.perf_counter):
                 r.outputs.append((x.copy(), v.copy()))
         r.last_x, r.last_v = x.copy(), v.copy()
         r.done_at = clock() - start
+        buf.release()
         sim.close()
     return requests
 
