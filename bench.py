@@ -54,6 +54,19 @@ WORKLOADS = {
 }
 
 
+def replica_reduce(elapsed, units):
+    """Max of the elapsed times and sum of the units over the ranks of the
+    default process group (replicas: every rank runs its own simulation; this
+    is the only cross-rank exchange, for reporting)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(elapsed)], dtype=torch.float64)
+    u = torch.tensor([float(units)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 def ensemble_members(count, nmin, nmax, seed=0):
     """(n, family, seed, dt, omega) of `count` simulations drawn from `seed`:
     N log-uniform in [nmin, nmax], initial conditions cycling over the sech^2
@@ -374,12 +387,10 @@ def main():
         for _ in range(args.steps):
             elapsed += sim.step(dt_leap, nleap, t0)
     st1 = sim.stats()
+    units = n * nleap * args.steps
     if world > 1:
-        import torch
-        t = torch.tensor([elapsed], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-    value = world * n * nleap * args.steps / elapsed
+        elapsed, units = replica_reduce(elapsed, units)
+    value = units / elapsed
     launches = st1["launches"] - st0["launches"]
 
     # The timed region launches k_bucket_step once per sub-step and nothing

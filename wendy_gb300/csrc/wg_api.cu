@@ -142,6 +142,8 @@ struct wg_sim {
   bool out_valid = false;  // x_out / v_out hold the last call's output
   int grid_bucket = 0;
   BucketTuning tune;             // bucket size, window, sort bits, CTAs per SM
+  SheetRec* call_xi = nullptr;    // extra outputs of the reference-shaped entry (this call)
+  double* call_a = nullptr;
   SimDev dev{};                  // host copy of the kernel's view of this simulation
   SimDev* d_dev = nullptr;       // device copy (one entry)
   BucketTask* d_tasks = nullptr; // [nb]: (0, b)
@@ -478,6 +480,8 @@ void fill_dev(wg_sim* s, double dt, double pre) {
   d.ocount = s->ocount;
   d.x_out = s->x_out;
   d.v_out = s->v_out;
+  d.xi_out = s->call_xi;
+  d.a_out = s->call_a;
   d.flags = s->flags;
   d.t_seq = s->t_seq;
   d.n = s->n;
@@ -546,6 +550,10 @@ __global__ void k_store_sheets(const StateTable* table, int64_t n, wg_sheet* xi)
     r.val = st.x[i];
     xi[i] = r;
   }
+}
+
+void store_sheets(const StateTable* table, int64_t n, wg_sheet* xi, cudaStream_t st) {
+  k_store_sheets<<<152 * 8, 256, 0, st>>>(table, n, xi);
 }
 
 }  // namespace
@@ -627,15 +635,8 @@ int wg_create(int64_t n, const double* x, const double* v, const double* m, doub
   return WG_OK;
 }
 
-int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
-  if (!s) {
-    set_error("null simulation");
-    return WG_ERR_ARG;
-  }
-  if (nleap < 1 || !std::isfinite(dt)) {
-    set_error("nleap must be >= 1 and dt finite");
-    return WG_ERR_ARG;
-  }
+static int run_call(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed,
+                    bool record_start) {
   int rc = alloc_call_arrays(s, nleap);
   if (rc) return rc;
   fill_times(s, dt, nleap, t0);
@@ -648,7 +649,7 @@ int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
     for (int i = 0; i < nleap; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
     s->epoch += (unsigned)nleap;
   }
-  WG_CUDA(cudaEventRecord(s->ev0, s->stream));
+  if (record_start) WG_CUDA(cudaEventRecord(s->ev0, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->t_seq, s->h_t, 8 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->epochs, s->h_ep, 4 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemsetAsync(s->flags, 0, sizeof(StepFlags) * (nleap + 1), s->stream));
@@ -722,9 +723,13 @@ int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
         f.dt_drift = (i == nleap - 1) ? dt / 2. : dt;
         f.ticket = s->tickets + i;
         f.flag_out = &s->flags[i + 1];
+        f.a_out = (i == nleap - 1 && s->call_a) ? s->a_sorted : nullptr;
         launch_force(f, s->n_tiles, s->stream);
         WG_CUDA(cudaStreamSynchronize(s->stream));  // pageable `one` stays valid
       }
+      if (s->call_a) launch_scatter_accel(s->table, s->n, s->a_sorted, s->call_a, s->stream);
+      if (s->call_xi) store_sheets(s->table, s->n, reinterpret_cast<wg_sheet*>(s->call_xi),
+                                   s->stream);
       s->st.launches += (int64_t)(nleap - k - 1) * (1 + kRadixLaunches);
       s->out_valid = false;
     }
@@ -743,6 +748,20 @@ int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
   }();
   s->st.last_max_disp = vmax * std::fabs(dt / 2.);
   return rc;
+}
+
+int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
+  if (!s) {
+    set_error("null simulation");
+    return WG_ERR_ARG;
+  }
+  if (nleap < 1 || !std::isfinite(dt)) {
+    set_error("nleap must be >= 1 and dt finite");
+    return WG_ERR_ARG;
+  }
+  s->call_xi = nullptr;
+  s->call_a = nullptr;
+  return run_call(s, dt, nleap, t0, time_elapsed, true);
 }
 
 int wg_download(wg_sim* s, double* x, double* v) {
@@ -1019,21 +1038,27 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   WG_CUDA(cudaMemcpyAsync(d_v, v, 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemcpyAsync(d_m, m, 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
   k_load_sheets<<<152 * 8, 256, 0, s->stream>>>(s->table, n, d_xi, d_v, d_m);
-  fill_times(s, dt, nleap, t0);
-  rc = enqueue_step(s, dt, nleap, true, dt / 2.);
-  if (rc) return rc;
-  k_store_sheets<<<152 * 8, 256, 0, s->stream>>>(s->table, n, d_xi);
-  launch_desort(s->table, n, s->x_out, s->v_out, s->stream);
-  launch_scatter_accel(s->table, n, s->a_sorted, s->stage_a, s->stream);
+  // the sheets are compact with the opening half drift pending: run the call
+  // on the bucket path, which also leaves xi (last sort order) and a
+  s->mode = 0;
+  s->call_xi = reinterpret_cast<SheetRec*>(d_xi);
+  s->call_a = s->stage_a;
+  rc = run_call(s, dt, nleap, t0, time_elapsed, false);
+  s->call_xi = nullptr;
+  s->call_a = nullptr;
+  if (rc) {
+    if (err) *err = rc;
+    return rc;
+  }
   WG_CUDA(cudaMemcpyAsync(xi, d_xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  if (!s->out_valid) {
+    launch_desort(s->table, n, s->x_out, s->v_out, s->stream);
+    s->out_valid = true;
+  }
   WG_CUDA(cudaMemcpyAsync(x, s->x_out, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
   WG_CUDA(cudaMemcpyAsync(v, s->v_out, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
   WG_CUDA(cudaMemcpyAsync(a, s->stage_a, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
-  WG_CUDA(cudaEventRecord(s->ev1, s->stream));
-  rc = finish_call(s, nleap);
-  float ms = 0;
-  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
-  if (time_elapsed) *time_elapsed = ms * 1e-3;
+  WG_CUDA(cudaStreamSynchronize(s->stream));
   if (rc && err) *err = rc;
   return rc;
 }

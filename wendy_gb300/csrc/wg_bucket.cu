@@ -121,7 +121,7 @@ __device__ __forceinline__ uint32_t block_excl_scan(StepSmem& S, uint32_t v, uin
 
 // Multi-pass fallback: stable LSD radix sort of 32-bit order-preserving
 // offsets, 8 bits per pass over the bits that differ, then exact tie order.
-__device__ void lsd_sort(StepSmem& S, int n, uint64_t kmin, uint64_t kmax) {
+__device__ __forceinline__ void lsd_sort(StepSmem& S, int n, uint64_t kmin, uint64_t kmax) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t span = kmax - kmin;
   const int bits = span ? 64 - __clzll((long long)span) : 0;
@@ -206,8 +206,8 @@ __device__ void lsd_sort(StepSmem& S, int n, uint64_t kmin, uint64_t kmax) {
 }
 
 // Sort the n <= CAP sheets of the bucket by (key, idx) into S.perm.
-__device__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin, uint64_t kmax,
-                            int qb) {
+__device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin,
+                                            uint64_t kmax, int qb) {
   const int tid = threadIdx.x;
   const uint64_t span = kmax - kmin;
   const int bits = span ? 64 - __clzll((long long)span) : 0;
@@ -283,7 +283,7 @@ __device__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin, uint64_t
 
 // Look-back over earlier buckets of the same simulation for the exclusive
 // (mass, count) prefix; all lanes of warp 0 call it.  Bounded waits.
-__device__ void bucket_lookback(BucketRec* recs, int64_t b, u128 mass, uint32_t cnt,
+__device__ __forceinline__ void bucket_lookback(BucketRec* recs, int64_t b, u128 mass, uint32_t cnt,
                                 unsigned ep, int lane, unsigned* err, u128& pmass,
                                 uint32_t& pcnt) {
   BucketRec* me = recs + b;
@@ -561,6 +561,17 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       qnk[D.nb] = ~0ull;
       qni[D.nb] = 0x7fffffff;
     }
+    // descriptor fields used per sheet, held in registers (the descriptor is
+    // in global memory and the compiler cannot prove the stores below leave it alone)
+    const int has_omega = D.has_omega;
+    const double omega2 = D.omega2;
+    const ExtForce ext = D.ext;
+    const uint32_t target = (uint32_t)D.target;
+    const int64_t nbk = D.nb;
+    double* const x_out = D.x_out;
+    double* const v_out = D.v_out;
+    SheetRec* const xi_out = D.xi_out;
+    double* const a_out = D.a_out;
     // ---- force, kick, drift, routing; new x, v go back to their slots and
     // the destination of every slot to the (now free) sort area
     int32_t* sdst = reinterpret_cast<int32_t*>(S.u.bins);          // [CAP]
@@ -595,17 +606,17 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
         const int sidx = sl[u];
         const uint32_t r = rank0 + (uint32_t)(i0 + u);
         const uint64_t key = S.key[sidx];
-        if (r != 0 && (r % (uint32_t)D.target) == 0) {
-          qnk[r / (uint32_t)D.target] = key;
-          qni[r / (uint32_t)D.target] = idv[u];
+        if (r != 0 && (r % target) == 0) {
+          qnk[r / target] = key;
+          qni[r / target] = idv[u];
         }
         const double x = S.x[sidx], v = S.v[sidx];
         const u128 M = mass_to_fixed(S.m[sidx], E);
         const i128 A = T - 2 * (i128)C - (i128)M;
         C += M;
         double acc = fixed_to_double(A, E);
-        if (D.has_omega) acc = fma(-D.omega2, x, acc);
-        if (D.ext.kind != EXT_NONE) acc = ext_force_at(D.ext, S.amp, x) + acc;
+        if (has_omega) acc = fma(-omega2, x, acc);
+        if (ext.kind != EXT_NONE) acc = ext_force_at(ext, S.amp, x) + acc;
         const double vn = fma(dt, acc, v);
         const double xn = fma(dt_drift, vn, x);
         S.x[sidx] = xn;
@@ -614,8 +625,16 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
             (unsigned long long)__double_as_longlong(vn) & 0x7FFFFFFFFFFFFFFFull;
         maxv = av > maxv ? av : maxv;
         if (last && !L.profile) {
-          D.x_out[idv[u]] = xn;
-          D.v_out[idv[u]] = vn;
+          x_out[idv[u]] = xn;
+          v_out[idv[u]] = vn;
+          if (xi_out) {
+            SheetRec rec;
+            rec.idx = idv[u];
+            rec.pad = 0;
+            rec.val = xn;
+            xi_out[r] = rec;
+          }
+          if (a_out) a_out[idv[u]] = acc;
         }
         kd[u] = key_of(dest_dt != 0.0 ? fma(dest_dt, vn, xn) : xn);
       }
@@ -633,7 +652,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
         if (!live[u]) continue;
-        const int d = inw[u] ? S.win_lo + l[u] : dest_bucket(S, qdk, qdi, D.nb, kd[u], idv[u]);
+        const int d = inw[u] ? S.win_lo + l[u] : dest_bucket(S, qdk, qdi, nbk, kd[u], idv[u]);
         sdst[sl[u]] = d;
         srank[sl[u]] = (d >= S.win_lo && d < S.win_hi)
                            ? (uint16_t)atomicAdd(&S.dcount[d - S.win_lo], 1u)

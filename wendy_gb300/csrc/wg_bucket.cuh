@@ -41,6 +41,13 @@ struct __align__(16) BucketRec {
   unsigned pad;
 };
 
+// Same layout as wendy's struct array_w_index (int idx; double val).
+struct SheetRec {
+  int32_t idx;
+  int32_t pad;
+  double val;
+};
+
 // One simulation as the sub-step kernel sees it.  Arrays are the
 // simulation's own; layouts, counts and splitters come in pairs used
 // alternately from sub-step to sub-step, starting at lay0 / qsel0.
@@ -60,6 +67,8 @@ struct SimDev {
   unsigned* ocount;      // [0] sheets in the overflow list, [1] 1 + sub-step that overflowed
   double* x_out;         // output of the call's last sub-step, original order
   double* v_out;
+  SheetRec* xi_out;      // optional: (idx, x) in the last sub-step's sorted order
+  double* a_out;         // optional: accelerations of the last force evaluation, original order
   StepFlags* flags;      // [nleap + 1] of this call
   const double* t_seq;   // [nleap] times of this call's force evaluations
   int64_t n;

@@ -524,6 +524,8 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
     d.ocount = p->ocount + 2 * k;
     d.x_out = s->x_out;
     d.v_out = s->v_out;
+    d.xi_out = nullptr;
+    d.a_out = nullptr;
     d.flags = p->flags + (size_t)k * (L1 + 1);
     d.t_seq = p->t_seq + (size_t)k * L1;
     d.n = s->n;
