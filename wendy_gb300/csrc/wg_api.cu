@@ -126,7 +126,8 @@ struct wg_sim {
   double* bv[2] = {nullptr, nullptr};
   double* bm[2] = {nullptr, nullptr};
   int32_t* bi[2] = {nullptr, nullptr};
-  unsigned* bcnt[2] = {nullptr, nullptr};
+  unsigned* bcnt[kAggSlots] = {nullptr, nullptr, nullptr};
+  unsigned long long* bmass[kAggSlots] = {nullptr, nullptr, nullptr};
   uint64_t* qk[2] = {nullptr, nullptr};
   int32_t* qi[2] = {nullptr, nullptr};
   BucketRec* brecs = nullptr;
@@ -138,6 +139,7 @@ struct wg_sim {
   int mode = 0;          // 0: compact sorted sets (half drift pending), 1: buckets
   int lay = 0;           // layout holding the sheets in bucket mode
   int qsel = 0;          // splitter array defining the next layout
+  int cslot = 0;         // aggregate slot describing layout `lay`
   double pending_dt = 0; // dt of the half drift the bucket layout was routed for
   bool out_valid = false;  // x_out / v_out hold the last call's output
   int grid_bucket = 0;
@@ -286,7 +288,8 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
   s->nb = (n + s->tune.target - 1) / s->tune.target;
   const int64_t nb = s->nb;
   const size_t slots = (size_t)nb * kBucketCap;
-  const size_t bk_b = 2 * (3 * al(slots * 8) + al(slots * 4)) + 2 * al(4 * (size_t)nb) +
+  const size_t bk_b = 2 * (3 * al(slots * 8) + al(slots * 4)) +
+                      kAggSlots * (al(4 * (size_t)nb) + al(32 * (size_t)nb)) +
                       2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
                       al(sizeof(BucketRec) * (size_t)nb) + 3 * nd + ni + al(64) +
                       al(4 * (size_t)nb) + al(sizeof(SimDev)) + al(sizeof(BucketTask) * (size_t)nb);
@@ -304,8 +307,9 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
     s->bm[k] = reinterpret_cast<double*>(p); p += al(slots * 8);
     s->bi[k] = reinterpret_cast<int32_t*>(p); p += al(slots * 4);
   }
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < kAggSlots; ++k) {
     s->bcnt[k] = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)nb);
+    s->bmass[k] = reinterpret_cast<unsigned long long*>(p); p += al(32 * (size_t)nb);
   }
   for (int k = 0; k < 2; ++k) {
     s->qk[k] = reinterpret_cast<uint64_t*>(p); p += al(8 * (size_t)(nb + 1));
@@ -332,8 +336,10 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
     }
   }
   if (cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)nb, s->stream) != cudaSuccess ||
-      cudaMemsetAsync(s->bcnt[0], 0, 4 * (size_t)nb, s->stream) != cudaSuccess ||
-      cudaMemsetAsync(s->bcnt[1], 0, 4 * (size_t)nb, s->stream) != cudaSuccess) {
+      cudaMemsetAsync(s->bcnt[0], 0,
+                      static_cast<char*>(static_cast<void*>(s->bmass[kAggSlots - 1])) +
+                          al(32 * (size_t)nb) - static_cast<char*>(static_cast<void*>(s->bcnt[0])),
+                      s->stream) != cudaSuccess) {
     set_error("memset failed");
     return fail(WG_ERR_CUDA);
   }
@@ -452,10 +458,10 @@ int enqueue_step(wg_sim* s, double dt, int nleap, bool want_accel, double dt_las
   return WG_OK;
 }
 
-// Bucket layout `lay` (+ overflow list) -> compact, unsorted sheets in the
-// current sorted-state set.
-void bucket_to_compact(wg_sim* s, int lay) {
-  launch_compact(s->table, s->nb, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay], s->bcnt[lay],
+// Bucket layout `lay` with the counts of aggregate slot `cslot` (+ overflow
+// list) -> compact, unsorted sheets in the current sorted-state set.
+void bucket_to_compact(wg_sim* s, int lay, int cslot) {
+  launch_compact(s->table, s->nb, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay], s->bcnt[cslot],
                  s->offs, s->ox, s->ov, s->om, s->oi, s->ocount, s->n, s->stream);
   s->st.launches += 2;
 }
@@ -468,9 +474,12 @@ void fill_dev(wg_sim* s, double dt, double pre) {
     d.bv[k] = s->bv[k];
     d.bm[k] = s->bm[k];
     d.bi[k] = s->bi[k];
-    d.bcnt[k] = s->bcnt[k];
     d.qk[k] = s->qk[k];
     d.qi[k] = s->qi[k];
+  }
+  for (int k = 0; k < kAggSlots; ++k) {
+    d.bcnt[k] = s->bcnt[k];
+    d.bmass[k] = s->bmass[k];
   }
   d.recs = s->brecs;
   d.ox = s->ox;
@@ -499,6 +508,7 @@ void fill_dev(wg_sim* s, double dt, double pre) {
   d.pre_dt = pre;
   d.lay0 = s->lay;
   d.qsel0 = s->qsel;
+  d.cs0 = s->cslot;
 }
 
 StepLaunch step_launch(wg_sim* s, int i, int nleap, int profile) {
@@ -657,7 +667,7 @@ static int run_call(wg_sim* s, double dt, int nleap, double* t0, double* time_el
   WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));  // overflow count and abort word
   if (s->mode == 1 && dt != s->pending_dt) {
     // routed for another dt: back to compact state, the half drift still pending
-    bucket_to_compact(s, s->lay);
+    bucket_to_compact(s, s->lay, s->cslot);
     s->mode = 0;
   }
   double pre = 0.0;
@@ -666,19 +676,21 @@ static int run_call(wg_sim* s, double dt, int nleap, double* t0, double* time_el
     radix_sort_state(s->table, s->n, &s->radix, &s->flags[0], s->err, s->stream);
     s->lay = 0;
     s->qsel = 0;
-    launch_bucketize(s->table, s->n, s->tune.target, s->nb, s->bx[0], s->bv[0], s->bm[0],
-                     s->bi[0], s->bcnt[0], s->qk[0], s->qi[0], s->bcnt[1], s->stream);
+    s->cslot = 0;
+    launch_bucketize(s->table, s->n, s->tune.target, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
+                     s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], s->stream);
     s->st.launches += 2 + kRadixLaunches;
     s->st.sorts_full += 1;
   } else {
     pre = dt / 2.;
   }
-  const int lay0 = s->lay;
+  const int lay0 = s->lay, cs0 = s->cslot;
   fill_dev(s, dt, pre);
   WG_CUDA(cudaMemcpyAsync(s->d_dev, &s->dev, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream));
   for (int i = 0; i < nleap; ++i) launch_bucket_step(step_launch(s, i, nleap, 0), s->grid_bucket, s->stream);
   s->lay = (lay0 + nleap) & 1;
   s->qsel = (s->qsel + nleap) & 1;
+  s->cslot = (cs0 + nleap) % kAggSlots;
   s->st.launches += nleap;
   WG_CUDA(cudaGetLastError());
   unsigned ab[2] = {0, 0};
@@ -694,7 +706,7 @@ static int run_call(wg_sim* s, double dt, int nleap, double* t0, double* time_el
     const int k = (int)ab[1] - 1;
     s->st.sorts_full += 1;
     const int lay_k = (k % 2 == 0) ? 1 - lay0 : lay0;
-    bucket_to_compact(s, lay_k);
+    bucket_to_compact(s, lay_k, (cs0 + k + 1) % kAggSlots);
     s->mode = 0;
     if (k < nleap - 1) {
       ForceArgs f;
@@ -836,7 +848,7 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   a.flag_out = &s->flags[s->cap];  // scratch slot
   WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));
   WG_CUDA(cudaStreamSynchronize(s->stream));
-  const int lay_start = s->lay;
+  const int lay_start = s->lay, cs_start = s->cslot;
   if (what == WG_PROF_BUCKET) {
     fill_dev(s, 0.0, 0.0);
     WG_CUDA(cudaMemcpyAsync(s->d_dev, &s->dev, sizeof(SimDev), cudaMemcpyHostToDevice,
@@ -869,9 +881,11 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
     WG_CUDA(cudaMemcpy(ab, s->ocount, 8, cudaMemcpyDeviceToHost));
     const int lay_end = ab[1] ? (((ab[1] - 1) % 2 == 0) ? 1 - lay_start : lay_start)
                               : ((lay_start + reps) & 1);
-    bucket_to_compact(s, lay_end);
+    const int cs_end = (cs_start + (ab[1] ? (int)ab[1] : reps)) % kAggSlots;
+    bucket_to_compact(s, lay_end, cs_end);
     s->lay = lay_end;
     s->qsel = (s->qsel + reps) & 1;
+    s->cslot = cs_end;
     s->mode = 0;
     WG_CUDA(cudaStreamSynchronize(s->stream));
   }

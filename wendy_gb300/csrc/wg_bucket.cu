@@ -6,11 +6,13 @@
 // launch per sub-step then does, per bucket (one CTA, persistent over a list
 // of (simulation, bucket) tasks):
 //
+//   claim the task one bucket ahead (warp 0, while the other warps write out
+//     the previous bucket): the bucket's sheet count and exact fixed-point
+//     mass were summed by the writers of the previous sub-step, so the
+//     look-back over the earlier buckets of the same simulation for the
+//     exclusive (mass, count) prefix never has to wait for a load
 //   load the bucket into shared memory (optionally applying the half drift
-//     a call starts with), summing its fixed-point mass and count
-//   decoupled look-back over the earlier buckets of the same simulation for
-//     the exclusive (mass, count) prefix -- before the sort, since the sums
-//     do not depend on the order inside the bucket
+//     a call starts with)
 //   sort the bucket by (key, index) in shared memory: the bounded-window
 //     fix-up, since a bucket only ever receives sheets from nearby buckets
 //     (one counting-sort pass on a 12-bit order-preserving offset, equal
@@ -20,7 +22,9 @@
 //     (totmass - 2 C - m [- omega^2 x]); kick; drift
 //   publish new splitters: the keys at global ranks j*T (quantiles)
 //   route every sheet to the bucket of the next layout that covers its new
-//     key (splitters computed by the previous sub-step) and append it there
+//     key (splitters computed by the previous sub-step), add the bucket's
+//     count and mass to that layout's aggregates and append the sheet there
+//     (the sheets of one warp bound for one bucket take consecutive slots)
 //
 // so a sub-step reads and writes each sheet once (28 B in, 28 B out).  A
 // bucket that would overflow its capacity sends the sheet to an overflow
@@ -60,36 +64,57 @@ struct LsdSmem {
   uint32_t hist[WARPS][256];
 };
 
+// What the processing of one task needs, prepared by warp 0 one task ahead
+// (while the other warps write out the current bucket), so that a bucket's
+// load waits only for its bulk copies and not for a chain of dependent global
+// reads, and its mass prefix is known before it starts.
+struct TaskMeta {
+  const double* x;
+  const double* v;
+  const double* m;
+  const int32_t* idx;
+  int64_t bucket;
+  unsigned task;  // ticket; ntasks or more ends the launch
+  int sim;
+  int n;          // sheets in the bucket; -1: the simulation has aborted this call
+  int lay;        // layout read by this sub-step
+  uint32_t pcnt;  // sheets in the simulation's earlier buckets
+  uint64_t pm_lo, pm_hi;  // their fixed-point mass
+};
+
 struct StepSmem {
   double x[CAP];
   double v[CAP];
   double m[CAP];
-  uint64_t key[CAP];
   int32_t idx[CAP];
   uint16_t perm[CAP];  // sorted position -> slot
   union {
     uint32_t bins[NBIN_PAD];
     LsdSmem lsd;
+    int32_t dst[CAP];  // destination bucket of each sorted position
   } u;
   uint64_t wkey[2 * RWIN + 2];
   int32_t widx[2 * RWIN + 2];
   uint32_t dcount[2 * RWIN + 2];
   uint32_t dbase[2 * RWIN + 2];
+  uint32_t dmass[2 * RWIN + 2][8];  // 16-bit mass limbs sent to each window bucket, summed
+  unsigned next_ticket;              // the next task's ticket and entry, read ahead
+  BucketTask next_tk;
   u128 warp_mass[WARPS];
   uint32_t warp_cnt[WARPS];
   uint32_t scan_tmp[WARPS];
   u128 prefix_mass;
   uint32_t prefix_cnt;
   uint64_t red_min[WARPS], red_max[WARPS];
-  unsigned task;
-  int sim;
-  int64_t bucket;
+  TaskMeta next;
   int win_lo, win_hi;
   double amp;
-  unsigned epoch;
   unsigned long long maxv;
   uint64_t mbar;  // completion of the bucket's bulk copies
 };
+
+// Two CTAs per SM: 228 KiB of shared memory per SM, 1 KiB reserved per CTA.
+static_assert(2 * (sizeof(StepSmem) + 1024) <= 228 * 1024, "StepSmem too large for 2 CTAs/SM");
 
 __device__ __forceinline__ bool pair_less(uint64_t k1, int32_t i1, uint64_t k2, int32_t i2) {
   return k1 < k2 || (k1 == k2 && i1 < i2);
@@ -130,7 +155,7 @@ __device__ __forceinline__ void lsd_sort(StepSmem& S, int n, uint64_t kmin, uint
   LsdSmem& L = S.u.lsd;
   __syncthreads();  // the union was just used as counting-sort bins
   for (int j = tid; j < n; j += BT) {
-    L.q[0][j] = (uint32_t)((S.key[j] - kmin) >> shift);
+    L.q[0][j] = (uint32_t)((key_of(S.x[j]) - kmin) >> shift);
     L.p[0][j] = (uint16_t)j;
   }
   int cur = 0;
@@ -192,10 +217,10 @@ __device__ __forceinline__ void lsd_sort(StepSmem& S, int n, uint64_t kmin, uint
     while (e + 1 < n && L.q[cur][e + 1] == qj) ++e;
     for (int a = j + 1; a <= e; ++a) {
       const uint16_t s = S.perm[a];
-      const uint64_t ks = S.key[s];
+      const uint64_t ks = key_of(S.x[s]);
       const int32_t is = S.idx[s];
       int b = a - 1;
-      while (b >= j && pair_less(ks, is, S.key[S.perm[b]], S.idx[S.perm[b]])) {
+      while (b >= j && pair_less(ks, is, key_of(S.x[S.perm[b]]), S.idx[S.perm[b]])) {
         S.perm[b + 1] = S.perm[b];
         --b;
       }
@@ -222,7 +247,7 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
   for (int i = 0; i < MAXI; ++i) {
     const int j = tid + i * BT;
     if (i < ipt && j < n) {
-      qv[i] = (uint16_t)((S.key[j] - kmin) >> shift);
+      qv[i] = (uint16_t)((key_of(S.x[j]) - kmin) >> shift);
       rk[i] = (uint16_t)atomicAdd(&bins[binp(qv[i])], 1u);
     }
   }
@@ -267,10 +292,10 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
       const uint32_t lo = bins[binp(qv[i])], hi = bins[binp(qv[i] + 1)];
       for (uint32_t a = lo + 1; a < hi; ++a) {
         const uint16_t s = S.perm[a];
-        const uint64_t ks = S.key[s];
+        const uint64_t ks = key_of(S.x[s]);
         const int32_t is = S.idx[s];
         int b = (int)a - 1;
-        while (b >= (int)lo && pair_less(ks, is, S.key[S.perm[b]], S.idx[S.perm[b]])) {
+        while (b >= (int)lo && pair_less(ks, is, key_of(S.x[S.perm[b]]), S.idx[S.perm[b]])) {
           S.perm[b + 1] = S.perm[b];
           --b;
         }
@@ -281,74 +306,19 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
   __syncthreads();
 }
 
-// Look-back over earlier buckets of the same simulation for the exclusive
-// (mass, count) prefix; all lanes of warp 0 call it.  Bounded waits.
-__device__ __forceinline__ void bucket_lookback(BucketRec* recs, int64_t b, u128 mass, uint32_t cnt,
-                                unsigned ep, int lane, unsigned* err, u128& pmass,
-                                uint32_t& pcnt) {
-  BucketRec* me = recs + b;
-  pmass = 0;
-  pcnt = 0;
-  if (b == 0) {
-    if (lane == 0) {
-      me->inc_lo = (uint64_t)mass;
-      me->inc_hi = (uint64_t)(mass >> 64);
-      me->inc_cnt = cnt;
-      st_release_u32(&me->flag, (ep << 2) | 2u);
-    }
-    return;
-  }
-  if (lane == 0) {
-    me->agg_lo = (uint64_t)mass;
-    me->agg_hi = (uint64_t)(mass >> 64);
-    me->agg_cnt = cnt;
-    st_release_u32(&me->flag, (ep << 2) | 1u);
-  }
-  int64_t j = b - 1;
-  for (;;) {
-    const int64_t jj = j - lane;
-    unsigned status = 0;
-    u128 vm = 0;
-    uint32_t vc = 0;
-    if (jj >= 0) {
-      const BucketRec* r = recs + jj;
-      unsigned f = 0, spins = 0;
-      for (;;) {
-        f = ld_acquire_u32(&r->flag);
-        if ((f >> 2) == ep && (f & 3u)) break;
-        if (++spins > kSpinLimit) {
-          atomicOr(err, DEV_ERR_LOOKBACK_TIMEOUT);
-          f = 0;
-          break;
-        }
-        __nanosleep(20);
-      }
-      status = ((f >> 2) == ep) ? (f & 3u) : 0u;
-      if (status == 2u) {
-        vm = (((u128)ld_cg_u64(&r->inc_hi)) << 64) | ld_cg_u64(&r->inc_lo);
-        vc = __ldcg(&r->inc_cnt);
-      } else if (status == 1u) {
-        vm = (((u128)ld_cg_u64(&r->agg_hi)) << 64) | ld_cg_u64(&r->agg_lo);
-        vc = __ldcg(&r->agg_cnt);
-      }
-    }
-    const unsigned pmask = __ballot_sync(0xffffffffu, status == 2u);
-    const int stop = pmask ? (__ffs(pmask) - 1) : 31;
-    const bool take = lane <= stop;
-    pmass += warp_sum_u128(take ? vm : (u128)0);
-    uint32_t c = take ? vc : 0u;
+// Adds a run of pn sheets of total fixed-point mass P bound for bucket d to
+// the aggregates of the next layout.
+__device__ __forceinline__ void add_run(StepSmem& S, int d, u128 P, uint32_t pn, int wlen,
+                                        unsigned long long* mass_out) {
+  const int w = d - S.win_lo;
+  if (w >= 0 && w < wlen) {
+    atomicAdd(&S.dcount[w], pn);
 #pragma unroll
-    for (int d = 16; d >= 1; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
-    pcnt += c;
-    if (pmask || j - 32 < 0) break;
-    j -= 32;
-  }
-  if (lane == 0) {
-    const u128 im = pmass + mass;
-    me->inc_lo = (uint64_t)im;
-    me->inc_hi = (uint64_t)(im >> 64);
-    me->inc_cnt = pcnt + cnt;
-    st_release_u32(&me->flag, (ep << 2) | 2u);
+    for (int k = 0; k < 8; ++k) atomicAdd(&S.dmass[w][k], (uint32_t)(P >> (16 * k)) & 0xffffu);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      atomicAdd(&mass_out[4 * (int64_t)d + k], (unsigned long long)(uint32_t)(P >> (32 * k)));
   }
 }
 
@@ -384,71 +354,161 @@ __device__ __forceinline__ int dest_bucket(const StepSmem& S, const uint64_t* qk
   return l;
 }
 
+__device__ __forceinline__ u128 mass_of_limbs(const unsigned long long* l) {
+  return (u128)l[0] + ((u128)l[1] << 32) + ((u128)l[2] << 64) + ((u128)l[3] << 96);
+}
+
+// Prepares task t (task-list entry tk) for processing; all lanes of one warp.
+//
+// Reads the simulation's abort word, its arrays for this sub-step and the
+// bucket's aggregate, clears the bucket's aggregate slot two sub-steps on,
+// and resolves the bucket's exclusive (mass, count) prefix by looking back
+// over the earlier buckets of the simulation: a bucket whose inclusive prefix
+// is published for this sub-step ends the walk, every other one contributes
+// its aggregate.  Aggregates were completed by the previous launch, so the
+// walk never waits; the bucket then publishes its own inclusive prefix.
+__device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsigned ep, int lane,
+                                             unsigned t, BucketTask tk, TaskMeta& out) {
+  if (t >= (unsigned)L.ntasks) {
+    if (lane == 0) out.task = t;
+    return;
+  }
+  const SimDev& D = L.sims[tk.sim];
+  const int64_t b = tk.bucket;
+  const int cs = (D.cs0 + sub) % kAggSlots;
+  const int cz = (cs + 2) % kAggSlots;
+  const unsigned* cnt = D.bcnt[cs];
+  const unsigned long long* mass = D.bmass[cs];
+  const unsigned ab = __ldcg(D.ocount + 1);
+  const unsigned own_c = cnt[b];
+  const u128 own_m = mass_of_limbs(mass + 4 * b);
+  // an earlier sub-step of this call overflowed the simulation: its host
+  // side finishes the call on the compact path
+  if (ab != 0 && (int)ab <= sub) {
+    if (lane == 0) {
+      out.task = t;
+      out.n = -1;
+    }
+    return;
+  }
+  if (lane == 0) D.bcnt[cz][b] = 0u;
+  if (lane < 4) D.bmass[cz][4 * b + lane] = 0ull;
+  BucketRec* recs = D.recs;
+  const unsigned inc_flag = (ep << 2) | 2u;
+  u128 pm = 0;
+  uint32_t pc = 0;
+  for (int64_t j = b - 1; j >= 0; j -= 32) {
+    const int64_t jj = j - lane;
+    bool inc = false;
+    u128 vm = 0;
+    uint32_t vc = 0;
+    if (jj >= 0) {
+      const unsigned c = cnt[jj];
+      const u128 m = mass_of_limbs(mass + 4 * jj);
+      const BucketRec* r = recs + jj;
+      inc = ld_acquire_u32(&r->flag) == inc_flag;
+      if (inc) {
+        vm = (((u128)ld_cg_u64(&r->inc_hi)) << 64) | ld_cg_u64(&r->inc_lo);
+        vc = __ldcg(&r->inc_cnt);
+      } else {
+        vm = m;
+        vc = c;
+      }
+    }
+    const unsigned pmask = __ballot_sync(0xffffffffu, inc);
+    const int stop = pmask ? (__ffs(pmask) - 1) : 31;
+    const bool take = lane <= stop;
+    pm += warp_sum_u128(take ? vm : (u128)0);
+    uint32_t c = take ? vc : 0u;
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
+    pc += c;
+    if (pmask) break;
+  }
+  if (lane == 0) {
+    BucketRec* me = recs + b;
+    const u128 im = pm + own_m;
+    me->inc_lo = (uint64_t)im;
+    me->inc_hi = (uint64_t)(im >> 64);
+    me->inc_cnt = pc + own_c;
+    st_release_u32(&me->flag, inc_flag);
+    const int lay = (D.lay0 + sub) & 1;
+    out.task = t;
+    out.sim = tk.sim;
+    out.bucket = b;
+    out.lay = lay;
+    out.x = D.bx[lay];
+    out.v = D.bv[lay];
+    out.m = D.bm[lay];
+    out.idx = D.bi[lay];
+    out.n = own_c < (unsigned)CAP ? (int)own_c : CAP;
+    out.pm_lo = (uint64_t)pm;
+    out.pm_hi = (uint64_t)(pm >> 64);
+    out.pcnt = pc;
+  }
+}
+
+// Claims a ticket and prepares its task; all lanes of one warp.
+__device__ __forceinline__ void claim_task(const StepLaunch& L, int sub, unsigned ep, int lane,
+                                           TaskMeta& out) {
+  unsigned t = 0;
+  if (lane == 0) t = atomicAdd(L.ticket, 1u);
+  t = __shfl_sync(0xffffffffu, t, 0);
+  BucketTask tk{0, 0};
+  if (t < (unsigned)L.ntasks) tk = L.tasks[t];
+  prepare_task(L, sub, ep, lane, t, tk, out);
+}
+
+// The fused sub-step.  LAST: the call's last sub-step (half drift, outputs).
+template <bool LAST>
 __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   StepSmem& S = *reinterpret_cast<StepSmem*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int sub = L.sub;
-  const bool last = sub == L.nleap - 1;
+  const unsigned ep = L.epochs[sub];
   if (tid == 0) {
-    S.epoch = L.epochs[sub];
     mbar_init(&S.mbar, 1);
     fence_proxy_async_smem();
   }
+  if (warp == 0) claim_task(L, sub, ep, lane, S.next);
   unsigned parity = 0;
   for (;;) {
     __syncthreads();
-    if (tid == 0) {
-      S.task = atomicAdd(L.ticket, 1u);
-      if (S.task < (unsigned)L.ntasks) {
-        const BucketTask t = L.tasks[S.task];
-        S.sim = t.sim;
-        S.bucket = t.bucket;
-      }
+    const TaskMeta tm = S.next;  // claimed during the previous task
+    if (tm.task >= (unsigned)L.ntasks) break;
+    if (tm.n < 0) {
+      __syncthreads();  // every thread has read S.next
+      if (warp == 0) claim_task(L, sub, ep, lane, S.next);
+      continue;
     }
-    __syncthreads();
-    if (S.task >= (unsigned)L.ntasks) break;
-    const SimDev& D = L.sims[S.sim];
-    {
-      // an earlier sub-step of this call overflowed this simulation: its
-      // host side finishes the call on the compact path
-      const unsigned ab = *(volatile const unsigned*)(D.ocount + 1);
-      if (ab != 0 && (int)ab <= sub) continue;
+    const SimDev& D = L.sims[tm.sim];
+    const int64_t b = tm.bucket;
+    const int lay = tm.lay;
+    const int n = tm.n;
+    const int64_t base = b * CAP;
+    // ---- load: the bucket's four arrays arrive by bulk copy (sizes rounded
+    // up to 4 sheets, which stays inside the bucket's capacity), then its
+    // keys and key range are formed from shared memory
+    const int n4 = (n + 3) & ~3;
+    if (n4 > 0 && tid == 0) {
+      fence_proxy_async_smem();  // earlier generic accesses to these buffers are done
+      mbar_expect_tx(&S.mbar, (uint32_t)n4 * 28u);
+      bulk_g2s(S.x, tm.x + base, (uint32_t)n4 * 8u, &S.mbar);
+      bulk_g2s(S.v, tm.v + base, (uint32_t)n4 * 8u, &S.mbar);
+      bulk_g2s(S.m, tm.m + base, (uint32_t)n4 * 8u, &S.mbar);
+      bulk_g2s(S.idx, tm.idx + base, (uint32_t)n4 * 4u, &S.mbar);
     }
-    const int64_t b = S.bucket;
-    const int lay = (D.lay0 + sub) & 1, qs = (D.qsel0 + sub) & 1;
-    const double* xin = D.bx[lay];
-    const double* vin = D.bv[lay];
-    const double* min = D.bm[lay];
-    const int32_t* iin = D.bi[lay];
-    unsigned* cnt_in = D.bcnt[lay];
+    // the next task's ticket and task-list entry are read ahead (thread 0)
+    // and the task is prepared by warp 0 during the write-out
+    unsigned nt = 0;
+    if (tid == 0) nt = atomicAdd(L.ticket, 1u);
+    const int qs = (D.qsel0 + sub) & 1;
     const uint64_t* qdk = D.qk[qs];
     const int32_t* qdi = D.qi[qs];
-    const int64_t base = b * CAP;
-    int n = (int)cnt_in[b];
-    n = n < CAP ? n : CAP;
     const int ipt = (n + BT - 1) / BT;
     const double pre = sub == 0 ? D.pre_dt : 0.0;
     const int E = D.E;
-    __syncthreads();  // every thread has read cnt_in[b]
-    if (tid == 0) {
-      cnt_in[b] = 0;  // this count buffer is the target two sub-steps on
-      S.amp = (D.ext.kind == EXT_PULSE_TANH) ? pulse_amplitude(D.ext, D.t_seq[sub]) : 0.0;
-    }
-    // ---- load: the bucket's four arrays arrive by bulk copy (sizes rounded
-    // up to 4 sheets, which stays inside the bucket's capacity), then its
-    // keys, key range, mass and count are formed from shared memory
-    const int n4 = (n + 3) & ~3;
-    if (n4 > 0) {
-      if (tid == 0) {
-        fence_proxy_async_smem();  // earlier generic accesses to these buffers are done
-        mbar_expect_tx(&S.mbar, (uint32_t)n4 * 28u);
-        bulk_g2s(S.x, xin + base, (uint32_t)n4 * 8u, &S.mbar);
-        bulk_g2s(S.v, vin + base, (uint32_t)n4 * 8u, &S.mbar);
-        bulk_g2s(S.m, min + base, (uint32_t)n4 * 8u, &S.mbar);
-        bulk_g2s(S.idx, iin + base, (uint32_t)n4 * 4u, &S.mbar);
-      }
-    }
     // splitter window of the next layout around this bucket, fetched while
     // the bulk copies are in flight
     const int rw = D.window;
@@ -458,18 +518,22 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       S.wkey[j] = qdk[wlo + j];
       S.widx[j] = qdi[wlo + j];
       S.dcount[j] = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) S.dmass[j][k] = 0u;
     }
     if (tid == 0) {
       S.win_lo = wlo;
       S.win_hi = whi;
       S.maxv = 0;
+      S.prefix_mass = (((u128)tm.pm_hi) << 64) | tm.pm_lo;
+      S.prefix_cnt = tm.pcnt;
+      S.amp = (D.ext.kind == EXT_PULSE_TANH) ? pulse_amplitude(D.ext, D.t_seq[sub]) : 0.0;
     }
     if (n4 > 0) {
       if (!mbar_wait(&S.mbar, parity) && tid == 0) atomicOr(L.err, DEV_ERR_BAD_STATE);
       parity ^= 1u;
     }
     uint64_t kmin = ~0ull, kmax = 0;
-    u128 msum = 0;
 #pragma unroll 4
     for (int j = tid; j < n; j += BT) {
       double x = S.x[j];
@@ -478,10 +542,8 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
         S.x[j] = x;
       }
       const uint64_t k = key_of(x);
-      S.key[j] = k;
       kmin = k < kmin ? k : kmin;
       kmax = k > kmax ? k : kmax;
-      msum += mass_to_fixed(S.m[j], E);
     }
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) {
@@ -490,22 +552,15 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       kmin = o1 < kmin ? o1 : kmin;
       kmax = o2 > kmax ? o2 : kmax;
     }
-    msum = warp_sum_u128(msum);
     if (lane == 0) {
       S.red_min[warp] = kmin;
       S.red_max[warp] = kmax;
-      S.warp_mass[warp] = msum;
     }
     __syncthreads();
-    if (warp == 0) {
-      const u128 bm = warp_sum_u128(lane < WARPS ? S.warp_mass[lane] : (u128)0);
-      u128 pm;
-      uint32_t pc;
-      bucket_lookback(D.recs, b, bm, (uint32_t)n, S.epoch, lane, L.err, pm, pc);
-      if (lane == 0) {
-        S.prefix_mass = pm;
-        S.prefix_cnt = pc;
-      }
+    BucketTask ntk{0, 0};
+    if (tid == 0) {
+      S.next_ticket = nt;
+      if (nt < (unsigned)L.ntasks) ntk = L.tasks[nt];
     }
     kmin = ~0ull;
     kmax = 0;
@@ -514,7 +569,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       kmin = S.red_min[w] < kmin ? S.red_min[w] : kmin;
       kmax = S.red_max[w] > kmax ? S.red_max[w] : kmax;
     }
-    // ---- sort the bucket (barriers inside wait for the look-back warp)
+    // ---- sort the bucket
     if (n > 1) {
       bucket_sort(S, n, ipt, kmin, kmax, D.sort_bits);
     } else {
@@ -524,6 +579,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
 
     // ---- exact prefix of the masses in sorted order: thread tid holds the
     // sorted positions [tid * ipt, tid * ipt + ipt)
+    if (tid == 0) S.next_tk = ntk;
     const int j0 = tid * ipt;
     const int nmine = (j0 < n) ? ((n - j0) < ipt ? (n - j0) : ipt) : 0;
     u128 tot = 0;
@@ -568,19 +624,19 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     const ExtForce ext = D.ext;
     const uint32_t target = (uint32_t)D.target;
     const int64_t nbk = D.nb;
-    double* const x_out = D.x_out;
-    double* const v_out = D.v_out;
-    SheetRec* const xi_out = D.xi_out;
-    double* const a_out = D.a_out;
     // ---- force, kick, drift, routing; new x, v go back to their slots and
-    // the destination of every slot to the (now free) sort area
-    int32_t* sdst = reinterpret_cast<int32_t*>(S.u.bins);          // [CAP]
-    uint16_t* srank = reinterpret_cast<uint16_t*>(sdst + CAP);     // [CAP]
+    // the destination of every sorted position to the (now free) sort area
+    int32_t* sdst = S.u.dst;
     const double dt = L.profile ? 0.0 : D.dt;
-    const double dt_drift = last ? dt / 2. : dt;
-    const double dest_dt = (last && !L.profile) ? dt / 2. : 0.0;
+    const double dt_drift = LAST ? dt / 2. : dt;
+    const double dest_dt = (LAST && !L.profile) ? dt / 2. : 0.0;
     const i128 T = (i128)((((u128)D.T_hi) << 64) | D.T_lo);
     unsigned long long maxv = 0;
+    // the first rank >= rank0 that is a positive multiple of the target
+    // starts the next splitter (one per thread at most: ipt <= 8 < target)
+    uint32_t qnext = (rank0 + target - 1) / target;
+    qnext = qnext ? qnext : 1u;
+    const uint32_t rnext = qnext * target;
     // two sheets at a time, interleaved, so that their shared-memory and
     // FP64 latencies overlap; the window searches run in lock-step
     const int wlen = S.win_hi - S.win_lo;
@@ -605,12 +661,11 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
         }
         const int sidx = sl[u];
         const uint32_t r = rank0 + (uint32_t)(i0 + u);
-        const uint64_t key = S.key[sidx];
-        if (r != 0 && (r % target) == 0) {
-          qnk[r / target] = key;
-          qni[r / target] = idv[u];
-        }
         const double x = S.x[sidx], v = S.v[sidx];
+        if (r == rnext) {
+          qnk[qnext] = key_of(x);
+          qni[qnext] = idv[u];
+        }
         const u128 M = mass_to_fixed(S.m[sidx], E);
         const i128 A = T - 2 * (i128)C - (i128)M;
         C += M;
@@ -624,9 +679,10 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
         const unsigned long long av =
             (unsigned long long)__double_as_longlong(vn) & 0x7FFFFFFFFFFFFFFFull;
         maxv = av > maxv ? av : maxv;
-        if (last && !L.profile) {
-          x_out[idv[u]] = xn;
-          v_out[idv[u]] = vn;
+        if (LAST && !L.profile) {
+          D.x_out[idv[u]] = xn;
+          D.v_out[idv[u]] = vn;
+          SheetRec* const xi_out = D.xi_out;
           if (xi_out) {
             SheetRec rec;
             rec.idx = idv[u];
@@ -634,9 +690,10 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
             rec.val = xn;
             xi_out[r] = rec;
           }
+          double* const a_out = D.a_out;
           if (a_out) a_out[idv[u]] = acc;
         }
-        kd[u] = key_of(dest_dt != 0.0 ? fma(dest_dt, vn, xn) : xn);
+        kd[u] = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, vn, xn) : xn);
       }
       // routing: binary lifting over the window, both sheets in lock-step
       int l[2] = {0, 0};
@@ -653,42 +710,104 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       for (int u = 0; u < 2; ++u) {
         if (!live[u]) continue;
         const int d = inw[u] ? S.win_lo + l[u] : dest_bucket(S, qdk, qdi, nbk, kd[u], idv[u]);
-        sdst[sl[u]] = d;
-        srank[sl[u]] = (d >= S.win_lo && d < S.win_hi)
-                           ? (uint16_t)atomicAdd(&S.dcount[d - S.win_lo], 1u)
-                           : (uint16_t)0xffffu;
+        sdst[j0 + i0 + u] = d;
       }
     }
     __syncthreads();
-    for (int j = tid; j < S.win_hi - S.win_lo; j += BT) {
-      const uint32_t c = S.dcount[j];
-      S.dbase[j] = c ? atomicAdd(&D.bcnt[1 - lay][S.win_lo + j], c) : 0u;
+    // ---- aggregates of the next layout: each thread walks its sorted
+    // positions and adds every run of sheets bound for one bucket, as
+    // (count, mass), to that bucket's window entry -- or, outside the window,
+    // the mass straight to the bucket's accumulators (the count of such
+    // sheets is added when their slots are claimed below)
+    const int cw = (D.cs0 + sub + 1) % kAggSlots;
+    unsigned* const cnt_out = D.bcnt[cw];
+    unsigned long long* const mass_out = D.bmass[cw];
+    {
+      int dcur = -1;
+      u128 P = 0;
+      uint32_t pn = 0;
+      for (int i = 0; i < nmine; ++i) {
+        const int d = sdst[j0 + i];
+        const u128 M = mass_to_fixed(S.m[S.perm[j0 + i]], E);
+        if (d != dcur) {
+          if (pn) add_run(S, dcur, P, pn, wlen, mass_out);
+          dcur = d;
+          P = M;
+          pn = 1;
+        } else {
+          P += M;
+          ++pn;
+        }
+      }
+      // the last runs of a warp's threads usually share a bucket: one add
+      const unsigned same = __match_any_sync(0xffffffffu, pn ? dcur : -1);
+      if (same == 0xffffffffu && pn) {
+        P = warp_sum_u128(P);
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) pn += __shfl_xor_sync(0xffffffffu, pn, d);
+        if (lane == 0) add_run(S, dcur, P, pn, wlen, mass_out);
+      } else if (pn) {
+        add_run(S, dcur, P, pn, wlen, mass_out);
+      }
     }
     __syncthreads();
-    double* xout = D.bx[1 - lay];
-    double* vout = D.bv[1 - lay];
-    double* mout = D.bm[1 - lay];
-    int32_t* iout = D.bi[1 - lay];
+    for (int j = tid; j < wlen; j += BT) {
+      const uint32_t c = S.dcount[j];
+      uint32_t db = 0;
+      if (c) {
+        const int64_t d = S.win_lo + j;
+        db = atomicAdd(&cnt_out[d], c);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          atomicAdd(&mass_out[4 * d + k], (unsigned long long)S.dmass[j][2 * k] +
+                                              ((unsigned long long)S.dmass[j][2 * k + 1] << 16));
+      }
+      S.dbase[j] = db;
+      S.dcount[j] = 0;  // reused below as the fill level of each destination
+    }
+    __syncthreads();
     bool overflow = false;
-#pragma unroll 4
-    for (int j = tid; j < n; j += BT) {
-      const int d = sdst[j];
-      const uint16_t rk = srank[j];
-      const uint32_t slot = rk == 0xffffu ? atomicAdd(&D.bcnt[1 - lay][d], 1u)
-                                          : S.dbase[d - S.win_lo] + rk;
-      if (slot < (uint32_t)CAP) {
-        const int64_t o = (int64_t)d * CAP + slot;
-        xout[o] = S.x[j];
-        vout[o] = S.v[j];
-        mout[o] = S.m[j];
-        iout[o] = S.idx[j];
-      } else {
-        const uint32_t o = atomicAdd(D.ocount, 1u);
-        D.ox[o] = S.x[j];
-        D.ov[o] = S.v[j];
-        D.om[o] = S.m[j];
-        D.oi[o] = S.idx[j];
-        overflow = true;
+    if (warp == 0) {
+      // the next task, prepared while the other warps write
+      prepare_task(L, sub, ep, lane, S.next_ticket, S.next_tk, S.next);
+    } else {
+      // write-out in sorted order: a warp takes 32 consecutive sorted
+      // positions, and the sheets among them bound for one bucket take
+      // consecutive slots there, so the stores coalesce
+      double* const xout = D.bx[1 - lay];
+      double* const vout = D.bv[1 - lay];
+      double* const mout = D.bm[1 - lay];
+      int32_t* const iout = D.bi[1 - lay];
+      const int nr = (n + 31) & ~31;
+      for (int p = tid - 32; p < nr; p += BT - 32) {
+        const bool ok = p < n;
+        const int d = ok ? sdst[p] : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int leader = __ffs(peers) - 1;
+        uint32_t first = 0;
+        if (ok && lane == leader) {
+          const int w = d - S.win_lo;
+          first = (w >= 0 && w < wlen) ? S.dbase[w] + atomicAdd(&S.dcount[w], __popc(peers))
+                                       : atomicAdd(&cnt_out[d], __popc(peers));
+        }
+        first = __shfl_sync(0xffffffffu, first, leader);
+        if (!ok) continue;
+        const uint32_t slot = first + __popc(peers & lanemask_lt());
+        const int s = S.perm[p];
+        if (slot < (uint32_t)CAP) {
+          const int64_t o = (int64_t)d * CAP + slot;
+          xout[o] = S.x[s];
+          vout[o] = S.v[s];
+          mout[o] = S.m[s];
+          iout[o] = S.idx[s];
+        } else {
+          const uint32_t o = atomicAdd(D.ocount, 1u);
+          D.ox[o] = S.x[s];
+          D.ov[o] = S.v[s];
+          D.om[o] = S.m[s];
+          D.oi[o] = S.idx[s];
+          overflow = true;
+        }
       }
     }
 #pragma unroll
@@ -703,28 +822,51 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
   }
 }
 
-// Compact sorted state -> bucket layout with exactly T sheets per bucket and
-// the splitters Q_b = (key, idx) of the sheet at rank b*T.
-__global__ void k_bucketize(const StateTable* table, int64_t n, int target, int64_t nb,
-                            double* x, double* v, double* m, int32_t* idx, unsigned* cnt,
-                            uint64_t* qk, int32_t* qi, unsigned* cnt_other) {
+// Compact sorted state -> bucket layout with exactly T sheets per bucket,
+// the splitters Q_b = (key, idx) of the sheet at rank b*T, and the buckets'
+// aggregates in slot 0 (slots 1 and 2 cleared).  One block per bucket.
+__global__ void k_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int E,
+                            double* x, double* v, double* m, int32_t* idx, unsigned* cnt0,
+                            unsigned* cnt1, unsigned* cnt2, unsigned long long* mass0,
+                            unsigned long long* mass1, unsigned long long* mass2, uint64_t* qk,
+                            int32_t* qi) {
+  __shared__ u128 s_mass[32];
   const StateRef st = table->cur;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += stride) {
-    const int64_t b = r / target, j = r - b * target;
-    const int64_t o = b * CAP + j;
-    x[o] = st.x[r];
-    v[o] = st.v[r];
-    m[o] = st.m[r];
-    idx[o] = st.idx[r];
-    if (j == 0) {
-      cnt[b] = (unsigned)((n - r) < target ? (n - r) : target);
-      cnt_other[b] = 0;
-      if (b > 0) {
-        qk[b] = key_of(st.x[r]);
-        qi[b] = st.idx[r];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t b = blockIdx.x; b < nb; b += gridDim.x) {
+    const int64_t r0 = b * target;
+    const int c = (int)((n - r0) < target ? (n - r0) : target);
+    u128 msum = 0;
+    for (int j = threadIdx.x; j < c; j += blockDim.x) {
+      const int64_t o = b * CAP + j;
+      const double mj = st.m[r0 + j];
+      x[o] = st.x[r0 + j];
+      v[o] = st.v[r0 + j];
+      m[o] = mj;
+      idx[o] = st.idx[r0 + j];
+      msum += mass_to_fixed(mj, E);
+    }
+    msum = warp_sum_u128(msum);
+    if (lane == 0) s_mass[warp] = msum;
+    __syncthreads();
+    if (warp == 0) {
+      const u128 t = warp_sum_u128(lane < (int)(blockDim.x >> 5) ? s_mass[lane] : (u128)0);
+      if (lane < 4) {
+        mass0[4 * b + lane] = (uint32_t)(t >> (32 * lane));
+        mass1[4 * b + lane] = 0ull;
+        mass2[4 * b + lane] = 0ull;
+      }
+      if (lane == 0) {
+        cnt0[b] = (unsigned)c;
+        cnt1[b] = 0u;
+        cnt2[b] = 0u;
+        if (b > 0) {
+          qk[b] = key_of(st.x[r0]);
+          qi[b] = st.idx[r0];
+        }
       }
     }
+    __syncthreads();
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     qk[0] = 0ull;
@@ -815,7 +957,9 @@ void set_tuning(const std::vector<std::pair<int64_t, BucketTuning>>& rows) {
 void bucket_step_prepare() {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_bucket_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_bucket_step<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(StepSmem));
+    cudaFuncSetAttribute(k_bucket_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)sizeof(StepSmem));
     attr = true;
   }
@@ -825,16 +969,20 @@ void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s) {
   bucket_step_prepare();
   if (grid > a.ntasks) grid = a.ntasks;
   if (grid < 1) grid = 1;
-  k_bucket_step<<<grid, BT, sizeof(StepSmem), s>>>(a);
+  if (a.sub == a.nleap - 1)
+    k_bucket_step<true><<<grid, BT, sizeof(StepSmem), s>>>(a);
+  else
+    k_bucket_step<false><<<grid, BT, sizeof(StepSmem), s>>>(a);
 }
 
-void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, double* x,
-                      double* v, double* m, int32_t* idx, unsigned* cnt, uint64_t* qk,
-                      int32_t* qi, unsigned* cnt_other, cudaStream_t s) {
-  int64_t g = (n + 255) / 256;
-  if (g > 152 * 16) g = 152 * 16;
-  k_bucketize<<<(unsigned)g, 256, 0, s>>>(table, n, target, nb, x, v, m, idx, cnt, qk, qi,
-                                           cnt_other);
+void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int E,
+                      double* x, double* v, double* m, int32_t* idx,
+                      unsigned* const cnt[kAggSlots], unsigned long long* const mass[kAggSlots],
+                      uint64_t* qk, int32_t* qi, cudaStream_t s) {
+  int64_t g = nb < 152 * 8 ? nb : 152 * 8;
+  if (g < 1) g = 1;
+  k_bucketize<<<(unsigned)g, 256, 0, s>>>(table, n, target, nb, E, x, v, m, idx, cnt[0], cnt[1],
+                                           cnt[2], mass[0], mass[1], mass[2], qk, qi);
 }
 
 void launch_compact(StateTable* table, int64_t nb, const double* x, const double* v,

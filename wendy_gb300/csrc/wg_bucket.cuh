@@ -32,14 +32,22 @@ BucketTuning tuning_for(int64_t n);
 namespace wg {
 void set_tuning(const std::vector<std::pair<int64_t, BucketTuning>>& rows);
 
-// Decoupled look-back record of one bucket (48 bytes).
+// Look-back record of one bucket (32 bytes): its inclusive (mass, count)
+// prefix, valid when flag == (epoch << 2) | 2 for the sub-step's epoch.
 struct __align__(16) BucketRec {
-  uint64_t agg_lo, agg_hi;    // bucket's fixed-point mass
-  uint64_t inc_lo, inc_hi;    // inclusive mass prefix
-  uint32_t agg_cnt, inc_cnt;  // sheet count, inclusive count prefix
-  unsigned flag;              // (epoch << 2) | {1: aggregate, 2: inclusive}
-  unsigned pad;
+  uint64_t inc_lo, inc_hi;    // inclusive fixed-point mass prefix
+  uint32_t inc_cnt;           // inclusive sheet-count prefix
+  unsigned flag;
+  uint64_t pad;
 };
+
+// Per-bucket aggregates (sheet count and fixed-point mass) rotate over three
+// slots: sub-step g reads slot g % 3 (filled by the writers of sub-step g - 1),
+// its writers fill slot (g + 1) % 3, and it clears slot (g + 2) % 3 for the
+// sub-step after.  The mass is kept as four 32-bit limbs in 64-bit
+// accumulators, mass = sum_k limb[k] << 32 k, so that writers can add to it
+// with plain 64-bit atomics.
+constexpr int kAggSlots = 3;
 
 // Same layout as wendy's struct array_w_index (int idx; double val).
 struct SheetRec {
@@ -56,7 +64,8 @@ struct SimDev {
   double* bv[2];
   double* bm[2];
   int32_t* bi[2];
-  unsigned* bcnt[2];     // per-bucket sheet counts of each layout
+  unsigned* bcnt[kAggSlots];         // per-bucket sheet counts
+  unsigned long long* bmass[kAggSlots];  // per-bucket mass limbs [4 * nb]
   uint64_t* qk[2];       // [nb + 1] splitter keys (Q_0 = -inf, Q_nb = +inf)
   int32_t* qi[2];        // [nb + 1] splitter indices
   BucketRec* recs;       // [nb]
@@ -86,6 +95,8 @@ struct SimDev {
   double pre_dt;         // half drift applied while loading the first sub-step (or 0)
   int lay0;              // layout read by the call's first sub-step
   int qsel0;             // splitter array defining the layout the first sub-step writes
+  int cs0;               // aggregate slot read by the call's first sub-step
+  int pad1;
 };
 
 struct BucketTask {
@@ -109,9 +120,12 @@ void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s);
 // One-time kernel attribute set-up; call before any stream capture.
 void bucket_step_prepare();
 int bucket_step_grid(int sm_count);
-void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, double* x,
-                      double* v, double* m, int32_t* idx, unsigned* cnt, uint64_t* qk,
-                      int32_t* qi, unsigned* cnt_other, cudaStream_t s);
+// Compact sorted state -> layout 0 with `target` sheets per bucket; fills
+// aggregate slot 0 and clears the other two.
+void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int E,
+                      double* x, double* v, double* m, int32_t* idx,
+                      unsigned* const cnt[kAggSlots], unsigned long long* const mass[kAggSlots],
+                      uint64_t* qk, int32_t* qi, cudaStream_t s);
 void launch_compact(StateTable* table, int64_t nb, const double* x, const double* v,
                     const double* m, const int32_t* idx, const unsigned* cnt, unsigned* offs,
                     const double* ox, const double* ov, const double* om, const int32_t* oi,

@@ -76,7 +76,8 @@ struct PoolSim {
   double* bv[2];
   double* bm[2];
   int32_t* bi[2];
-  unsigned* bcnt[2];
+  unsigned* bcnt[kAggSlots];
+  unsigned long long* bmass[kAggSlots];
   uint64_t* qk[2];
   int32_t* qi[2];
   BucketRec* recs;
@@ -89,6 +90,7 @@ struct PoolSim {
   ExtForce ext{};
   int mode = 0;  // 0: sheets compact in ox..oi, half drift pending; 1: bucket layout
   int lay = 0, qsel = 0;
+  int cslot = 0;  // aggregate slot describing layout `lay`
   double pending_dt = 0;
   bool fresh = false;      // just bucketized: the opening half drift is already applied
   bool out_valid = false;  // x_out / v_out hold the last output
@@ -99,7 +101,8 @@ size_t sim_bytes(int64_t n) {
   const BucketTuning t = tuning_for(n);
   const int64_t nb = (n + t.target - 1) / t.target;
   const size_t slots = (size_t)nb * kBucketCap;
-  return 2 * (3 * al(slots * 8) + al(slots * 4)) + 2 * al(4 * (size_t)nb) +
+  return 2 * (3 * al(slots * 8) + al(slots * 4)) +
+         kAggSlots * (al(4 * (size_t)nb) + al(32 * (size_t)nb)) +
          2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
          al(sizeof(BucketRec) * (size_t)nb) + 3 * al(8 * (size_t)n) + al(4 * (size_t)n) +
          2 * al(8 * (size_t)n);
@@ -114,8 +117,9 @@ void carve(PoolSim* s) {
     s->bm[k] = reinterpret_cast<double*>(p); p += al(slots * 8);
     s->bi[k] = reinterpret_cast<int32_t*>(p); p += al(slots * 4);
   }
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < kAggSlots; ++k) {
     s->bcnt[k] = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)s->nb);
+    s->bmass[k] = reinterpret_cast<unsigned long long*>(p); p += al(32 * (size_t)s->nb);
   }
   for (int k = 0; k < 2; ++k) {
     s->qk[k] = reinterpret_cast<uint64_t*>(p); p += al(8 * (size_t)(s->nb + 1));
@@ -297,21 +301,22 @@ int to_buckets(wg_pool* p, PoolSim* s, double dt) {
   k_set_table<<<1, 1, 0, p->stream>>>(p->table, own, p->set[1]);
   launch_drift(p->table, s->n, dt / 2., &p->wflags[0], p->stream);  // also marks "unsorted"
   radix_sort_state(p->table, s->n, &p->radix, &p->wflags[0], p->err, p->stream);
-  launch_bucketize(p->table, s->n, s->tune.target, s->nb, s->bx[0], s->bv[0], s->bm[0],
-                   s->bi[0], s->bcnt[0], s->qk[0], s->qi[0], s->bcnt[1], p->stream);
+  launch_bucketize(p->table, s->n, s->tune.target, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
+                   s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], p->stream);
   p->launches += 3 + kRadixLaunches;
   s->lay = 0;
   s->qsel = 0;
+  s->cslot = 0;
   s->mode = 1;
   s->pending_dt = dt;
   return WG_OK;
 }
 
-// Bucket layout `lay` of s (+ the overflow entries counted in oc) -> the
-// workspace's first set, unsorted.
-void buckets_to_workspace(wg_pool* p, PoolSim* s, int lay, const unsigned* oc) {
+// Bucket layout `lay` of s with the counts of aggregate slot `cslot` (+ the
+// overflow entries counted in oc) -> the workspace's first set, unsorted.
+void buckets_to_workspace(wg_pool* p, PoolSim* s, int lay, int cslot, const unsigned* oc) {
   k_set_table<<<1, 1, 0, p->stream>>>(p->table, p->set[0], p->set[1]);
-  launch_compact(p->table, s->nb, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay], s->bcnt[lay],
+  launch_compact(p->table, s->nb, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay], s->bcnt[cslot],
                  p->offs, s->ox, s->ov, s->om, s->oi, oc, s->n, p->stream);
   p->launches += 3;
 }
@@ -491,7 +496,7 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
     if (s->mode == 1 && dt[k] != s->pending_dt) {
       rc = ensure_workspace(p, s->n);
       if (rc) return rc;
-      buckets_to_workspace(p, s, s->lay, p->ocount + 2 * k);
+      buckets_to_workspace(p, s, s->lay, s->cslot, p->ocount + 2 * k);
       store_compact(p, s);
       s->mode = 0;
     }
@@ -512,9 +517,12 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
       d.bv[j] = s->bv[j];
       d.bm[j] = s->bm[j];
       d.bi[j] = s->bi[j];
-      d.bcnt[j] = s->bcnt[j];
       d.qk[j] = s->qk[j];
       d.qi[j] = s->qi[j];
+    }
+    for (int j = 0; j < kAggSlots; ++j) {
+      d.bcnt[j] = s->bcnt[j];
+      d.bmass[j] = s->bmass[j];
     }
     d.recs = s->recs;
     d.ox = s->ox;
@@ -543,6 +551,7 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
     d.pre_dt = s->fresh ? 0.0 : dt[k] / 2.;
     d.lay0 = s->lay;
     d.qsel0 = s->qsel;
+    d.cs0 = s->cslot;
     for (int64_t b = 0; b < s->nb; ++b) p->h_tasks[t++] = BucketTask{k, (int)b};
   }
   // device sequence of the call, captured in a CUDA graph and replayed while
@@ -604,9 +613,10 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
   // bookkeeping, and recovery of simulations that overflowed a bucket
   for (int k = 0; k < count; ++k) {
     PoolSim* s = act[(size_t)k];
-    const int lay0 = s->lay;
+    const int lay0 = s->lay, cs0 = s->cslot;
     s->lay = (lay0 + nleap) & 1;
     s->qsel = (s->qsel + nleap) & 1;
+    s->cslot = (cs0 + nleap) % kAggSlots;
     s->mode = 1;
     s->pending_dt = dt[k];
     s->fresh = false;
@@ -617,7 +627,7 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
     const int lay_k = (kk % 2 == 0) ? 1 - lay0 : lay0;
     rc = ensure_workspace(p, s->n);
     if (rc) return rc;
-    buckets_to_workspace(p, s, lay_k, p->ocount + 2 * k);
+    buckets_to_workspace(p, s, lay_k, (cs0 + kk + 1) % kAggSlots, p->ocount + 2 * k);
     if (kk < nleap - 1) {
       ForceArgs f;
       f.table = p->table;
