@@ -413,18 +413,26 @@ int finish_call(wg_sim* s, int nleap, bool count_sorts = true) {
   return WG_OK;
 }
 
+// Epochs of the next `count` sub-steps into s->h_ep.  They stay within
+// [1, kEpochLimit]: before passing it every look-back record is cleared and
+// the epochs restart at 1.
+int take_epochs(wg_sim* s, int count) {
+  if (s->epoch + (unsigned)count > kEpochLimit) {
+    WG_CUDA(cudaMemsetAsync(s->recs, 0, sizeof(TileRec) * (size_t)s->n_tiles, s->stream));
+    WG_CUDA(cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)s->nb, s->stream));
+    s->epoch = 1;
+  }
+  for (int i = 0; i < count; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
+  s->epoch += (unsigned)count;
+  return WG_OK;
+}
+
 // Enqueue one output interval: half drift, nleap x [sort, force/kick/drift].
 // The last force evaluation's accelerations go to s->a_sorted when
 // want_accel is set.  t_seq must be in s->h_t already.
 int enqueue_step(wg_sim* s, double dt, int nleap, bool want_accel, double dt_last_drift) {
-  for (int i = 0; i < nleap; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
-  s->epoch += (unsigned)nleap;
-  if (s->epoch > (1u << 29)) {  // keep (epoch << 2) in 32 bits: restart epochs
-    WG_CUDA(cudaMemsetAsync(s->recs, 0, sizeof(TileRec) * (size_t)s->n_tiles, s->stream));
-    s->epoch = 1;
-    for (int i = 0; i < nleap; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
-    s->epoch += (unsigned)nleap;
-  }
+  int rc = take_epochs(s, nleap);
+  if (rc) return rc;
   WG_CUDA(cudaMemcpyAsync(s->t_seq, s->h_t, 8 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->epochs, s->h_ep, 4 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemsetAsync(s->flags, 0, sizeof(StepFlags) * (nleap + 1), s->stream));
@@ -650,15 +658,8 @@ static int run_call(wg_sim* s, double dt, int nleap, double* t0, double* time_el
   int rc = alloc_call_arrays(s, nleap);
   if (rc) return rc;
   fill_times(s, dt, nleap, t0);
-  for (int i = 0; i < nleap; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
-  s->epoch += (unsigned)nleap;
-  if (s->epoch > (1u << 29)) {
-    WG_CUDA(cudaMemsetAsync(s->recs, 0, sizeof(TileRec) * (size_t)s->n_tiles, s->stream));
-    WG_CUDA(cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)s->nb, s->stream));
-    s->epoch = 1;
-    for (int i = 0; i < nleap; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
-    s->epoch += (unsigned)nleap;
-  }
+  rc = take_epochs(s, nleap);
+  if (rc) return rc;
   if (record_start) WG_CUDA(cudaEventRecord(s->ev0, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->t_seq, s->h_t, 8 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->epochs, s->h_ep, 4 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
@@ -767,7 +768,7 @@ int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
     set_error("null simulation");
     return WG_ERR_ARG;
   }
-  if (nleap < 1 || !std::isfinite(dt)) {
+  if (nleap < 1 || nleap > kMaxLeap || !std::isfinite(dt)) {
     set_error("nleap must be >= 1 and dt finite");
     return WG_ERR_ARG;
   }
@@ -806,7 +807,7 @@ int wg_destroy(wg_sim* s) {
 }
 
 int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
-  if (!s || reps < 1 || !avg_seconds ||
+  if (!s || reps < 1 || reps > kMaxLeap || !avg_seconds ||
       (what != WG_PROF_FORCE && what != WG_PROF_SORT && what != WG_PROF_BUCKET)) {
     set_error("bad arguments to wg_profile");
     return WG_ERR_ARG;
@@ -817,11 +818,9 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   }
   int rc = alloc_call_arrays(s, reps);
   if (rc) return rc;
-  for (int i = 0; i < reps; ++i) {
-    s->h_t[i] = 0.0;
-    s->h_ep[i] = s->epoch + (unsigned)i;
-  }
-  s->epoch += (unsigned)reps;
+  for (int i = 0; i < reps; ++i) s->h_t[i] = 0.0;
+  rc = take_epochs(s, reps);
+  if (rc) return rc;
   WG_CUDA(cudaMemcpyAsync(s->t_seq, s->h_t, 8 * (size_t)reps, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->epochs, s->h_ep, 4 * (size_t)reps, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemsetAsync(s->tickets, 0, 4 * (size_t)reps, s->stream));
@@ -998,8 +997,8 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
                             double omega2, int ext_kind, const double* ext_params,
                             int n_ext_params, int* err, double* time_elapsed) {
   if (err) *err = 0;
-  if (!xi || !x || !v || !m || !a || nleap < 1 || n < 1) {
-    set_error("null buffer, n < 1 or nleap < 1");
+  if (!xi || !x || !v || !m || !a || nleap < 1 || nleap > kMaxLeap || n < 1) {
+    set_error("null buffer, n < 1, nleap < 1 or nleap > %d", kMaxLeap);
     return WG_ERR_ARG;
   }
   ExtForce ext;

@@ -91,7 +91,10 @@ struct StepSmem {
   union {
     uint32_t bins[NBIN_PAD];
     LsdSmem lsd;
-    int32_t dst[CAP];  // destination bucket of each sorted position
+    struct {
+      u128 mfix[CAP];    // fixed-point mass of each sorted position
+      int32_t dst[CAP];  // destination bucket of each sorted position
+    } pos;
   } u;
   uint64_t wkey[2 * RWIN + 2];
   int32_t widx[2 * RWIN + 2];
@@ -121,7 +124,8 @@ __device__ __forceinline__ bool pair_less(uint64_t k1, int32_t i1, uint64_t k2, 
 }
 
 // Block-wide exclusive scan of one value per thread; returns the exclusive
-// prefix and (through total) the block total.  Contains barriers.
+// prefix and (through total) the block total.  Contains one barrier; the
+// caller passes another before the next call (scan_tmp is reused).
 __device__ __forceinline__ uint32_t block_excl_scan(StepSmem& S, uint32_t v, uint32_t& total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t incl = v;
@@ -140,7 +144,6 @@ __device__ __forceinline__ uint32_t block_excl_scan(StepSmem& S, uint32_t v, uin
     pre += (w < warp) ? t : 0u;
     total += t;
   }
-  __syncthreads();
   return pre + incl - v;
 }
 
@@ -230,7 +233,8 @@ __device__ __forceinline__ void lsd_sort(StepSmem& S, int n, uint64_t kmin, uint
   __syncthreads();
 }
 
-// Sort the n <= CAP sheets of the bucket by (key, idx) into S.perm.
+// Sort the n <= CAP sheets of the bucket by (key, idx) into S.perm.  The
+// bins [0, binp(2^qb)] are zero on entry (cleared while the bucket loads).
 __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin,
                                             uint64_t kmax, int qb) {
   const int tid = threadIdx.x;
@@ -240,8 +244,6 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
   const int nbin = 1 << qb;
   const int per = nbin / BT;  // bins per thread in the scan (1..16)
   uint32_t* bins = S.u.bins;
-  for (int j = tid; j < binp(nbin) + 1; j += BT) bins[j] = 0;
-  __syncthreads();
   uint16_t qv[MAXI], rk[MAXI];
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
@@ -306,13 +308,12 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
   __syncthreads();
 }
 
-// Adds a run of pn sheets of total fixed-point mass P bound for bucket d to
-// the aggregates of the next layout.
-__device__ __forceinline__ void add_run(StepSmem& S, int d, u128 P, uint32_t pn, int wlen,
+// Adds the fixed-point mass P of a run of sheets bound for bucket d to the
+// aggregates of the next layout.
+__device__ __forceinline__ void add_run(StepSmem& S, int d, u128 P, int wlen,
                                         unsigned long long* mass_out) {
   const int w = d - S.win_lo;
   if (w >= 0 && w < wlen) {
-    atomicAdd(&S.dcount[w], pn);
 #pragma unroll
     for (int k = 0; k < 8; ++k) atomicAdd(&S.dmass[w][k], (uint32_t)(P >> (16 * k)) & 0xffffu);
   } else {
@@ -394,7 +395,8 @@ __device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsig
   if (lane == 0) D.bcnt[cz][b] = 0u;
   if (lane < 4) D.bmass[cz][4 * b + lane] = 0ull;
   BucketRec* recs = D.recs;
-  const unsigned inc_flag = (ep << 2) | 2u;
+  const uint64_t tag = (uint64_t)(ep & kEpochLimit) << 40;
+  constexpr uint64_t PAY = (1ull << 40) - 1;
   u128 pm = 0;
   uint32_t pc = 0;
   for (int64_t j = b - 1; j >= 0; j -= 32) {
@@ -405,11 +407,14 @@ __device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsig
     if (jj >= 0) {
       const unsigned c = cnt[jj];
       const u128 m = mass_of_limbs(mass + 4 * jj);
-      const BucketRec* r = recs + jj;
-      inc = ld_acquire_u32(&r->flag) == inc_flag;
+      const ulonglong2* r = reinterpret_cast<const ulonglong2*>(recs + jj);
+      const ulonglong2 r0 = __ldcg(r), r1 = __ldcg(r + 1);
+      inc = ((r0.x & ~PAY) == tag) && ((r0.y & ~PAY) == tag) && ((r1.x & ~PAY) == tag) &&
+            ((r1.y & ~PAY) == tag);
       if (inc) {
-        vm = (((u128)ld_cg_u64(&r->inc_hi)) << 64) | ld_cg_u64(&r->inc_lo);
-        vc = __ldcg(&r->inc_cnt);
+        vm = (u128)(r0.x & PAY) | ((u128)(r0.y & PAY) << 40) | ((u128)(r1.x & PAY) << 80) |
+             ((u128)((r1.y >> 32) & 0x7Full) << 120);
+        vc = (uint32_t)r1.y;
       } else {
         vm = m;
         vc = c;
@@ -426,12 +431,12 @@ __device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsig
     if (pmask) break;
   }
   if (lane == 0) {
-    BucketRec* me = recs + b;
     const u128 im = pm + own_m;
-    me->inc_lo = (uint64_t)im;
-    me->inc_hi = (uint64_t)(im >> 64);
-    me->inc_cnt = pc + own_c;
-    st_release_u32(&me->flag, inc_flag);
+    const uint32_t ic = pc + own_c;
+    ulonglong2* r = reinterpret_cast<ulonglong2*>(recs + b);
+    __stcg(r, make_ulonglong2(tag | ((uint64_t)im & PAY), tag | ((uint64_t)(im >> 40) & PAY)));
+    __stcg(r + 1, make_ulonglong2(tag | ((uint64_t)(im >> 80) & PAY),
+                                  tag | (((uint64_t)(im >> 120) & 0x7Full) << 32) | ic));
     const int lay = (D.lay0 + sub) & 1;
     out.task = t;
     out.sim = tk.sim;
@@ -442,6 +447,15 @@ __device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsig
     out.m = D.bm[lay];
     out.idx = D.bi[lay];
     out.n = own_c < (unsigned)CAP ? (int)own_c : CAP;
+    // the bucket is loaded after the current one: bring it into L2 now
+    const uint32_t n4 = (uint32_t)((out.n + 3) & ~3);
+    if (n4) {
+      const int64_t base = b * CAP;
+      bulk_prefetch_l2(out.x + base, n4 * 8u);
+      bulk_prefetch_l2(out.v + base, n4 * 8u);
+      bulk_prefetch_l2(out.m + base, n4 * 8u);
+      bulk_prefetch_l2(out.idx + base, n4 * 4u);
+    }
     out.pm_lo = (uint64_t)pm;
     out.pm_hi = (uint64_t)(pm >> 64);
     out.pcnt = pc;
@@ -529,6 +543,11 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       S.prefix_cnt = tm.pcnt;
       S.amp = (D.ext.kind == EXT_PULSE_TANH) ? pulse_amplitude(D.ext, D.t_seq[sub]) : 0.0;
     }
+    {
+      // counting-sort bins, cleared while the copies are in flight
+      const int nbz = binp(1 << D.sort_bits) + 1;
+      for (int j = tid; j < nbz; j += BT) S.u.bins[j] = 0u;
+    }
     if (n4 > 0) {
       if (!mbar_wait(&S.mbar, parity) && tid == 0) atomicOr(L.err, DEV_ERR_BAD_STATE);
       parity ^= 1u;
@@ -583,7 +602,11 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     const int j0 = tid * ipt;
     const int nmine = (j0 < n) ? ((n - j0) < ipt ? (n - j0) : ipt) : 0;
     u128 tot = 0;
-    for (int i = 0; i < nmine; ++i) tot += mass_to_fixed(S.m[S.perm[j0 + i]], E);
+    for (int i = 0; i < nmine; ++i) {
+      const u128 M = mass_to_fixed(S.m[S.perm[j0 + i]], E);
+      S.u.pos.mfix[j0 + i] = M;
+      tot += M;
+    }
     const u128 incl = warp_inclusive_scan_u128(tot, lane);
     uint32_t cin = (uint32_t)nmine;
 #pragma unroll
@@ -626,7 +649,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     const int64_t nbk = D.nb;
     // ---- force, kick, drift, routing; new x, v go back to their slots and
     // the destination of every sorted position to the (now free) sort area
-    int32_t* sdst = S.u.dst;
+    int32_t* sdst = S.u.pos.dst;
     const double dt = L.profile ? 0.0 : D.dt;
     const double dt_drift = LAST ? dt / 2. : dt;
     const double dest_dt = (LAST && !L.profile) ? dt / 2. : 0.0;
@@ -666,7 +689,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
           qnk[qnext] = key_of(x);
           qni[qnext] = idv[u];
         }
-        const u128 M = mass_to_fixed(S.m[sidx], E);
+        const u128 M = S.u.pos.mfix[j0 + i0 + u];
         const i128 A = T - 2 * (i128)C - (i128)M;
         C += M;
         double acc = fixed_to_double(A, E);
@@ -701,36 +724,54 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
 #pragma unroll
       for (int u = 0; u < 2; ++u)
         inw[u] = live[u] && win_ge(S, 0, kd[u], idv[u]) && !win_ge(S, wlen, kd[u], idv[u]);
+      // the largest l with key Q_l <= key, on keys alone; then splitters with
+      // an equal key and a larger index step back (pair order)
       for (int step = top; step >= 1; step >>= 1) {
 #pragma unroll
         for (int u = 0; u < 2; ++u)
-          if (l[u] + step < wlen && win_ge(S, l[u] + step, kd[u], idv[u])) l[u] += step;
+          if (l[u] + step < wlen && S.wkey[l[u] + step] <= kd[u]) l[u] += step;
       }
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+        while (l[u] > 0 && S.wkey[l[u]] == kd[u] && S.widx[l[u]] > idv[u]) --l[u];
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
         if (!live[u]) continue;
         const int d = inw[u] ? S.win_lo + l[u] : dest_bucket(S, qdk, qdi, nbk, kd[u], idv[u]);
         sdst[j0 + i0 + u] = d;
+        if (inw[u]) atomicAdd(&S.dcount[l[u]], 1u);
       }
     }
     __syncthreads();
-    // ---- aggregates of the next layout: each thread walks its sorted
-    // positions and adds every run of sheets bound for one bucket, as
-    // (count, mass), to that bucket's window entry -- or, outside the window,
-    // the mass straight to the bucket's accumulators (the count of such
-    // sheets is added when their slots are claimed below)
+    // ---- slots in the next layout: one atomic per destination bucket of the
+    // window, whose round trip overlaps the mass pass below
     const int cw = (D.cs0 + sub + 1) % kAggSlots;
     unsigned* const cnt_out = D.bcnt[cw];
     unsigned long long* const mass_out = D.bmass[cw];
-    {
+    uint32_t db = 0;
+    if (tid < wlen) {
+      const uint32_t c = S.dcount[tid];
+      if (c) db = atomicAdd(&cnt_out[S.win_lo + tid], c);
+    }
+    if (warp == 0) {
+      // the next task, prepared while the other warps sum masses
+      prepare_task(L, sub, ep, lane, S.next_ticket, S.next_tk, S.next);
+    } else {
+      // ---- masses of the next layout: each thread walks a range of sorted
+      // positions and adds every run of sheets bound for one bucket to that
+      // bucket's window entry -- or, outside the window, straight to the
+      // bucket's accumulators
+      const int ipm = (n + BT - 33) / (BT - 32);
+      const int m0 = (tid - 32) * ipm;
+      const int nm = (m0 < n) ? ((n - m0) < ipm ? (n - m0) : ipm) : 0;
       int dcur = -1;
       u128 P = 0;
       uint32_t pn = 0;
-      for (int i = 0; i < nmine; ++i) {
-        const int d = sdst[j0 + i];
-        const u128 M = mass_to_fixed(S.m[S.perm[j0 + i]], E);
+      for (int i = 0; i < nm; ++i) {
+        const int d = sdst[m0 + i];
+        const u128 M = S.u.pos.mfix[m0 + i];
         if (d != dcur) {
-          if (pn) add_run(S, dcur, P, pn, wlen, mass_out);
+          if (pn) add_run(S, dcur, P, wlen, mass_out);
           dcur = d;
           P = M;
           pn = 1;
@@ -739,47 +780,40 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
           ++pn;
         }
       }
-      // the last runs of a warp's threads usually share a bucket: one add
+      // the last runs of a warp's threads often share a bucket: one add
       const unsigned same = __match_any_sync(0xffffffffu, pn ? dcur : -1);
       if (same == 0xffffffffu && pn) {
         P = warp_sum_u128(P);
-#pragma unroll
-        for (int d = 16; d >= 1; d >>= 1) pn += __shfl_xor_sync(0xffffffffu, pn, d);
-        if (lane == 0) add_run(S, dcur, P, pn, wlen, mass_out);
+        if (lane == 0) add_run(S, dcur, P, wlen, mass_out);
       } else if (pn) {
-        add_run(S, dcur, P, pn, wlen, mass_out);
+        add_run(S, dcur, P, wlen, mass_out);
       }
     }
+    if (tid < wlen) {
+      S.dbase[tid] = db;
+      S.dcount[tid] = 0;  // reused below as the fill level of each destination
+    }
     __syncthreads();
-    for (int j = tid; j < wlen; j += BT) {
-      const uint32_t c = S.dcount[j];
-      uint32_t db = 0;
-      if (c) {
-        const int64_t d = S.win_lo + j;
-        db = atomicAdd(&cnt_out[d], c);
+    if (tid < wlen) {
+      const int64_t d = S.win_lo + tid;
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-          atomicAdd(&mass_out[4 * d + k], (unsigned long long)S.dmass[j][2 * k] +
-                                              ((unsigned long long)S.dmass[j][2 * k + 1] << 16));
+      for (int k = 0; k < 4; ++k) {
+        const unsigned long long v = (unsigned long long)S.dmass[tid][2 * k] +
+                                     ((unsigned long long)S.dmass[tid][2 * k + 1] << 16);
+        if (v) atomicAdd(&mass_out[4 * d + k], v);
       }
-      S.dbase[j] = db;
-      S.dcount[j] = 0;  // reused below as the fill level of each destination
     }
-    __syncthreads();
     bool overflow = false;
-    if (warp == 0) {
-      // the next task, prepared while the other warps write
-      prepare_task(L, sub, ep, lane, S.next_ticket, S.next_tk, S.next);
-    } else {
+    {
       // write-out in sorted order: a warp takes 32 consecutive sorted
       // positions, and the sheets among them bound for one bucket take
-      // consecutive slots there, so the stores coalesce
+      // consecutive slots there
       double* const xout = D.bx[1 - lay];
       double* const vout = D.bv[1 - lay];
       double* const mout = D.bm[1 - lay];
       int32_t* const iout = D.bi[1 - lay];
       const int nr = (n + 31) & ~31;
-      for (int p = tid - 32; p < nr; p += BT - 32) {
+      for (int p = tid; p < nr; p += BT) {
         const bool ok = p < n;
         const int d = ok ? sdst[p] : -1;
         const unsigned peers = __match_any_sync(0xffffffffu, d);

@@ -32,13 +32,20 @@ BucketTuning tuning_for(int64_t n);
 namespace wg {
 void set_tuning(const std::vector<std::pair<int64_t, BucketTuning>>& rows);
 
-// Look-back record of one bucket (32 bytes): its inclusive (mass, count)
-// prefix, valid when flag == (epoch << 2) | 2 for the sub-step's epoch.
-struct __align__(16) BucketRec {
-  uint64_t inc_lo, inc_hi;    // inclusive fixed-point mass prefix
-  uint32_t inc_cnt;           // inclusive sheet-count prefix
-  unsigned flag;
-  uint64_t pad;
+// Epochs tag the records of one sub-step; they run from 1 to kEpochLimit,
+// after which the host clears every record and starts again at 1.
+constexpr unsigned kEpochLimit = (1u << 24) - 1;
+constexpr int kMaxLeap = 1 << 22;  // sub-steps in one call
+
+// Look-back record of one bucket: its inclusive (mass, count) prefix in four
+// 64-bit words, each carrying the 24-bit epoch of the sub-step that wrote it
+// in its top bits and 40 payload bits below: mass bits [0,40), [40,80),
+// [80,120), and mass bits [120,127) << 32 | count.  Each word is stored and
+// loaded whole, so a reader that finds the current epoch in all four has the
+// complete prefix without any flag or fence; a cleared record (epoch 0) never
+// matches.
+struct __align__(32) BucketRec {
+  uint64_t w[4];
 };
 
 // Per-bucket aggregates (sheet count and fixed-point mass) rotate over three

@@ -167,6 +167,10 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// Bulk prefetch of global memory into L2 (16-byte aligned, size a multiple of 16).
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 // Wait for the phase with the given parity; false if the bounded wait expired.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
   for (unsigned it = 0; it < kSpinLimit; ++it) {

@@ -450,7 +450,7 @@ int wg_pool_remove(wg_pool* p, int sim_id) {
 
 int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nleap, double* t0,
                  double* time_elapsed) {
-  if (!p || count < 1 || !ids || !dt || nleap < 1)
+  if (!p || count < 1 || !ids || !dt || nleap < 1 || nleap > kMaxLeap)
     return pool_fail(WG_ERR_ARG, "bad arguments to wg_pool_step");
   std::vector<PoolSim*> act((size_t)count);
   int64_t ntasks = 0;
@@ -476,7 +476,7 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
     }
     if (t0) t0[k] = t;
   }
-  if (p->epoch + (unsigned)nleap + 2 > (1u << 29)) {
+  if (p->epoch + (unsigned)nleap > kEpochLimit) {
     // restart epochs: forget every look-back record
     for (PoolSim* s : p->sims)
       if (s) PC(cudaMemsetAsync(s->recs, 0, sizeof(BucketRec) * (size_t)s->nb, p->stream));
