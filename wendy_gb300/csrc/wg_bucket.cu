@@ -79,6 +79,9 @@ struct TaskMeta {
   int n;          // sheets in the bucket; -1: the simulation has aborted this call
   int lay;        // layout read by this sub-step
   uint32_t pcnt;  // sheets in the simulation's earlier buckets
+  int wlo, whi;   // splitter window [wlo, whi] of the next layout ...
+  int wbuf;       // ... in wkey[wbuf], widx[wbuf]
+  double amp;     // time factor of a pulsed external force at this sub-step
   uint64_t pm_lo, pm_hi;  // their fixed-point mass
 };
 
@@ -89,15 +92,21 @@ struct StepSmem {
   int32_t idx[CAP];
   uint16_t perm[CAP];  // sorted position -> slot
   union {
-    uint32_t bins[NBIN_PAD];
+    struct {
+      uint32_t bins[NBIN_PAD];
+      uint64_t skey[CAP];  // key and index of each position in bin order
+      int32_t sidx[CAP];
+    } srt;
     LsdSmem lsd;
     struct {
       u128 mfix[CAP];    // fixed-point mass of each sorted position
       int32_t dst[CAP];  // destination bucket of each sorted position
     } pos;
   } u;
-  uint64_t wkey[2 * RWIN + 2];
-  int32_t widx[2 * RWIN + 2];
+  // splitter windows of the next layout, double-buffered: the one of the
+  // next task is read while the current task runs
+  uint64_t wkey[2][2 * RWIN + 2];
+  int32_t widx[2][2 * RWIN + 2];
   uint32_t dcount[2 * RWIN + 2];
   uint32_t dbase[2 * RWIN + 2];
   uint32_t dmass[2 * RWIN + 2][8];  // 16-bit mass limbs sent to each window bucket, summed
@@ -110,7 +119,7 @@ struct StepSmem {
   uint32_t prefix_cnt;
   uint64_t red_min[WARPS], red_max[WARPS];
   TaskMeta next;
-  int win_lo, win_hi;
+  int win_lo, win_hi, cur_wbuf;
   double amp;
   unsigned long long maxv;
   uint64_t mbar;  // completion of the bucket's bulk copies
@@ -239,17 +248,30 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
                                             uint64_t kmax, int qb) {
   const int tid = threadIdx.x;
   const uint64_t span = kmax - kmin;
-  const int bits = span ? 64 - __clzll((long long)span) : 0;
-  const int shift = bits > qb ? bits - qb : 0;
   const int nbin = 1 << qb;
   const int per = nbin / BT;  // bins per thread in the scan (1..16)
-  uint32_t* bins = S.u.bins;
+  // Bin of a key: (key - kmin) * scale / 2^64, which is non-decreasing in the
+  // key and spreads the bucket's key range over all nbin bins (a shift would
+  // leave up to half of them empty).  The scale is a single-precision
+  // reciprocal shrunk by 2^-20, so the largest key still lands below nbin;
+  // a range narrower than nbin keys maps one key per bin.
+  const bool narrow = span < (uint64_t)nbin;
+  uint64_t scale = 0;
+  if (!narrow) {
+    const float f = (float)nbin / ((float)span + 1.0f) * 18446744073709551616.0f *
+                    (1.0f - 9.5367431640625e-07f);
+    scale = (uint64_t)f;
+  }
+  uint32_t* bins = S.u.srt.bins;
+  uint64_t* skey = S.u.srt.skey;
+  int32_t* sidx = S.u.srt.sidx;
   uint16_t qv[MAXI], rk[MAXI];
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
     const int j = tid + i * BT;
     if (i < ipt && j < n) {
-      qv[i] = (uint16_t)((key_of(S.x[j]) - kmin) >> shift);
+      const uint64_t dk = key_of(S.x[j]) - kmin;
+      qv[i] = (uint16_t)(narrow ? dk : __umul64hi(dk, scale));
       rk[i] = (uint16_t)atomicAdd(&bins[binp(qv[i])], 1u);
     }
   }
@@ -281,12 +303,18 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
     const int j = tid + i * BT;
-    if (i < ipt && j < n) S.perm[bins[binp(qv[i])] + rk[i]] = (uint16_t)j;
+    if (i < ipt && j < n) {
+      const uint32_t pos = bins[binp(qv[i])] + rk[i];
+      S.perm[pos] = (uint16_t)j;
+      skey[pos] = key_of(S.x[j]);
+      sidx[pos] = S.idx[j];
+    }
   }
   __syncthreads();
   // The order inside a bin came from atomics: sort each bin with two or more
-  // sheets by (key, idx).  The sheet that arrived second in a bin does it,
-  // so only occupied bins cost anything.
+  // sheets by (key, idx), on the keys and indices laid out in bin order.  The
+  // sheet that arrived second in a bin does it, so only occupied bins cost
+  // anything.
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
     const int j = tid + i * BT;
@@ -294,14 +322,18 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
       const uint32_t lo = bins[binp(qv[i])], hi = bins[binp(qv[i] + 1)];
       for (uint32_t a = lo + 1; a < hi; ++a) {
         const uint16_t s = S.perm[a];
-        const uint64_t ks = key_of(S.x[s]);
-        const int32_t is = S.idx[s];
+        const uint64_t ks = skey[a];
+        const int32_t is = sidx[a];
         int b = (int)a - 1;
-        while (b >= (int)lo && pair_less(ks, is, key_of(S.x[S.perm[b]]), S.idx[S.perm[b]])) {
+        while (b >= (int)lo && pair_less(ks, is, skey[b], sidx[b])) {
           S.perm[b + 1] = S.perm[b];
+          skey[b + 1] = skey[b];
+          sidx[b + 1] = sidx[b];
           --b;
         }
         S.perm[b + 1] = s;
+        skey[b + 1] = ks;
+        sidx[b + 1] = is;
       }
     }
   }
@@ -325,20 +357,20 @@ __device__ __forceinline__ void add_run(StepSmem& S, int d, u128 P, int wlen,
 
 // Bucket of the next layout covering (k, i): the largest j with Q_j <= (k, i).
 // (k, i) >= splitter j of the window (keys first; indices only on a tie)
-__device__ __forceinline__ bool win_ge(const StepSmem& S, int j, uint64_t k, int32_t i) {
-  const uint64_t K = S.wkey[j];
-  return k > K || (k == K && i >= S.widx[j]);
+__device__ __forceinline__ bool win_ge(const uint64_t* wk, const int32_t* wi, int j, uint64_t k,
+                                       int32_t i) {
+  const uint64_t K = wk[j];
+  return k > K || (k == K && i >= wi[j]);
 }
 
-__device__ __forceinline__ int dest_bucket(const StepSmem& S, const uint64_t* qk,
-                                           const int32_t* qi, int64_t nb, uint64_t k,
-                                           int32_t i) {
-  const int lo = S.win_lo, w = S.win_hi - S.win_lo;
-  if (win_ge(S, 0, k, i) && !win_ge(S, w, k, i)) {
+__device__ __forceinline__ int dest_bucket(const uint64_t* wk, const int32_t* wi, int lo, int w,
+                                           const uint64_t* qk, const int32_t* qi, int64_t nb,
+                                           uint64_t k, int32_t i) {
+  if (win_ge(wk, wi, 0, k, i) && !win_ge(wk, wi, w, k, i)) {
     int l = 0, len = w;  // Q_{lo+l} <= (k,i) < Q_{lo+l+len}
     while (len > 1) {
       const int half = len >> 1;
-      const bool ge = win_ge(S, l + half, k, i);
+      const bool ge = win_ge(wk, wi, l + half, k, i);
       l = ge ? l + half : l;
       len = ge ? len - half : half;
     }
@@ -359,103 +391,156 @@ __device__ __forceinline__ u128 mass_of_limbs(const unsigned long long* l) {
   return (u128)l[0] + ((u128)l[1] << 32) + ((u128)l[2] << 64) + ((u128)l[3] << 96);
 }
 
+// What the look-back reads of one earlier bucket.
+struct PredLoad {
+  unsigned c;          // its aggregate count ...
+  u128 m;              // ... and mass
+  ulonglong2 r0, r1;   // its look-back record
+};
+
+__device__ __forceinline__ PredLoad load_pred(const unsigned* cnt, const unsigned long long* mass,
+                                              const BucketRec* recs, int64_t jj) {
+  PredLoad p;
+  if (jj >= 0) {
+    p.c = cnt[jj];
+    p.m = mass_of_limbs(mass + 4 * jj);
+    const ulonglong2* r = reinterpret_cast<const ulonglong2*>(recs + jj);
+    p.r0 = __ldcg(r);
+    p.r1 = __ldcg(r + 1);
+  } else {
+    p.c = 0;
+    p.m = 0;
+    p.r0 = make_ulonglong2(0ull, 0ull);
+    p.r1 = p.r0;
+  }
+  return p;
+}
+
 // Prepares task t (task-list entry tk) for processing; all lanes of one warp.
 //
-// Reads the simulation's abort word, its arrays for this sub-step and the
-// bucket's aggregate, clears the bucket's aggregate slot two sub-steps on,
-// and resolves the bucket's exclusive (mass, count) prefix by looking back
-// over the earlier buckets of the simulation: a bucket whose inclusive prefix
-// is published for this sub-step ends the walk, every other one contributes
-// its aggregate.  Aggregates were completed by the previous launch, so the
-// walk never waits; the bucket then publishes its own inclusive prefix.
+// Reads the simulation's abort word, its arrays for this sub-step, the
+// bucket's aggregate and the splitter window of the next layout around the
+// bucket, clears the bucket's aggregate slot two sub-steps on, and resolves
+// the bucket's exclusive (mass, count) prefix by looking back over the
+// earlier buckets of the simulation: a bucket whose inclusive prefix is
+// published for this sub-step ends the walk, every other one contributes its
+// aggregate.  Aggregates were completed by the previous launch, so the walk
+// never waits; the bucket then publishes its own inclusive prefix.  The
+// loads of the first look-back group are issued together with all the others.
 __device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsigned ep, int lane,
-                                             unsigned t, BucketTask tk, TaskMeta& out) {
-  if (t >= (unsigned)L.ntasks) {
-    if (lane == 0) out.task = t;
-    return;
+                                             unsigned t, BucketTask tk, StepSmem& S, int wbuf) {
+  TaskMeta& out = S.next;
+  if (lane == 0) {
+    out.task = t;
+    out.wbuf = wbuf;
   }
+  if (t >= (unsigned)L.ntasks) return;
   const SimDev& D = L.sims[tk.sim];
   const int64_t b = tk.bucket;
   const int cs = (D.cs0 + sub) % kAggSlots;
-  const int cz = (cs + 2) % kAggSlots;
   const unsigned* cnt = D.bcnt[cs];
   const unsigned long long* mass = D.bmass[cs];
+  const BucketRec* recs = D.recs;
+  const int rw = D.window;
+  const int64_t nbk = D.nb;
+  const int wlo = (int)(b > rw ? b - rw : 0);
+  const int whi = (int)((b + rw + 1) < nbk ? (b + rw + 1) : nbk);
+  const int qs = (D.qsel0 + sub) & 1;
+  const uint64_t* qdk = D.qk[qs];
+  const int32_t* qdi = D.qi[qs];
+  // ---- one round of loads
   const unsigned ab = __ldcg(D.ocount + 1);
   const unsigned own_c = cnt[b];
   const u128 own_m = mass_of_limbs(mass + 4 * b);
+  constexpr int WQ = (2 * RWIN + 2 + 31) / 32;
+  uint64_t wkr[WQ];
+  int32_t wir[WQ];
+#pragma unroll
+  for (int q = 0; q < WQ; ++q) {
+    const int j = lane + 32 * q;
+    if (j <= whi - wlo) {
+      wkr[q] = qdk[wlo + j];
+      wir[q] = qdi[wlo + j];
+    }
+  }
+  int64_t j = b - 1;
+  PredLoad pl = load_pred(cnt, mass, recs, j - lane);
+  double amp = 0.0;
+  if (lane == 0 && D.ext.kind == EXT_PULSE_TANH) amp = pulse_amplitude(D.ext, D.t_seq[sub]);
   // an earlier sub-step of this call overflowed the simulation: its host
   // side finishes the call on the compact path
   if (ab != 0 && (int)ab <= sub) {
-    if (lane == 0) {
-      out.task = t;
-      out.n = -1;
-    }
+    if (lane == 0) out.n = -1;
     return;
   }
-  if (lane == 0) D.bcnt[cz][b] = 0u;
-  if (lane < 4) D.bmass[cz][4 * b + lane] = 0ull;
-  BucketRec* recs = D.recs;
+  const int n = own_c < (unsigned)CAP ? (int)own_c : CAP;
+  const int lay = (D.lay0 + sub) & 1;
+  if (lane == 0 && n > 0) {
+    // the bucket is loaded after the current one: bring it into L2 now
+    const uint32_t n4 = (uint32_t)((n + 3) & ~3);
+    const int64_t base = b * CAP;
+    bulk_prefetch_l2(D.bx[lay] + base, n4 * 8u);
+    bulk_prefetch_l2(D.bv[lay] + base, n4 * 8u);
+    bulk_prefetch_l2(D.bm[lay] + base, n4 * 8u);
+    bulk_prefetch_l2(D.bi[lay] + base, n4 * 4u);
+  }
+#pragma unroll
+  for (int q = 0; q < WQ; ++q) {
+    const int jw = lane + 32 * q;
+    if (jw <= whi - wlo) {
+      S.wkey[wbuf][jw] = wkr[q];
+      S.widx[wbuf][jw] = wir[q];
+    }
+  }
+  {
+    const int cz = (cs + 2) % kAggSlots;
+    if (lane == 0) D.bcnt[cz][b] = 0u;
+    if (lane < 4) D.bmass[cz][4 * b + lane] = 0ull;
+  }
+  // ---- look-back
   const uint64_t tag = (uint64_t)(ep & kEpochLimit) << 40;
   constexpr uint64_t PAY = (1ull << 40) - 1;
   u128 pm = 0;
   uint32_t pc = 0;
-  for (int64_t j = b - 1; j >= 0; j -= 32) {
-    const int64_t jj = j - lane;
-    bool inc = false;
-    u128 vm = 0;
-    uint32_t vc = 0;
-    if (jj >= 0) {
-      const unsigned c = cnt[jj];
-      const u128 m = mass_of_limbs(mass + 4 * jj);
-      const ulonglong2* r = reinterpret_cast<const ulonglong2*>(recs + jj);
-      const ulonglong2 r0 = __ldcg(r), r1 = __ldcg(r + 1);
-      inc = ((r0.x & ~PAY) == tag) && ((r0.y & ~PAY) == tag) && ((r1.x & ~PAY) == tag) &&
-            ((r1.y & ~PAY) == tag);
-      if (inc) {
-        vm = (u128)(r0.x & PAY) | ((u128)(r0.y & PAY) << 40) | ((u128)(r1.x & PAY) << 80) |
-             ((u128)((r1.y >> 32) & 0x7Full) << 120);
-        vc = (uint32_t)r1.y;
-      } else {
-        vm = m;
-        vc = c;
-      }
-    }
+  while (j >= 0) {
+    const bool inc = (j - lane >= 0) && ((pl.r0.x & ~PAY) == tag) &&
+                     ((pl.r0.y & ~PAY) == tag) && ((pl.r1.x & ~PAY) == tag) &&
+                     ((pl.r1.y & ~PAY) == tag);
+    const u128 vm = inc ? ((u128)(pl.r0.x & PAY) | ((u128)(pl.r0.y & PAY) << 40) |
+                           ((u128)(pl.r1.x & PAY) << 80) |
+                           ((u128)((pl.r1.y >> 32) & 0x7Full) << 120))
+                        : pl.m;
+    const uint32_t vcl = inc ? (uint32_t)pl.r1.y : pl.c;
     const unsigned pmask = __ballot_sync(0xffffffffu, inc);
     const int stop = pmask ? (__ffs(pmask) - 1) : 31;
     const bool take = lane <= stop;
     pm += warp_sum_u128(take ? vm : (u128)0);
-    uint32_t c = take ? vc : 0u;
+    uint32_t c = take ? vcl : 0u;
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
     pc += c;
     if (pmask) break;
+    j -= 32;
+    if (j >= 0) pl = load_pred(cnt, mass, recs, j - lane);
   }
   if (lane == 0) {
     const u128 im = pm + own_m;
     const uint32_t ic = pc + own_c;
-    ulonglong2* r = reinterpret_cast<ulonglong2*>(recs + b);
+    ulonglong2* r = reinterpret_cast<ulonglong2*>(D.recs + b);
     __stcg(r, make_ulonglong2(tag | ((uint64_t)im & PAY), tag | ((uint64_t)(im >> 40) & PAY)));
     __stcg(r + 1, make_ulonglong2(tag | ((uint64_t)(im >> 80) & PAY),
                                   tag | (((uint64_t)(im >> 120) & 0x7Full) << 32) | ic));
-    const int lay = (D.lay0 + sub) & 1;
-    out.task = t;
     out.sim = tk.sim;
+    out.wlo = wlo;
+    out.whi = whi;
     out.bucket = b;
     out.lay = lay;
     out.x = D.bx[lay];
     out.v = D.bv[lay];
     out.m = D.bm[lay];
     out.idx = D.bi[lay];
-    out.n = own_c < (unsigned)CAP ? (int)own_c : CAP;
-    // the bucket is loaded after the current one: bring it into L2 now
-    const uint32_t n4 = (uint32_t)((out.n + 3) & ~3);
-    if (n4) {
-      const int64_t base = b * CAP;
-      bulk_prefetch_l2(out.x + base, n4 * 8u);
-      bulk_prefetch_l2(out.v + base, n4 * 8u);
-      bulk_prefetch_l2(out.m + base, n4 * 8u);
-      bulk_prefetch_l2(out.idx + base, n4 * 4u);
-    }
+    out.n = n;
+    out.amp = amp;
     out.pm_lo = (uint64_t)pm;
     out.pm_hi = (uint64_t)(pm >> 64);
     out.pcnt = pc;
@@ -464,13 +549,13 @@ __device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsig
 
 // Claims a ticket and prepares its task; all lanes of one warp.
 __device__ __forceinline__ void claim_task(const StepLaunch& L, int sub, unsigned ep, int lane,
-                                           TaskMeta& out) {
+                                           StepSmem& S, int wbuf) {
   unsigned t = 0;
   if (lane == 0) t = atomicAdd(L.ticket, 1u);
   t = __shfl_sync(0xffffffffu, t, 0);
   BucketTask tk{0, 0};
   if (t < (unsigned)L.ntasks) tk = L.tasks[t];
-  prepare_task(L, sub, ep, lane, t, tk, out);
+  prepare_task(L, sub, ep, lane, t, tk, S, wbuf);
 }
 
 // The fused sub-step.  LAST: the call's last sub-step (half drift, outputs).
@@ -485,7 +570,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     mbar_init(&S.mbar, 1);
     fence_proxy_async_smem();
   }
-  if (warp == 0) claim_task(L, sub, ep, lane, S.next);
+  if (warp == 0) claim_task(L, sub, ep, lane, S, 0);
   unsigned parity = 0;
   for (;;) {
     __syncthreads();
@@ -493,7 +578,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     if (tm.task >= (unsigned)L.ntasks) break;
     if (tm.n < 0) {
       __syncthreads();  // every thread has read S.next
-      if (warp == 0) claim_task(L, sub, ep, lane, S.next);
+      if (warp == 0) claim_task(L, sub, ep, lane, S, tm.wbuf);
       continue;
     }
     const SimDev& D = L.sims[tm.sim];
@@ -517,36 +602,30 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     // and the task is prepared by warp 0 during the write-out
     unsigned nt = 0;
     if (tid == 0) nt = atomicAdd(L.ticket, 1u);
-    const int qs = (D.qsel0 + sub) & 1;
-    const uint64_t* qdk = D.qk[qs];
-    const int32_t* qdi = D.qi[qs];
     const int ipt = (n + BT - 1) / BT;
     const double pre = sub == 0 ? D.pre_dt : 0.0;
     const int E = D.E;
-    // splitter window of the next layout around this bucket, fetched while
-    // the bulk copies are in flight
-    const int rw = D.window;
-    const int wlo = (int)(b > rw ? b - rw : 0);
-    const int whi = (int)((b + rw + 1) < D.nb ? (b + rw + 1) : D.nb);
-    for (int j = tid; j <= whi - wlo; j += BT) {
-      S.wkey[j] = qdk[wlo + j];
-      S.widx[j] = qdi[wlo + j];
+    // the splitter window of the next layout around this bucket arrived with
+    // the task; the per-destination counters are cleared here
+    const uint64_t* const wk = S.wkey[tm.wbuf];
+    const int32_t* const wi = S.widx[tm.wbuf];
+    for (int j = tid; j <= tm.whi - tm.wlo; j += BT) {
       S.dcount[j] = 0;
 #pragma unroll
       for (int k = 0; k < 8; ++k) S.dmass[j][k] = 0u;
     }
     if (tid == 0) {
-      S.win_lo = wlo;
-      S.win_hi = whi;
+      S.win_lo = tm.wlo;
+      S.win_hi = tm.whi;
+      S.cur_wbuf = tm.wbuf;
       S.maxv = 0;
       S.prefix_mass = (((u128)tm.pm_hi) << 64) | tm.pm_lo;
       S.prefix_cnt = tm.pcnt;
-      S.amp = (D.ext.kind == EXT_PULSE_TANH) ? pulse_amplitude(D.ext, D.t_seq[sub]) : 0.0;
+      S.amp = tm.amp;
     }
     {
       // counting-sort bins, cleared while the copies are in flight
-      const int nbz = binp(1 << D.sort_bits) + 1;
-      for (int j = tid; j < nbz; j += BT) S.u.bins[j] = 0u;
+      for (int j = tid; j < NBIN_PAD; j += BT) S.u.srt.bins[j] = 0u;
     }
     if (n4 > 0) {
       if (!mbar_wait(&S.mbar, parity) && tid == 0) atomicOr(L.err, DEV_ERR_BAD_STATE);
@@ -632,8 +711,8 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     rank0 += cin - (uint32_t)nmine;
 
     // ---- splitters of the layout after next: keys at global ranks j*T
-    uint64_t* qnk = D.qk[1 - qs];
-    int32_t* qni = D.qi[1 - qs];
+    uint64_t* qnk = D.qk[1 - ((D.qsel0 + sub) & 1)];
+    int32_t* qni = D.qi[1 - ((D.qsel0 + sub) & 1)];
     if (b == 0 && tid == 0) {
       qnk[0] = 0ull;
       qni[0] = (int32_t)0x80000000;
@@ -723,21 +802,23 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       bool inw[2];
 #pragma unroll
       for (int u = 0; u < 2; ++u)
-        inw[u] = live[u] && win_ge(S, 0, kd[u], idv[u]) && !win_ge(S, wlen, kd[u], idv[u]);
+        inw[u] = live[u] && win_ge(wk, wi, 0, kd[u], idv[u]) && !win_ge(wk, wi, wlen, kd[u], idv[u]);
       // the largest l with key Q_l <= key, on keys alone; then splitters with
       // an equal key and a larger index step back (pair order)
       for (int step = top; step >= 1; step >>= 1) {
 #pragma unroll
         for (int u = 0; u < 2; ++u)
-          if (l[u] + step < wlen && S.wkey[l[u] + step] <= kd[u]) l[u] += step;
+          if (l[u] + step < wlen && wk[l[u] + step] <= kd[u]) l[u] += step;
       }
 #pragma unroll
       for (int u = 0; u < 2; ++u)
-        while (l[u] > 0 && S.wkey[l[u]] == kd[u] && S.widx[l[u]] > idv[u]) --l[u];
+        while (l[u] > 0 && wk[l[u]] == kd[u] && wi[l[u]] > idv[u]) --l[u];
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
         if (!live[u]) continue;
-        const int d = inw[u] ? S.win_lo + l[u] : dest_bucket(S, qdk, qdi, nbk, kd[u], idv[u]);
+        const int d = inw[u] ? S.win_lo + l[u]
+                             : dest_bucket(wk, wi, S.win_lo, wlen, D.qk[(D.qsel0 + sub) & 1],
+                                           D.qi[(D.qsel0 + sub) & 1], nbk, kd[u], idv[u]);
         sdst[j0 + i0 + u] = d;
         if (inw[u]) atomicAdd(&S.dcount[l[u]], 1u);
       }
@@ -755,7 +836,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     }
     if (warp == 0) {
       // the next task, prepared while the other warps sum masses
-      prepare_task(L, sub, ep, lane, S.next_ticket, S.next_tk, S.next);
+      prepare_task(L, sub, ep, lane, S.next_ticket, S.next_tk, S, S.cur_wbuf ^ 1);
     } else {
       // ---- masses of the next layout: each thread walks a range of sorted
       // positions and adds every run of sheets bound for one bucket to that
