@@ -75,3 +75,38 @@ def test_exact_solver_is_not_offered():
     g = wendy_gb300.nbody(numpy.array([-1., 1.]), numpy.zeros(2), numpy.ones(2), 2)
     with pytest.raises(NotImplementedError):
         next(g)
+
+
+def test_tuning_table_rows_select_by_size():
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("CUDA library not built here")
+    from wendy_gb300 import autotune
+    saved = [dict(n_min=0, **autotune.current(0))]
+    try:
+        rows = [dict(n_min=0, target=512, window=32, sort_bits=11, ctas_per_sm=2),
+                dict(n_min=1 << 16, target=1024, window=64, sort_bits=12, ctas_per_sm=2)]
+        autotune.apply(rows)
+        assert autotune.current(1000)["target"] == 512
+        assert autotune.current((1 << 16) - 1)["window"] == 32
+        assert autotune.current(1 << 16)["target"] == 1024
+        assert autotune.current(1 << 30)["sort_bits"] == 12
+        for bad in (dict(n_min=0, target=4096, window=64, sort_bits=12, ctas_per_sm=2),
+                    dict(n_min=0, target=1024, window=65, sort_bits=12, ctas_per_sm=2),
+                    dict(n_min=0, target=1024, window=64, sort_bits=13, ctas_per_sm=2),
+                    dict(n_min=0, target=1024, window=64, sort_bits=12, ctas_per_sm=3)):
+            with pytest.raises(_lib.WendyGPUError):
+                autotune.apply([bad])
+    finally:
+        autotune.apply(autotune.load_table() or saved)
+
+
+def test_shipped_tuning_table_is_valid():
+    from wendy_gb300 import autotune
+    rows = autotune.load_table()
+    if rows is None:
+        pytest.skip("no shipped table")
+    assert rows[0]["n_min"] == 0
+    assert all(a["n_min"] <= b["n_min"] for a, b in zip(rows, rows[1:]))
+    for r in rows:
+        assert 64 <= r["target"] <= 1536 and 1 <= r["window"] <= 64
+        assert 8 <= r["sort_bits"] <= 12 and r["ctas_per_sm"] in (1, 2)

@@ -5,14 +5,18 @@ number of sheets of a simulation (how many buckets there are to keep the SMs
 busy, how far sheets travel in bucket units, how clustered the keys inside a
 bucket are):
 
-  target       sheets per bucket right after a re-sort (bucket capacity is 2048)
+  target       sheets per bucket right after a re-sort (capacity 2048, at most 1536)
   window       splitters searched in shared memory on each side of a bucket
   sort_bits    2^sort_bits bins of the in-bucket counting sort
   ctas_per_sm  persistent CTAs per SM
 
-:func:`tune` times candidate settings on seeded sech^2 disks of a few sizes
-(a real output interval each, CUDA-event device time through ``wg_step``) by
-coordinate descent from the defaults, and returns a table of rows
+:func:`tune` times candidate settings by coordinate descent from the
+defaults, for a few simulation sizes n.  Each timing advances a pool of
+identical seeded sech^2 disks of n sheets, as many as make about 2^23 sheets
+in all (a single simulation from that size up), by real output intervals
+(CUDA-event device time through ``wg_pool_step``): the objective is the
+throughput of a full GPU, which is what both a large simulation and an
+ensemble of small ones need.  It returns a table of rows
 ``(n_min, target, window, sort_bits, ctas_per_sm)``; :func:`apply` installs
 a table in the library (``wg_set_tuning``), which uses the row with the
 largest ``n_min <= n`` for every simulation created afterwards.  A table
@@ -30,8 +34,8 @@ from . import _lib
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE_PATH = os.path.join(HERE, "tuning_gb300.json")
-DEFAULT = dict(target=1024, window=64, sort_bits=12, ctas_per_sm=2)
-SPACE = dict(target=(256, 512, 768, 1024), window=(16, 32, 64), sort_bits=(10, 11, 12),
+DEFAULT = dict(target=1536, window=64, sort_bits=12, ctas_per_sm=2)
+SPACE = dict(target=(768, 1024, 1280, 1536), window=(16, 32, 64), sort_bits=(11, 12),
              ctas_per_sm=(1, 2))
 
 
@@ -70,22 +74,25 @@ def apply_shipped():
     return rows
 
 
-def _time(n, setting, nleap=10, outputs=2, seed=0):
+def _time(n, setting, nleap=10, outputs=2, seed=0, total=1 << 23):
+    """Device seconds per sub-step of a pool of max(1, total // n) simulations of n sheets."""
+    from .ensemble import Pool
     from .ics import sech2_disk
-    from .wendy import Simulation
     apply([dict(n_min=0, **setting)])
     x, v, m = sech2_disk(n, seed=seed, masses="lognormal")
-    sim = Simulation(x, v, m, numpy.sum(m), 1.21)
-    t = ctypes.c_double(0.)
-    sim.step(0.001, nleap, t)
-    el = 0.0
-    for _ in range(outputs):
-        el += sim.step(0.001, nleap, t)
-    sim.close()
+    pool = Pool()
+    try:
+        ids = [pool.add(x, v, m, omega=1.1) for _ in range(max(1, total // n))]
+        pool.step(ids, 0.001, nleap)
+        el = 0.0
+        for _ in range(outputs):
+            el += pool.step(ids, 0.001, nleap)
+    finally:
+        pool.close()
     return el / (outputs * nleap)
 
 
-def tune(sizes=(1 << 12, 1 << 16, 1 << 20, 1 << 24), rounds=2, verbose=False):
+def tune(sizes=(1 << 11, 1 << 14, 1 << 17, 1 << 20, 1 << 24), rounds=2, verbose=False):
     """Coordinate descent over SPACE for each size; returns the table rows."""
     rows = []
     for n in sizes:

@@ -16,11 +16,12 @@ constexpr int kBucketThreads = 256;
 constexpr int kBucketCap = 2048;      // sheets a bucket can hold
 constexpr int kSplitterWindow = 64;   // largest splitter window (buckets on each side)
 constexpr int kSortBitsMax = 12;      // largest counting-sort offset (bits)
+constexpr int kMaxTarget = kBucketCap * 3 / 4;  // largest bucket target
 
 // Tunables of the fused sub-step, chosen per simulation size by the
 // autotuner (wendy_gb300/autotune.py) or left at their defaults.
 struct BucketTuning {
-  int target = 1024;      // sheets per bucket right after a re-sort (<= kBucketCap / 2)
+  int target = 1536;      // sheets per bucket right after a re-sort (<= kMaxTarget)
   int window = 64;        // splitters searched in shared memory on each side
   int sort_bits = 12;     // counting-sort bins = 2^sort_bits (8..12)
   int ctas_per_sm = 2;    // persistent CTAs per SM (1 or 2)
