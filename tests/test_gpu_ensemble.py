@@ -100,3 +100,29 @@ def test_budget_is_enforced():
             pool.add(x, v, m)
         assert e.value.status == -6
         assert pool.info()["sims"] == 1
+
+
+def _converging(n, seed):
+    # every sheet reaches the origin within one sub-step: the bucket layout
+    # overflows and the call finishes on a full re-sort
+    rng = numpy.random.default_rng(seed)
+    x = rng.uniform(-1, 1, size=n)
+    return x, -x / 0.01 * 0.999, numpy.full(n, 1.0 / n)
+
+
+def test_members_overflowing_in_one_call_recover_independently():
+    # two members overflow in the same call, a third does not; each must
+    # still equal the oracle (the recoveries share the pool's workspace)
+    cases = [_converging(50000, 7), _converging(30001, 8), ics.sech2_disk(20000, seed=9)]
+    pool = Pool()
+    ids = [pool.add(x, v, m) for (x, v, m) in cases]
+    gens = [O.nbody_approx(x, v, m, 0.05, 5) for (x, v, m) in cases]
+    t0 = numpy.zeros(len(ids))
+    for _ in range(2):
+        pool.step(ids, 0.01, 5, t0)
+        for sid, g, (x, _, _) in zip(ids, gens, cases):
+            gx, gv = pool.download(sid)
+            rx, rv = next(g)
+            assert numpy.max(numpy.abs(gx - rx)) <= 1e-9
+            assert numpy.max(numpy.abs(gv - rv)) <= 1e-9
+    pool.close()

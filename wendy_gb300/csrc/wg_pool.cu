@@ -645,6 +645,10 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
       f.a_out = nullptr;
       const int64_t tiles = (s->n + kForceTile - 1) / kForceTile;
       PC(cudaMemsetAsync(p->tickets, 0, 4 * (size_t)nleap, p->stream));
+      // the tile records are shared by every simulation recovered in this
+      // call, under the same epochs: clear them so that no tile takes
+      // another simulation's prefix
+      PC(cudaMemsetAsync(p->trecs, 0, sizeof(TileRec) * (size_t)tiles, p->stream));
       for (int i = kk + 1; i < nleap; ++i) {
         const StepFlags one{1u, 0u, 0ull};
         PC(cudaMemcpyAsync(&p->wflags[i], &one, sizeof(one), cudaMemcpyHostToDevice, p->stream));

@@ -353,8 +353,12 @@ void radix_sort_state(StateTable* table, int64_t n, RadixWork* w, const StepFlag
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     attr_set = true;
   }
+  // the workspace may be bound for more sheets than this sort has: tiles,
+  // look-back words and launches follow n
+  const int64_t tiles = (n + kRadixTile - 1) / kRadixTile;
   cudaMemsetAsync(w->hist, 0, 8 * R * 4, s);
-  cudaMemsetAsync(w->status, 0, w->scratch_bytes, s);
+  cudaMemsetAsync(w->status, 0, (size_t)8 * tiles * R * 4, s);
+  cudaMemsetAsync(w->counters, 0, 16 * 4, s);
   int hist_grid = (int)((n + 255) / 256);
   if (hist_grid > 152 * 8) hist_grid = 152 * 8;
   if (hist_grid < 1) hist_grid = 1;
@@ -363,7 +367,7 @@ void radix_sort_state(StateTable* table, int64_t n, RadixWork* w, const StepFlag
   PassArgs a;
   a.table = table;
   a.n = n;
-  a.n_tiles = w->n_tiles;
+  a.n_tiles = tiles;
   a.keys0 = w->keys[0];
   a.keys1 = w->keys[1];
   a.pos0 = w->pos[0];
@@ -376,7 +380,7 @@ void radix_sort_state(StateTable* table, int64_t n, RadixWork* w, const StepFlag
   for (int p = 0; p < 8; ++p) {
     a.pass = p;
     k_radix_pass<kRadixThreads, kRadixItems>
-        <<<(unsigned)w->n_tiles, kRadixThreads, dyn, s>>>(a);
+        <<<(unsigned)tiles, kRadixThreads, dyn, s>>>(a);
   }
   int g = (int)((n + 255) / 256);
   if (g > 152 * 16) g = 152 * 16;
