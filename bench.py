@@ -194,6 +194,9 @@ def run_serve(args, w):
     print(json.dumps(line))
 
 HBM_FALLBACK_GBS = 6800.0
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_bucket_step launch at
+# N = 2^23 (237.5 MB + 184.6 MB), per sheet
+TRAFFIC_PER_SHEET = (237.515776e6 + 184.6016e6) / (1 << 23)
 
 
 def peaks():
@@ -412,9 +415,16 @@ def main():
                                     "achieved_gbs": 40.0 * n / f_s / 1e9},
              "radix_resort": {"ms": s_s * 1e3, "algorithmic_bytes_per_sheet": 250,
                               "achieved_gbs": 250.0 * n / s_s / 1e9}}
+    # DRAM bytes (read + write) of one k_bucket_step launch from an ncu capture
+    # of one sub-step at N = 2^23, scaled by the sheets of this workload: the
+    # traffic grows in proportion to the sheets
+    traffic = TRAFFIC_PER_SHEET * n
     roof = {"bound": "hbm", "kernel": "k_bucket_step", "achieved": bucket_gbs, "peak": hbm,
             "unit": "GB/s", "frac": bucket_gbs / hbm, "peak_kind": hbm_kind,
-            "traffic": None, "components": comps, "substep_ms": sub_s * 1e3,
+            "traffic": traffic, "traffic_unit": "bytes per launch",
+            "traffic_source": "ncu capture at N = 2^23, scaled to N",
+            "algorithmic_bytes_per_launch": 56.0 * n,
+            "components": comps, "substep_ms": sub_s * 1e3,
             "stats": {k: st1[k] - st0[k] for k in ("sorts_full", "sorts_window", "substeps")}}
     sim.close()
 

@@ -80,7 +80,9 @@ int wg_create(int64_t n, const double *x, const double *v, const double *m, doub
    (dt here is the reference's dt_leap = dt_output / nleap).  *t0 is updated
    exactly as the reference does (repeated += dt, only with an external
    force); *time_elapsed receives the device time of the call in seconds.
+   nleap is limited to WG_MAX_LEAP sub-steps per call (WG_ERR_ARG beyond).
    Reference: _wendy_nbody_approx_onestep, wendy/wendy.c:385-418. */
+#define WG_MAX_LEAP 4194304
 int wg_step(wg_sim *s, double dt, int nleap, double *t0, double *time_elapsed);
 
 /* Copy positions and velocities back in original particle order.

@@ -208,6 +208,11 @@ def test_bad_inputs_raise():
         wendy_gb300.Simulation(numpy.zeros(3), numpy.zeros(3), numpy.array([1., -1., 1.]), 1.)
     with pytest.raises(_lib.WendyGPUError):
         wendy_gb300.Simulation(numpy.array([0., numpy.nan, 1.]), numpy.zeros(3), numpy.ones(3), 3.)
+    import ctypes
+    sim = wendy_gb300.Simulation(numpy.array([-1., 0., 1.]), numpy.zeros(3), numpy.ones(3), 3.)
+    with pytest.raises(_lib.WendyGPUError):
+        sim.step(0.01, (1 << 22) + 1, ctypes.c_double(0.))  # above WG_MAX_LEAP sub-steps
+    sim.close()
 
 
 def test_large_n_trajectory_matches_oracle():

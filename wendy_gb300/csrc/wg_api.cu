@@ -413,6 +413,8 @@ int finish_call(wg_sim* s, int nleap, bool count_sorts = true) {
   return WG_OK;
 }
 
+static_assert(kMaxLeap == WG_MAX_LEAP, "sub-step limit of the C header");
+
 // Epochs of the next `count` sub-steps into s->h_ep.  They stay within
 // [1, kEpochLimit]: before passing it every look-back record is cleared and
 // the epochs restart at 1.

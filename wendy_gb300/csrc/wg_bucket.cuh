@@ -36,7 +36,7 @@ void set_tuning(const std::vector<std::pair<int64_t, BucketTuning>>& rows);
 // Epochs tag the records of one sub-step; they run from 1 to kEpochLimit,
 // after which the host clears every record and starts again at 1.
 constexpr unsigned kEpochLimit = (1u << 24) - 1;
-constexpr int kMaxLeap = 1 << 22;  // sub-steps in one call
+constexpr int kMaxLeap = 1 << 22;  // sub-steps in one call (WG_MAX_LEAP)
 
 // Look-back record of one bucket: its inclusive (mass, count) prefix in four
 // 64-bit words, each carrying the 24-bit epoch of the sub-step that wrote it
