@@ -92,7 +92,7 @@ def test_tuning_table_rows_select_by_size():
         assert autotune.current(1 << 30)["sort_bits"] == 12
         for bad in (dict(n_min=0, target=4096, window=64, sort_bits=12, ctas_per_sm=2),
                     dict(n_min=0, target=1024, window=65, sort_bits=12, ctas_per_sm=2),
-                    dict(n_min=0, target=1024, window=64, sort_bits=13, ctas_per_sm=2),
+                    dict(n_min=0, target=1024, window=64, sort_bits=14, ctas_per_sm=2),
                     dict(n_min=0, target=1024, window=64, sort_bits=12, ctas_per_sm=3)):
             with pytest.raises(_lib.WendyGPUError):
                 autotune.apply([bad])
@@ -109,4 +109,4 @@ def test_shipped_tuning_table_is_valid():
     assert all(a["n_min"] <= b["n_min"] for a, b in zip(rows, rows[1:]))
     for r in rows:
         assert 64 <= r["target"] <= 1536 and 1 <= r["window"] <= 64
-        assert 8 <= r["sort_bits"] <= 12 and r["ctas_per_sm"] in (1, 2)
+        assert 9 <= r["sort_bits"] <= 13 and r["ctas_per_sm"] in (1, 2)

@@ -35,7 +35,7 @@ from . import _lib
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE_PATH = os.path.join(HERE, "tuning_gb300.json")
 DEFAULT = dict(target=1536, window=64, sort_bits=12, ctas_per_sm=2)
-SPACE = dict(target=(768, 1024, 1280, 1536), window=(16, 32, 64), sort_bits=(11, 12),
+SPACE = dict(target=(768, 1024, 1280, 1536), window=(16, 32, 64), sort_bits=(11, 12, 13),
              ctas_per_sm=(1, 2))
 
 

@@ -909,11 +909,11 @@ int wg_set_tuning(const wg_tuning* rows, int nrows) {
   for (int i = 0; i < nrows; ++i) {
     const wg_tuning& r = rows[i];
     if (r.target < 64 || r.target > kMaxTarget || r.window < 1 ||
-        r.window > kSplitterWindow || r.sort_bits < 8 || r.sort_bits > kSortBitsMax ||
+        r.window > kSplitterWindow || r.sort_bits < kSortBitsMin || r.sort_bits > kSortBitsMax ||
         r.ctas_per_sm < 1 || r.ctas_per_sm > 2 || (i > 0 && r.n_min < rows[i - 1].n_min)) {
-      set_error("tuning row %d out of range (target 64..%d, window 1..%d, sort_bits 8..%d, "
+      set_error("tuning row %d out of range (target 64..%d, window 1..%d, sort_bits %d..%d, "
                 "ctas_per_sm 1..2, n_min ascending)", i, kMaxTarget, kSplitterWindow,
-                kSortBitsMax);
+                kSortBitsMin, kSortBitsMax);
       return WG_ERR_ARG;
     }
     BucketTuning b;

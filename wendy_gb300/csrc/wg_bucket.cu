@@ -53,10 +53,17 @@ constexpr int WARPS = BT / 32;
 constexpr int RWIN = kSplitterWindow;
 constexpr int NBIN = 1 << kSortBitsMax;  // bins the shared memory is sized for
 constexpr int MAXBIN = 48;          // a fuller bin sends the bucket to the radix sort
-// Bins are padded with one word per 32 so that a thread scanning 16
-// consecutive bins and its 31 neighbours hit 32 different banks.
-constexpr int NBIN_PAD = NBIN + NBIN / 32 + 1;
-__device__ __forceinline__ int binp(int b) { return b + (b >> 5); }
+// Two 16-bit bin counters (later offsets) per 32-bit word: bin b lives in the
+// half (b & 1) of word b / 2.  Words are padded with one per 32 so that a
+// thread scanning 16 consecutive words and its 31 neighbours hit 32
+// different banks.
+constexpr int NWORD = NBIN / 2;
+constexpr int NBIN_PAD = NWORD + NWORD / 32 + 1;
+__device__ __forceinline__ int binp(int w) { return w + (w >> 5); }
+// Offset (or count) of bin b in the packed words.
+__device__ __forceinline__ uint32_t bin_get(const uint32_t* bins, int b) {
+  return (bins[binp(b >> 1)] >> ((b & 1) << 4)) & 0xffffu;
+}
 
 struct LsdSmem {
   uint32_t q[2][CAP];
@@ -99,17 +106,20 @@ struct StepSmem {
     } srt;
     LsdSmem lsd;
     struct {
-      u128 mfix[CAP];    // fixed-point mass of each sorted position
-      int32_t dst[CAP];  // destination bucket of each sorted position
+      u128 mfix[CAP];      // fixed-point mass of each sorted position
+      uint16_t drk[CAP];   // rank of each sorted position among the sheets of its destination
+      uint16_t order[CAP]; // sorted positions grouped by destination
+      uint8_t dw[CAP];     // destination of each sorted position: window entry, or the
+                           // window length for a bucket outside the window
     } pos;
   } u;
   // splitter windows of the next layout, double-buffered: the one of the
   // next task is read while the current task runs
   uint64_t wkey[2][2 * RWIN + 2];
   int32_t widx[2][2 * RWIN + 2];
-  uint32_t dcount[2 * RWIN + 2];
-  uint32_t dbase[2 * RWIN + 2];
-  uint32_t dmass[2 * RWIN + 2][8];  // 16-bit mass limbs sent to each window bucket, summed
+  uint32_t dcount[2 * RWIN + 2];  // sheets bound for each window entry (+ outside the window)
+  uint32_t dstart[2 * RWIN + 3];  // their exclusive prefix: segments of the grouped order
+  uint32_t dbase[2 * RWIN + 2];   // first slot of each window bucket taken by this bucket
   unsigned next_ticket;              // the next task's ticket and entry, read ahead
   BucketTask next_tk;
   u128 warp_mass[WARPS];
@@ -154,6 +164,12 @@ __device__ __forceinline__ uint32_t block_excl_scan(StepSmem& S, uint32_t v, uin
     total += t;
   }
   return pre + incl - v;
+}
+
+// Barrier of warps 1 .. WARPS-1 only (named barrier 1): warp 0 meanwhile
+// prepares the next task.
+__device__ __forceinline__ void bar_sync_workers() {
+  asm volatile("bar.sync 1, %0;" ::"n"(BT - 32) : "memory");
 }
 
 // Multi-pass fallback: stable LSD radix sort of 32-bit order-preserving
@@ -242,14 +258,15 @@ __device__ __forceinline__ void lsd_sort(StepSmem& S, int n, uint64_t kmin, uint
   __syncthreads();
 }
 
-// Sort the n <= CAP sheets of the bucket by (key, idx) into S.perm.  The
-// bins [0, binp(2^qb)] are zero on entry (cleared while the bucket loads).
+// Sort the n <= CAP sheets of the bucket by (key, idx) into S.perm, with
+// 2^qb bins (9 <= qb <= 13).  The bin words are zero on entry (cleared while
+// the bucket loads).
 __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_t kmin,
                                             uint64_t kmax, int qb) {
   const int tid = threadIdx.x;
   const uint64_t span = kmax - kmin;
   const int nbin = 1 << qb;
-  const int per = nbin / BT;  // bins per thread in the scan (1..16)
+  const int wpt = nbin / (2 * BT);  // bin words per thread in the scan (1..16)
   // Bin of a key: (key - kmin) * scale / 2^64, which is non-decreasing in the
   // key and spreads the bucket's key range over all nbin bins (a shift would
   // leave up to half of them empty).  The scale is a single-precision
@@ -272,19 +289,22 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
     if (i < ipt && j < n) {
       const uint64_t dk = key_of(S.x[j]) - kmin;
       qv[i] = (uint16_t)(narrow ? dk : __umul64hi(dk, scale));
-      rk[i] = (uint16_t)atomicAdd(&bins[binp(qv[i])], 1u);
+      const int sh = (qv[i] & 1) << 4;
+      rk[i] = (uint16_t)(atomicAdd(&bins[binp(qv[i] >> 1)], 1u << sh) >> sh);
     }
   }
   __syncthreads();
-  // exclusive scan of the bins: thread t owns bins [16 t, 16 t + 16)
-  constexpr int PERMAX = NBIN / BT;
-  uint32_t c[PERMAX];
+  // exclusive scan of the bins: thread t owns words [wpt t, wpt t + wpt)
+  constexpr int WMAX = NWORD / BT;
+  uint32_t c[WMAX];
   uint32_t run = 0, mx = 0;
 #pragma unroll
-  for (int k = 0; k < PERMAX; ++k) {
-    c[k] = k < per ? bins[binp(tid * per + k)] : 0u;
-    mx = c[k] > mx ? c[k] : mx;
-    run += c[k];
+  for (int k = 0; k < WMAX; ++k) {
+    c[k] = k < wpt ? bins[binp(tid * wpt + k)] : 0u;
+    const uint32_t lo = c[k] & 0xffffu, hi = c[k] >> 16;
+    mx = lo > mx ? lo : mx;
+    mx = hi > mx ? hi : mx;
+    run += lo + hi;
   }
   const int too_full = __syncthreads_or(mx > (uint32_t)MAXBIN);
   if (too_full) {
@@ -294,17 +314,18 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
   uint32_t total;
   uint32_t off = block_excl_scan(S, run, total);
 #pragma unroll
-  for (int k = 0; k < PERMAX; ++k) {
-    if (k < per) bins[binp(tid * per + k)] = off;
-    off += c[k];
+  for (int k = 0; k < WMAX; ++k) {
+    const uint32_t lo = c[k] & 0xffffu, hi = c[k] >> 16;
+    if (k < wpt) bins[binp(tid * wpt + k)] = off | ((off + lo) << 16);
+    off += lo + hi;
   }
-  if (tid == 0) bins[binp(nbin)] = (uint32_t)n;
+  if (tid == 0) bins[binp(nbin >> 1)] = (uint32_t)n;  // offset of bin nbin
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
     const int j = tid + i * BT;
     if (i < ipt && j < n) {
-      const uint32_t pos = bins[binp(qv[i])] + rk[i];
+      const uint32_t pos = bin_get(bins, qv[i]) + rk[i];
       S.perm[pos] = (uint16_t)j;
       skey[pos] = key_of(S.x[j]);
       sidx[pos] = S.idx[j];
@@ -319,7 +340,7 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
   for (int i = 0; i < MAXI; ++i) {
     const int j = tid + i * BT;
     if (i < ipt && j < n && rk[i] == 1) {
-      const uint32_t lo = bins[binp(qv[i])], hi = bins[binp(qv[i] + 1)];
+      const uint32_t lo = bin_get(bins, qv[i]), hi = bin_get(bins, qv[i] + 1);
       for (uint32_t a = lo + 1; a < hi; ++a) {
         const uint16_t s = S.perm[a];
         const uint64_t ks = skey[a];
@@ -338,21 +359,6 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
     }
   }
   __syncthreads();
-}
-
-// Adds the fixed-point mass P of a run of sheets bound for bucket d to the
-// aggregates of the next layout.
-__device__ __forceinline__ void add_run(StepSmem& S, int d, u128 P, int wlen,
-                                        unsigned long long* mass_out) {
-  const int w = d - S.win_lo;
-  if (w >= 0 && w < wlen) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) atomicAdd(&S.dmass[w][k], (uint32_t)(P >> (16 * k)) & 0xffffu);
-  } else {
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      atomicAdd(&mass_out[4 * (int64_t)d + k], (unsigned long long)(uint32_t)(P >> (32 * k)));
-  }
 }
 
 // Bucket of the next layout covering (k, i): the largest j with Q_j <= (k, i).
@@ -609,11 +615,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     // the task; the per-destination counters are cleared here
     const uint64_t* const wk = S.wkey[tm.wbuf];
     const int32_t* const wi = S.widx[tm.wbuf];
-    for (int j = tid; j <= tm.whi - tm.wlo; j += BT) {
-      S.dcount[j] = 0;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) S.dmass[j][k] = 0u;
-    }
+    for (int j = tid; j <= tm.whi - tm.wlo; j += BT) S.dcount[j] = 0;  // wlen + 1 entries
     if (tid == 0) {
       S.win_lo = tm.wlo;
       S.win_hi = tm.whi;
@@ -728,7 +730,6 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     const int64_t nbk = D.nb;
     // ---- force, kick, drift, routing; new x, v go back to their slots and
     // the destination of every sorted position to the (now free) sort area
-    int32_t* sdst = S.u.pos.dst;
     const double dt = L.profile ? 0.0 : D.dt;
     const double dt_drift = LAST ? dt / 2. : dt;
     const double dest_dt = (LAST && !L.profile) ? dt / 2. : 0.0;
@@ -816,111 +817,129 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
         if (!live[u]) continue;
-        const int d = inw[u] ? S.win_lo + l[u]
-                             : dest_bucket(wk, wi, S.win_lo, wlen, D.qk[(D.qsel0 + sub) & 1],
-                                           D.qi[(D.qsel0 + sub) & 1], nbk, kd[u], idv[u]);
-        sdst[j0 + i0 + u] = d;
-        if (inw[u]) atomicAdd(&S.dcount[l[u]], 1u);
+        // destination: window entry l, or wlen for a bucket outside the
+        // window (found again, by a global search, where it is needed)
+        const int w = inw[u] ? l[u] : wlen;
+        const int pq = j0 + i0 + u;
+        S.u.pos.dw[pq] = (uint8_t)w;
+        S.u.pos.drk[pq] = (uint16_t)atomicAdd(&S.dcount[w], 1u);
       }
     }
     __syncthreads();
-    // ---- slots in the next layout: one atomic per destination bucket of the
-    // window, whose round trip overlaps the mass pass below
+    // ---- the sheets grouped by destination bucket of the next layout.  Warp 0
+    // prepares the next task meanwhile; the other warps synchronise among
+    // themselves (named barrier 1) until the block-wide barrier below.
     const int cw = (D.cs0 + sub + 1) % kAggSlots;
     unsigned* const cnt_out = D.bcnt[cw];
     unsigned long long* const mass_out = D.bmass[cw];
+    const uint64_t* const qfar = D.qk[(D.qsel0 + sub) & 1];
+    const int32_t* const ifar = D.qi[(D.qsel0 + sub) & 1];
     uint32_t db = 0;
-    if (tid < wlen) {
-      const uint32_t c = S.dcount[tid];
-      if (c) db = atomicAdd(&cnt_out[S.win_lo + tid], c);
-    }
     if (warp == 0) {
-      // the next task, prepared while the other warps sum masses
       prepare_task(L, sub, ep, lane, S.next_ticket, S.next_tk, S, S.cur_wbuf ^ 1);
     } else {
-      // ---- masses of the next layout: each thread walks a range of sorted
-      // positions and adds every run of sheets bound for one bucket to that
-      // bucket's window entry -- or, outside the window, straight to the
-      // bucket's accumulators
-      const int ipm = (n + BT - 33) / (BT - 32);
-      const int m0 = (tid - 32) * ipm;
-      const int nm = (m0 < n) ? ((n - m0) < ipm ? (n - m0) : ipm) : 0;
-      int dcur = -1;
-      u128 P = 0;
-      uint32_t pn = 0;
-      for (int i = 0; i < nm; ++i) {
-        const int d = sdst[m0 + i];
-        const u128 M = S.u.pos.mfix[m0 + i];
-        if (d != dcur) {
-          if (pn) add_run(S, dcur, P, wlen, mass_out);
-          dcur = d;
-          P = M;
-          pn = 1;
-        } else {
-          P += M;
-          ++pn;
+      const int wt = tid - 32;  // 0 .. BT - 33
+      // slots: one atomic per window bucket, its round trip overlapping the
+      // grouping and the mass sums
+      if (wt < wlen) {
+        const uint32_t c = S.dcount[wt];
+        if (c) db = atomicAdd(&cnt_out[S.win_lo + wt], c);
+      }
+      if (warp == 1) {
+        // segments: exclusive prefix of the counts of the wlen + 1 entries
+        constexpr int E5 = (2 * RWIN + 2 + 31) / 32;
+        uint32_t cv[E5];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < E5; ++k) {
+          const int j = lane * E5 + k;
+          cv[k] = j <= wlen ? S.dcount[j] : 0u;
+          sum += cv[k];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        uint32_t ex = incl - sum;
+#pragma unroll
+        for (int k = 0; k < E5; ++k) {
+          const int j = lane * E5 + k;
+          if (j <= wlen) S.dstart[j] = ex;
+          ex += cv[k];
+        }
+        if (lane == 31) S.dstart[wlen + 1] = incl;
+      }
+      bar_sync_workers();
+      for (int pq = wt; pq < n; pq += BT - 32)
+        S.u.pos.order[S.dstart[S.u.pos.dw[pq]] + S.u.pos.drk[pq]] = (uint16_t)pq;
+      bar_sync_workers();
+      // ---- masses of the next layout: a warp sums the fixed-point masses of
+      // a window bucket's segment and adds them to that bucket's accumulators
+      for (int w = warp - 1; w < wlen; w += WARPS - 1) {
+        const int q0 = (int)S.dstart[w], q1 = (int)S.dstart[w + 1];
+        if (q0 == q1) continue;
+        u128 P = 0;
+        for (int q = q0 + lane; q < q1; q += 32) P += S.u.pos.mfix[S.u.pos.order[q]];
+        P = warp_sum_u128(P);
+        if (lane < 4) {
+          const unsigned long long limb = (unsigned long long)(uint32_t)(P >> (32 * lane));
+          if (limb) atomicAdd(&mass_out[4 * (int64_t)(S.win_lo + w) + lane], limb);
         }
       }
-      // the last runs of a warp's threads often share a bucket: one add
-      const unsigned same = __match_any_sync(0xffffffffu, pn ? dcur : -1);
-      if (same == 0xffffffffu && pn) {
-        P = warp_sum_u128(P);
-        if (lane == 0) add_run(S, dcur, P, wlen, mass_out);
-      } else if (pn) {
-        add_run(S, dcur, P, wlen, mass_out);
+      // sheets bound outside the window: one by one
+      for (int q = (int)S.dstart[wlen] + wt; q < n; q += BT - 32) {
+        const int pq = S.u.pos.order[q];
+        const int sl = S.perm[pq];
+        const double xn = S.x[sl];
+        const uint64_t kf = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, S.v[sl], xn) : xn);
+        const int d = dest_bucket(wk, wi, S.win_lo, wlen, qfar, ifar, nbk, kf, S.idx[sl]);
+        const u128 M = S.u.pos.mfix[pq];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const unsigned long long limb = (unsigned long long)(uint32_t)(M >> (32 * k));
+          if (limb) atomicAdd(&mass_out[4 * (int64_t)d + k], limb);
+        }
       }
-    }
-    if (tid < wlen) {
-      S.dbase[tid] = db;
-      S.dcount[tid] = 0;  // reused below as the fill level of each destination
+      if (wt < wlen) S.dbase[wt] = db;
     }
     __syncthreads();
-    if (tid < wlen) {
-      const int64_t d = S.win_lo + tid;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const unsigned long long v = (unsigned long long)S.dmass[tid][2 * k] +
-                                     ((unsigned long long)S.dmass[tid][2 * k + 1] << 16);
-        if (v) atomicAdd(&mass_out[4 * d + k], v);
-      }
-    }
     bool overflow = false;
     {
-      // write-out in sorted order: a warp takes 32 consecutive sorted
-      // positions, and the sheets among them bound for one bucket take
-      // consecutive slots there
+      // write-out grouped by destination: consecutive positions of a segment
+      // take consecutive slots, so a warp's stores coalesce
       double* const xout = D.bx[1 - lay];
       double* const vout = D.bv[1 - lay];
       double* const mout = D.bm[1 - lay];
       int32_t* const iout = D.bi[1 - lay];
-      const int nr = (n + 31) & ~31;
-      for (int p = tid; p < nr; p += BT) {
-        const bool ok = p < n;
-        const int d = ok ? sdst[p] : -1;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const int leader = __ffs(peers) - 1;
-        uint32_t first = 0;
-        if (ok && lane == leader) {
-          const int w = d - S.win_lo;
-          first = (w >= 0 && w < wlen) ? S.dbase[w] + atomicAdd(&S.dcount[w], __popc(peers))
-                                       : atomicAdd(&cnt_out[d], __popc(peers));
+      for (int q = tid; q < n; q += BT) {
+        const int pq = S.u.pos.order[q];
+        const int w = S.u.pos.dw[pq];
+        const int sl = S.perm[pq];
+        int d;
+        uint32_t slot;
+        if (w < wlen) {
+          d = S.win_lo + w;
+          slot = S.dbase[w] + (uint32_t)q - S.dstart[w];
+        } else {
+          const double xn = S.x[sl];
+          const uint64_t kf = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, S.v[sl], xn) : xn);
+          d = dest_bucket(wk, wi, S.win_lo, wlen, qfar, ifar, nbk, kf, S.idx[sl]);
+          slot = atomicAdd(&cnt_out[d], 1u);
         }
-        first = __shfl_sync(0xffffffffu, first, leader);
-        if (!ok) continue;
-        const uint32_t slot = first + __popc(peers & lanemask_lt());
-        const int s = S.perm[p];
         if (slot < (uint32_t)CAP) {
           const int64_t o = (int64_t)d * CAP + slot;
-          xout[o] = S.x[s];
-          vout[o] = S.v[s];
-          mout[o] = S.m[s];
-          iout[o] = S.idx[s];
+          xout[o] = S.x[sl];
+          vout[o] = S.v[sl];
+          mout[o] = S.m[sl];
+          iout[o] = S.idx[sl];
         } else {
           const uint32_t o = atomicAdd(D.ocount, 1u);
-          D.ox[o] = S.x[s];
-          D.ov[o] = S.v[s];
-          D.om[o] = S.m[s];
-          D.oi[o] = S.idx[s];
+          D.ox[o] = S.x[sl];
+          D.ov[o] = S.v[sl];
+          D.om[o] = S.m[sl];
+          D.oi[o] = S.idx[sl];
           overflow = true;
         }
       }

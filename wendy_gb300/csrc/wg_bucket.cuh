@@ -15,7 +15,8 @@ namespace wg {
 constexpr int kBucketThreads = 256;
 constexpr int kBucketCap = 2048;      // sheets a bucket can hold
 constexpr int kSplitterWindow = 64;   // largest splitter window (buckets on each side)
-constexpr int kSortBitsMax = 12;      // largest counting-sort offset (bits)
+constexpr int kSortBitsMin = 9;       // smallest counting-sort offset (bits)
+constexpr int kSortBitsMax = 13;      // largest counting-sort offset (bits)
 constexpr int kMaxTarget = kBucketCap * 3 / 4;  // largest bucket target
 
 // Tunables of the fused sub-step, chosen per simulation size by the
@@ -23,7 +24,7 @@ constexpr int kMaxTarget = kBucketCap * 3 / 4;  // largest bucket target
 struct BucketTuning {
   int target = 1536;      // sheets per bucket right after a re-sort (<= kMaxTarget)
   int window = 64;        // splitters searched in shared memory on each side
-  int sort_bits = 12;     // counting-sort bins = 2^sort_bits (8..12)
+  int sort_bits = 12;     // counting-sort bins = 2^sort_bits (9..13)
   int ctas_per_sm = 2;    // persistent CTAs per SM (1 or 2)
 };
 BucketTuning tuning_for(int64_t n);
@@ -92,7 +93,7 @@ struct SimDev {
   int64_t nb;
   int target;            // sheets per bucket at a re-sort (splitters at ranks j * target)
   int window;            // splitter window half-width (<= kSplitterWindow)
-  int sort_bits;         // counting-sort offset bits (8..12)
+  int sort_bits;         // counting-sort offset bits (9..13)
   int pad0;
   uint64_t T_lo, T_hi;   // totmass in fixed point
   int E;
