@@ -332,29 +332,21 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
     }
   }
   __syncthreads();
-  // The order inside a bin came from atomics: sort each bin with two or more
-  // sheets by (key, idx), on the keys and indices laid out in bin order.  The
-  // sheet that arrived second in a bin does it, so only occupied bins cost
-  // anything.
+  // The order inside a bin came from atomics: every sheet of a bin with two
+  // or more counts the sheets of its bin that precede it in (key, idx) order,
+  // on the keys and indices laid out in bin order, and takes that place.
+  // Only perm is written here, each place by exactly one sheet.
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
     const int j = tid + i * BT;
-    if (i < ipt && j < n && rk[i] == 1) {
+    if (i < ipt && j < n) {
       const uint32_t lo = bin_get(bins, qv[i]), hi = bin_get(bins, qv[i] + 1);
-      for (uint32_t a = lo + 1; a < hi; ++a) {
-        const uint16_t s = S.perm[a];
-        const uint64_t ks = skey[a];
-        const int32_t is = sidx[a];
-        int b = (int)a - 1;
-        while (b >= (int)lo && pair_less(ks, is, skey[b], sidx[b])) {
-          S.perm[b + 1] = S.perm[b];
-          skey[b + 1] = skey[b];
-          sidx[b + 1] = sidx[b];
-          --b;
-        }
-        S.perm[b + 1] = s;
-        skey[b + 1] = ks;
-        sidx[b + 1] = is;
+      if (hi - lo > 1) {
+        const uint64_t kj = skey[lo + rk[i]];
+        const int32_t ij = sidx[lo + rk[i]];
+        uint32_t r = 0;
+        for (uint32_t b = lo; b < hi; ++b) r += pair_less(skey[b], sidx[b], kj, ij) ? 1u : 0u;
+        S.perm[lo + r] = (uint16_t)j;
       }
     }
   }
