@@ -390,6 +390,22 @@ def main():
         for _ in range(args.steps):
             elapsed += sim.step(dt_leap, nleap, t0)
     st1 = sim.stats()
+    # energy / momentum of the last output: on the device (wg_energy) and with
+    # the reference's formula on the host, outside the timed region
+    diag = None
+    if rank == 0 and not args.no_cpu_baseline and ext is None:
+        from wendy_gb300 import diagnostics
+        gx, gv = numpy.empty(n), numpy.empty(n)
+        sim.download(gx, gv)
+        tq = time.perf_counter()
+        e_dev, p_dev = sim.energy(omega=w["omega"])
+        t_dev = time.perf_counter() - tq
+        tq = time.perf_counter()
+        e_host = diagnostics.energy(gx, gv, m, omega=w["omega"])
+        t_host = time.perf_counter() - tq
+        diag = {"device_energy_s": t_dev, "host_energy_s": t_host, "energy": e_dev,
+                "energy_rel_diff_vs_host": abs(e_dev - e_host) / abs(e_host),
+                "momentum": p_dev, "host": "numpy, reference formula (argsort + cumsum)"}
     units = n * nleap * args.steps
     if world > 1:
         elapsed, units = replica_reduce(elapsed, units)
@@ -471,6 +487,7 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "resident state larger than L2; no flush"},
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                "diagnostics": diag,
                 "gpu_launches": launches}
         print(json.dumps(line))
     if world > 1:

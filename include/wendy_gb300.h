@@ -90,6 +90,15 @@ int wg_step(wg_sim *s, double dt, int nleap, double *t0, double *time_elapsed);
    of wendy/wendy.py:434-437. */
 int wg_download(wg_sim *s, double *x, double *v);
 
+/* Total energy and momentum of the simulation's current state (the last
+   output), computed on the device: sorted order, one self-gravity force
+   evaluation, and sums in a fixed order.  twopiG and omega2 (< 0: no
+   harmonic term) have the meaning of the reference's energy(); the masses
+   the simulation holds are already times twopiG.  The potential term uses
+   sum_{x_j<x_i} m_i m_j (x_i - x_j) = -sum_i m_i x_i a_i / twopiG.  Leaves the
+   simulation compact (the next wg_step re-sorts once).
+   Reference: energy and momentum, wendy/wendy.py:439-491. */
+int wg_energy(wg_sim *s, double twopiG, double omega2, double *energy, double *momentum);
 int wg_get_stats(wg_sim *s, wg_stats *out);
 int wg_destroy(wg_sim *s);
 

@@ -136,6 +136,7 @@ struct wg_sim {
   unsigned* ocount = nullptr;
   unsigned* abort_word = nullptr;
   unsigned* offs = nullptr;
+  double* diag = nullptr;        // energy / momentum sums and their block partials
   int mode = 0;          // 0: compact sorted sets (half drift pending), 1: buckets
   int lay = 0;           // layout holding the sheets in bucket mode
   int qsel = 0;          // splitter array defining the next layout
@@ -292,7 +293,8 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
                       kAggSlots * (al(4 * (size_t)nb) + al(32 * (size_t)nb)) +
                       2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
                       al(sizeof(BucketRec) * (size_t)nb) + 3 * nd + ni + al(64) +
-                      al(4 * (size_t)nb) + al(sizeof(SimDev)) + al(sizeof(BucketTask) * (size_t)nb);
+                      al(4 * (size_t)nb) + al(sizeof(SimDev)) + al(sizeof(BucketTask) * (size_t)nb) +
+                      al(8 * 4 * (size_t)(kEnergyBlocks + 1));
   e = cudaMalloc(&s->bk, bk_b);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -326,6 +328,7 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
   s->offs = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)nb);
   s->d_dev = reinterpret_cast<SimDev*>(p); p += al(sizeof(SimDev));
   s->d_tasks = reinterpret_cast<BucketTask*>(p); p += al(sizeof(BucketTask) * (size_t)nb);
+  s->diag = reinterpret_cast<double*>(p); p += al(8 * 4 * (size_t)(kEnergyBlocks + 1));
   {
     std::vector<BucketTask> tasks((size_t)nb);
     for (int64_t b = 0; b < nb; ++b) tasks[(size_t)b] = BucketTask{0, (int)b};
@@ -952,6 +955,42 @@ int wg_host_register(void* ptr, int64_t bytes) {
 
 int wg_host_unregister(void* ptr) {
   WG_CUDA(cudaHostUnregister(ptr));
+  return WG_OK;
+}
+
+int wg_energy(wg_sim* s, double twopiG, double omega2, double* energy, double* momentum) {
+  if (!s || !(twopiG > 0.0) || !std::isfinite(twopiG) || !std::isfinite(omega2)) {
+    set_error("wg_energy needs a simulation, a positive finite twopiG and a finite omega2");
+    return WG_ERR_ARG;
+  }
+  // the current state in sorted order: the bucket layout (if any) goes back
+  // to the compact sets, which the next wg_step re-sorts and re-buckets
+  if (s->mode == 1) {
+    bucket_to_compact(s, s->lay, s->cslot);
+    s->mode = 0;
+  }
+  int rc = alloc_call_arrays(s, 1);
+  if (rc) return rc;
+  s->h_t[0] = 0.0;
+  // one self-gravity force evaluation (no harmonic or external term), dt = 0
+  const double om = s->omega2;
+  const ExtForce ext = s->ext;
+  s->omega2 = -1.0;
+  s->ext.kind = EXT_NONE;
+  rc = enqueue_step(s, 0.0, 1, true, 0.0);
+  s->omega2 = om;
+  s->ext = ext;
+  if (rc) return rc;
+  launch_energy(s->table, s->n, s->a_sorted, s->diag, s->stream);
+  s->st.launches += 3 + kRadixLaunches;
+  double sums[4];
+  WG_CUDA(cudaMemcpyAsync(sums, s->diag, sizeof(sums), cudaMemcpyDeviceToHost, s->stream));
+  rc = finish_call(s, 0, false);  // synchronises and checks the device error word
+  if (rc) return rc;
+  // masses on the device are m twopiG (wendy/wendy.py:373)
+  const double e = sums[0] + (omega2 >= 0.0 ? omega2 * sums[1] : 0.0) + sums[2];
+  if (energy) *energy = e / twopiG;
+  if (momentum) *momentum = sums[3] / twopiG;
   return WG_OK;
 }
 

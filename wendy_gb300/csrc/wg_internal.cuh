@@ -89,6 +89,12 @@ void launch_desort(const StateTable* table, int64_t n, double* x_out, double* v_
 void launch_scatter_accel(const StateTable* table, int64_t n, const double* a_sorted,
                           double* a_orig, cudaStream_t s);
 void launch_init_state(StateTable* table, int64_t n, cudaStream_t s);
+// Energy / momentum sums of the sorted state (deterministic): scratch[0..3]
+// receives sum m v^2/2, sum m x^2/2, -sum m x a, sum m v; scratch holds
+// 4 (kEnergyBlocks + 1) doubles.
+constexpr int kEnergyBlocks = 152 * 4;
+void launch_energy(const StateTable* table, int64_t n, const double* a_sorted, double* scratch,
+                   cudaStream_t s);
 
 // Record a message for wg_last_error() (wg_api.cu).
 void record_last_error(const char* msg);

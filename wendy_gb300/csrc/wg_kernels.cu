@@ -321,6 +321,58 @@ void launch_scatter_accel(const StateTable* table, int64_t n, const double* a_so
   k_scatter_accel<<<grid_for(n, 256), 256, 0, s>>>(table, n, a_sorted, a_orig);
 }
 
+// Sums of the energy and momentum diagnostics over the sorted state, with
+// the self-gravity accelerations a_sorted of that state:
+//   part[0] = sum m v^2 / 2, part[1] = sum m x^2 / 2, part[2] = -sum m x a,
+//   part[3] = sum m v.
+// The pair sum of the reference's potential energy (wendy/wendy.py:467-475),
+// sum_{x_j < x_i} m_i m_j (x_i - x_j), equals -sum_i m_i x_i a_i / 2piG for
+// a_i = M - 2 C_i - m_i.  Each block writes its partial sums; the final
+// kernel adds the partials in block order, so the result is deterministic.
+constexpr int kEnergyThreads = 256;
+__global__ void k_energy_partial(const StateTable* table, int64_t n, const double* a_sorted,
+                                 double* part) {
+  __shared__ double red[4][kEnergyThreads / 32];
+  const StateRef st = table->cur;
+  double k = 0.0, h = 0.0, w = 0.0, p = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double m = st.m[i], x = st.x[i], v = st.v[i];
+    k += m * v * v / 2.0;
+    h += m * x * x / 2.0;
+    w -= m * x * a_sorted[i];
+    p += m * v;
+  }
+  double val[4] = {k, h, w, p};
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1) val[q] += __shfl_down_sync(0xffffffffu, val[q], d);
+    if (lane == 0) red[q][warp] = val[q];
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double t = 0.0;
+    for (int j = 0; j < kEnergyThreads / 32; ++j) t += red[threadIdx.x][j];
+    part[4 * blockIdx.x + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_energy_final(const double* part, int nblocks, double* out) {
+  if (threadIdx.x < 4) {
+    double t = 0.0;
+    for (int j = 0; j < nblocks; ++j) t += part[4 * j + threadIdx.x];
+    out[threadIdx.x] = t;
+  }
+}
+
+void launch_energy(const StateTable* table, int64_t n, const double* a_sorted, double* scratch,
+                   cudaStream_t s) {
+  k_energy_partial<<<kEnergyBlocks, kEnergyThreads, 0, s>>>(table, n, a_sorted, scratch + 4);
+  k_energy_final<<<1, 32, 0, s>>>(scratch + 4, kEnergyBlocks, scratch);
+}
+
 void launch_init_state(StateTable* table, int64_t n, cudaStream_t s) {
   k_iota<<<grid_for(n, 256), 256, 0, s>>>(table, n);
 }

@@ -48,6 +48,20 @@ class Simulation:
                                    ctypes.byref(elapsed)), "wg_step")
         return elapsed.value
 
+    def energy(self, twopiG=1., omega=None):
+        """Total energy and momentum of the last output, computed on the device.
+
+        Same quantities as wendy.energy(x, v, m, twopiG, omega=omega) and
+        wendy.momentum(v, m) (wendy/wendy.py:439-491) for the masses m this
+        simulation was created with divided by twopiG; returns (energy,
+        momentum).  Leaves the sheets compact: the next step re-sorts once.
+        """
+        e, p = ctypes.c_double(0.), ctypes.c_double(0.)
+        omega2 = -1. if omega is None else float(omega) ** 2.
+        _lib.check(self._L.wg_energy(self._h, float(twopiG), omega2, ctypes.byref(e),
+                                     ctypes.byref(p)), "wg_energy")
+        return e.value, p.value
+
     def download(self, x, v):
         for arr in (x, v):
             if not (arr.flags.c_contiguous and arr.flags.writeable and arr.dtype == numpy.float64
