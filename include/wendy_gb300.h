@@ -85,6 +85,17 @@ int wg_create(int64_t n, const double *x, const double *v, const double *m, doub
 #define WG_MAX_LEAP 4194304
 int wg_step(wg_sim *s, double dt, int nleap, double *t0, double *time_elapsed);
 
+/* wg_step in two halves: wg_step_begin enqueues the output interval on the
+   simulation's stream and returns at once (*t0 is advanced immediately);
+   wg_step_end waits for it, completes it (a sub-step that overflowed a
+   bucket is finished on the full re-sort path here) and reports its device
+   time.  Between the two, every other entry on the simulation except
+   wg_destroy returns WG_ERR_ARG.  Lets a caller overlap its own work on the
+   previous output with the device computing the next one.
+   Reference: _wendy_nbody_approx_onestep, wendy/wendy.c:385-418. */
+int wg_step_begin(wg_sim *s, double dt, int nleap, double *t0);
+int wg_step_end(wg_sim *s, double *time_elapsed);
+
 /* Copy positions and velocities back in original particle order.
    Reference: the de-sort at wendy/wendy.c:413-415 and the in-place yield
    of wendy/wendy.py:434-437. */

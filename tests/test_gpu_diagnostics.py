@@ -1,8 +1,11 @@
-"""Device energy and momentum (wg_energy) against the reference's formulas.
+"""Output-side entries: device energy and momentum (wg_energy) against the
+reference's formulas, and the split step (wg_step_begin / wg_step_end) the
+generator uses to compute the next output while the caller holds this one.
 
-The reference computes both on the host from the yielded arrays
-(wendy/wendy.py:439-491); wendy_gb300.diagnostics restates them in numpy with
-the same operation order.  The device sums differ only in summation order.
+The reference computes energy and momentum on the host from the yielded
+arrays (wendy/wendy.py:439-491); wendy_gb300.diagnostics restates them in
+numpy with the same operation order.  The device sums differ only in
+summation order.
 """
 import ctypes
 
@@ -63,4 +66,48 @@ def test_energy_of_a_fresh_simulation_and_bad_arguments():
     assert abs(e - diagnostics.energy(x, v, m)) <= 1e-12 * abs(e)
     with pytest.raises(wendy_gb300._lib.WendyGPUError):
         sim.energy(twopiG=0.)
+    sim.close()
+
+
+def test_step_begin_end_equals_step_and_guards_the_handle():
+    n = 20000
+    x, v, m = ics.sech2_disk(n, seed=6, masses="lognormal")
+    a = wendy_gb300.Simulation(x, v, m, float(numpy.sum(m)), 1.21)
+    b = wendy_gb300.Simulation(x, v, m, float(numpy.sum(m)), 1.21)
+    ta, tb = ctypes.c_double(1.0), ctypes.c_double(1.0)
+    for _ in range(3):
+        a.step(0.002, 5, ta)
+        b.step_begin(0.002, 5, tb)
+        # every other entry refuses a handle with a step in flight
+        with pytest.raises(wendy_gb300._lib.WendyGPUError):
+            b.download(numpy.empty(n), numpy.empty(n))
+        with pytest.raises(wendy_gb300._lib.WendyGPUError):
+            b.step(0.002, 5, tb)
+        with pytest.raises(wendy_gb300._lib.WendyGPUError):
+            b.energy()
+        assert b.step_end() > 0.0
+    with pytest.raises(wendy_gb300._lib.WendyGPUError):
+        b.step_end()
+    assert ta.value == tb.value
+    ax, av, bx, bv = (numpy.empty(n) for _ in range(4))
+    a.download(ax, av)
+    b.download(bx, bv)
+    assert numpy.array_equal(ax, bx) and numpy.array_equal(av, bv)
+    b.step_begin(0.002, 5, tb)
+    b.close()  # destroying a handle with a step in flight waits for it
+    a.close()
+
+
+def test_generator_computes_ahead_and_stops_cleanly():
+    x, v, m = ics.sech2_disk(50000, seed=7)
+    g = wendy_gb300.nbody(x, v, m, 0.01, approx=True, nleap=5)
+    outs = [tuple(a.copy() for a in next(g)) for _ in range(3)]
+    g.close()
+    sim = wendy_gb300.Simulation(x, v, m, float(numpy.sum(m)))
+    t = ctypes.c_double(0.)
+    for ox, ov in outs:
+        sim.step(0.002, 5, t)
+        gx, gv = numpy.empty(len(x)), numpy.empty(len(x))
+        sim.download(gx, gv)
+        assert numpy.array_equal(gx, ox) and numpy.array_equal(gv, ov)
     sim.close()

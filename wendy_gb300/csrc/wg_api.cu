@@ -119,6 +119,11 @@ struct wg_sim {
   double* h_t = nullptr;         // pinned host mirrors
   unsigned* h_ep = nullptr;
   StepFlags* h_flags = nullptr;
+  unsigned* h_ab = nullptr;      // page-locked copy of the overflow count and abort word
+  // a call enqueued by wg_step_begin and not yet completed by wg_step_end
+  bool pend_active = false;
+  double pend_dt = 0;
+  int pend_nleap = 0, pend_lay0 = 0, pend_cs0 = 0;
   // bucketed layout (the fast path of wg_step)
   void* bk = nullptr;
   int64_t nb = 0;
@@ -196,6 +201,7 @@ int alloc_call_arrays(wg_sim* s, int nleap) {
   WG_CUDA(cudaMallocHost(&s->h_t, 8 * (size_t)cap));
   WG_CUDA(cudaMallocHost(&s->h_ep, 4 * (size_t)cap));
   WG_CUDA(cudaMallocHost(&s->h_flags, sizeof(StepFlags) * (cap + 1)));
+  if (!s->h_ab) WG_CUDA(cudaMallocHost(&s->h_ab, 64));
   WG_CUDA(cudaStreamSynchronize(s->stream));
   s->cap = cap;
   return WG_OK;
@@ -211,6 +217,7 @@ void free_sim(wg_sim* s) {
   if (s->h_t) cudaFreeHost(s->h_t);
   if (s->h_ep) cudaFreeHost(s->h_ep);
   if (s->h_flags) cudaFreeHost(s->h_flags);
+  if (s->h_ab) cudaFreeHost(s->h_ab);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -658,8 +665,9 @@ int wg_create(int64_t n, const double* x, const double* v, const double* m, doub
   return WG_OK;
 }
 
-static int run_call(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed,
-                    bool record_start) {
+// Enqueue one output interval on the simulation's stream (returns without
+// waiting); run_call_end completes it.
+static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool record_start) {
   int rc = alloc_call_arrays(s, nleap);
   if (rc) return rc;
   fill_times(s, dt, nleap, t0);
@@ -699,9 +707,28 @@ static int run_call(wg_sim* s, double dt, int nleap, double* t0, double* time_el
   s->cslot = (cs0 + nleap) % kAggSlots;
   s->st.launches += nleap;
   WG_CUDA(cudaGetLastError());
-  unsigned ab[2] = {0, 0};
-  WG_CUDA(cudaMemcpyAsync(ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
+  s->pend_active = true;
+  s->pend_dt = dt;
+  s->pend_nleap = nleap;
+  s->pend_lay0 = lay0;
+  s->pend_cs0 = cs0;
+  return WG_OK;
+}
+
+// Wait for the enqueued call, finish it on the compact path if a sub-step
+// overflowed a bucket, and report its device time.
+static int run_call_end(wg_sim* s, double* time_elapsed) {
+  if (!s->pend_active) {
+    set_error("no step in flight");
+    return WG_ERR_ARG;
+  }
+  s->pend_active = false;
+  const double dt = s->pend_dt;
+  const int nleap = s->pend_nleap, lay0 = s->pend_lay0, cs0 = s->pend_cs0;
   WG_CUDA(cudaStreamSynchronize(s->stream));
+  const unsigned ab[2] = {s->h_ab[0], s->h_ab[1]};
+  int rc = WG_OK;
   s->out_valid = true;
   s->mode = 1;
   s->pending_dt = dt;
@@ -768,11 +795,30 @@ static int run_call(wg_sim* s, double dt, int nleap, double* t0, double* time_el
   return rc;
 }
 
-int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
+static int run_call(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed,
+                    bool record_start) {
+  const int rc = run_call_begin(s, dt, nleap, t0, record_start);
+  if (rc) return rc;
+  return run_call_end(s, time_elapsed);
+}
+
+// Entries other than wg_step_end and wg_destroy refuse a simulation with a
+// step in flight.
+static int check_idle(wg_sim* s) {
   if (!s) {
     set_error("null simulation");
     return WG_ERR_ARG;
   }
+  if (s->pend_active) {
+    set_error("a step is in flight: call wg_step_end first");
+    return WG_ERR_ARG;
+  }
+  return WG_OK;
+}
+
+int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
+  int rc = check_idle(s);
+  if (rc) return rc;
   if (nleap < 1 || nleap > kMaxLeap || !std::isfinite(dt)) {
     set_error("nleap must be >= 1 and dt finite");
     return WG_ERR_ARG;
@@ -782,11 +828,29 @@ int wg_step(wg_sim* s, double dt, int nleap, double* t0, double* time_elapsed) {
   return run_call(s, dt, nleap, t0, time_elapsed, true);
 }
 
-int wg_download(wg_sim* s, double* x, double* v) {
+int wg_step_begin(wg_sim* s, double dt, int nleap, double* t0) {
+  int rc = check_idle(s);
+  if (rc) return rc;
+  if (nleap < 1 || nleap > kMaxLeap || !std::isfinite(dt)) {
+    set_error("nleap must be >= 1 and dt finite");
+    return WG_ERR_ARG;
+  }
+  s->call_xi = nullptr;
+  s->call_a = nullptr;
+  return run_call_begin(s, dt, nleap, t0, true);
+}
+
+int wg_step_end(wg_sim* s, double* time_elapsed) {
   if (!s) {
     set_error("null simulation");
     return WG_ERR_ARG;
   }
+  return run_call_end(s, time_elapsed);
+}
+
+int wg_download(wg_sim* s, double* x, double* v) {
+  int rc = check_idle(s);
+  if (rc) return rc;
   if (!s->out_valid) {
     launch_desort(s->table, s->n, s->x_out, s->v_out, s->stream);
     s->out_valid = true;
@@ -812,7 +876,8 @@ int wg_destroy(wg_sim* s) {
 }
 
 int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
-  if (!s || reps < 1 || reps > kMaxLeap || !avg_seconds ||
+  if (check_idle(s)) return WG_ERR_ARG;
+  if (reps < 1 || reps > kMaxLeap || !avg_seconds ||
       (what != WG_PROF_FORCE && what != WG_PROF_SORT && what != WG_PROF_BUCKET)) {
     set_error("bad arguments to wg_profile");
     return WG_ERR_ARG;
@@ -959,7 +1024,8 @@ int wg_host_unregister(void* ptr) {
 }
 
 int wg_energy(wg_sim* s, double twopiG, double omega2, double* energy, double* momentum) {
-  if (!s || !(twopiG > 0.0) || !std::isfinite(twopiG) || !std::isfinite(omega2)) {
+  if (check_idle(s)) return WG_ERR_ARG;
+  if (!(twopiG > 0.0) || !std::isfinite(twopiG) || !std::isfinite(omega2)) {
     set_error("wg_energy needs a simulation, a positive finite twopiG and a finite omega2");
     return WG_ERR_ARG;
   }

@@ -9,8 +9,10 @@ numpy's sum of them, ``omega=None`` means no harmonic term, and every
 yields the same ``x, v`` arrays, updated in place, in original particle
 order (plus the elapsed time with ``full_output=True``).
 
-The sheets stay on the device between outputs; each ``next()`` is one call
-into the C ABI (include/wendy_gb300.h) followed by a copy of x and v back.
+The sheets stay on the device between outputs.  Each ``next()`` completes
+the output interval enqueued before, copies x and v back into the yielded
+(page-locked) arrays, and enqueues the next interval before yielding, so the
+device computes output k + 1 while the caller works on output k.
 """
 import copy
 import ctypes
@@ -46,6 +48,17 @@ class Simulation:
         elapsed = ctypes.c_double(0.)
         _lib.check(self._L.wg_step(self._h, float(dt_leap), int(nleap), ctypes.byref(t0),
                                    ctypes.byref(elapsed)), "wg_step")
+        return elapsed.value
+
+    def step_begin(self, dt_leap, nleap, t0):
+        """Enqueue one output interval and return at once (``t0`` advances now)."""
+        _lib.check(self._L.wg_step_begin(self._h, float(dt_leap), int(nleap), ctypes.byref(t0)),
+                   "wg_step_begin")
+
+    def step_end(self):
+        """Complete the interval enqueued by step_begin; returns its device time."""
+        elapsed = ctypes.c_double(0.)
+        _lib.check(self._L.wg_step_end(self._h, ctypes.byref(elapsed)), "wg_step_end")
         return elapsed.value
 
     def energy(self, twopiG=1., omega=None):
@@ -97,9 +110,10 @@ def nbody(x, v, m, dt, t0=0., twopiG=1., omega=None, ext_force=None, approx=Fals
         if nleap is None:
             raise ValueError("When approx is True, the number of leapfrog steps nleap= per output "
                              "time step needs to be set")
-        for item in _nbody_approx(x, v, m, dt, nleap, t0=t0, sort=sort, omega=omega,
-                                  ext_force=ext_force, twopiG=twopiG, full_output=full_output):
-            yield item
+        # yield from: closing this generator closes the inner one (and its
+        # simulation) at once
+        yield from _nbody_approx(x, v, m, dt, nleap, t0=t0, sort=sort, omega=omega,
+                                 ext_force=ext_force, twopiG=twopiG, full_output=full_output)
     raise NotImplementedError("wendy_gb300 implements the approximate integrator (approx=True); "
                               "the exact event-driven solver is the reference wendy's")
 
@@ -123,13 +137,27 @@ def _nbody_approx(x, v, m, dt, nleap, t0=0., omega=None, ext_force=None, sort="c
     sim = Simulation(x, v, m, totmass, omega2, ext_force)
     t = ctypes.c_double(t0)
     dt_leap = dt / nleap
-    while True:
-        elapsed = sim.step(dt_leap, nleap, t)
-        sim.download(x, v)
-        if full_output:
-            yield (x, v, elapsed)
-        else:
-            yield (x, v)
+    L = _lib.lib()
+    pinned = [a for a in (x, v)
+              if a.nbytes >= (1 << 20) and L.wg_host_register(a.ctypes.data, a.nbytes) == 0]
+    try:
+        sim.step_begin(dt_leap, nleap, t)
+        while True:
+            elapsed = sim.step_end()
+            sim.download(x, v)
+            sim.step_begin(dt_leap, nleap, t)
+            if full_output:
+                yield (x, v, elapsed)
+            else:
+                yield (x, v)
+    finally:
+        # also runs when an unclosed generator is collected at interpreter exit
+        try:
+            for a in pinned:
+                L.wg_host_unregister(a.ctypes.data)
+            sim.close()
+        except Exception:
+            pass
 
 
 def accel(x, m, totmass, omega2=-1., ext_force=None, t=0.):
