@@ -260,3 +260,28 @@ def test_changing_dt_between_outputs():
     sim_g.download(gx, gv)
     assert numpy.max(numpy.abs(gx - xx)) <= 1e-10
     assert numpy.max(numpy.abs(gv - vv)) <= 1e-10
+
+
+def test_repeated_overflow_falls_back_and_recovers():
+    # the sheets converge on the origin, cross and spread again: buckets
+    # overflow on consecutive sub-steps (re-sort, restart, then the compact
+    # path with back-off) and the bucket path resumes later; every output
+    # still matches the oracle
+    n = 50000
+    rng = numpy.random.default_rng(11)
+    x = rng.uniform(-1, 1, size=n)
+    v = -x / 0.02
+    m = numpy.full(n, 1.0 / n)
+    sim = wendy_gb300.Simulation(x, v, m, numpy.sum(m))
+    r = O.nbody_approx(x, v, m, 0.05, 5)
+    import ctypes
+    t = ctypes.c_double(0.)
+    gx, gv = numpy.empty(n), numpy.empty(n)
+    for _ in range(8):
+        sim.step(0.01, 5, t)
+        sim.download(gx, gv)
+        rx, rv = next(r)
+        assert numpy.max(numpy.abs(gx - rx)) <= 1e-9
+        assert numpy.max(numpy.abs(gv - rv)) <= 1e-9
+    assert sim.stats()["sorts_full"] > 2
+    sim.close()

@@ -122,6 +122,7 @@ struct wg_sim {
   unsigned* h_ab = nullptr;      // page-locked copy of the overflow count and abort word
   // a call enqueued by wg_step_begin and not yet completed by wg_step_end
   bool pend_active = false;
+  bool pend_compact = false;     // ... and it runs on the compact path
   double pend_dt = 0;
   int pend_nleap = 0, pend_lay0 = 0, pend_cs0 = 0;
   // bucketed layout (the fast path of wg_step)
@@ -146,6 +147,11 @@ struct wg_sim {
   int lay = 0;           // layout holding the sheets in bucket mode
   int qsel = 0;          // splitter array defining the next layout
   int cslot = 0;         // aggregate slot describing layout `lay`
+  // Calls a bucket overflow right after a re-sort sends to the compact path
+  // (full re-sort + fused force kernel per sub-step), and the next such
+  // penalty; the penalty halves after every call the bucket path completes.
+  int compact_calls = 0;
+  int backoff = 1;
   double pending_dt = 0; // dt of the half drift the bucket layout was routed for
   bool out_valid = false;  // x_out / v_out hold the last call's output
   int grid_bucket = 0;
@@ -582,9 +588,11 @@ __global__ void k_store_sheets(const StateTable* table, int64_t n, wg_sheet* xi)
   }
 }
 
+// The sorted sheets as the reference's (idx, val) records, for the drop-in's xi.
 void store_sheets(const StateTable* table, int64_t n, wg_sheet* xi, cudaStream_t st) {
   k_store_sheets<<<152 * 8, 256, 0, st>>>(table, n, xi);
 }
+
 
 }  // namespace
 
@@ -665,12 +673,71 @@ int wg_create(int64_t n, const double* x, const double* v, const double* m, doub
   return WG_OK;
 }
 
+// Sub-steps from .. nleap - 1 of the current call on the compact path: the
+// compact sets hold the sheets at the start of sub-step `from`; each sub-step
+// re-sorts them in full and runs the fused force / kick / drift kernel.  The
+// call's extra outputs (a, xi) come from the last one.  Waits.
+static int compact_continue(wg_sim* s, double dt, int nleap, int from) {
+  ForceArgs f;
+  f.table = s->table;
+  f.n = s->n;
+  f.T_lo = s->T_lo;
+  f.T_hi = s->T_hi;
+  f.E = s->E;
+  f.has_omega = s->omega2 >= 0;
+  f.omega2 = s->omega2;
+  f.ext = s->ext;
+  f.t_seq = s->t_seq;
+  f.epochs = s->epochs;
+  f.recs = s->recs;
+  f.err = s->err;
+  // the bucket launches of these sub-steps consumed their tickets
+  WG_CUDA(cudaMemsetAsync(s->tickets + from, 0, 4 * (size_t)(nleap - from), s->stream));
+  for (int i = from; i < nleap; ++i) {
+    WG_CUDA(cudaMemsetAsync(&s->flags[i].unsorted, 1, sizeof(unsigned), s->stream));
+    radix_sort_state(s->table, s->n, &s->radix, &s->flags[i], s->err, s->stream);
+    f.sub = i;
+    f.dt_kick = dt;
+    f.dt_drift = (i == nleap - 1) ? dt / 2. : dt;
+    f.ticket = s->tickets + i;
+    f.flag_out = &s->flags[i + 1];
+    f.a_out = (i == nleap - 1 && s->call_a) ? s->a_sorted : nullptr;
+    launch_force(f, s->n_tiles, s->stream);
+  }
+  if (s->call_a) launch_scatter_accel(s->table, s->n, s->a_sorted, s->call_a, s->stream);
+  if (s->call_xi) store_sheets(s->table, s->n, reinterpret_cast<wg_sheet*>(s->call_xi), s->stream);
+  s->st.launches += (int64_t)(nleap - from) * (1 + kRadixLaunches);
+  WG_CUDA(cudaStreamSynchronize(s->stream));
+  return WG_OK;
+}
+
 // Enqueue one output interval on the simulation's stream (returns without
 // waiting); run_call_end completes it.
 static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool record_start) {
   int rc = alloc_call_arrays(s, nleap);
   if (rc) return rc;
   fill_times(s, dt, nleap, t0);
+  if (s->compact_calls > 0) {
+    // a recent overflow right after a re-sort: this call runs on the compact
+    // path (full re-sort + fused force kernel per sub-step)
+    if (record_start) WG_CUDA(cudaEventRecord(s->ev0, s->stream));
+    if (s->mode == 1) {
+      WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));
+      bucket_to_compact(s, s->lay, s->cslot);
+      s->mode = 0;
+    }
+    rc = enqueue_step(s, dt, nleap, s->call_a != nullptr, dt / 2.);
+    if (rc) return rc;
+    if (s->call_a) launch_scatter_accel(s->table, s->n, s->a_sorted, s->call_a, s->stream);
+    if (s->call_xi)
+      store_sheets(s->table, s->n, reinterpret_cast<wg_sheet*>(s->call_xi), s->stream);
+    s->compact_calls--;
+    s->pend_active = true;
+    s->pend_compact = true;
+    s->pend_dt = dt;
+    s->pend_nleap = nleap;
+    return WG_OK;
+  }
   rc = take_epochs(s, nleap);
   if (rc) return rc;
   if (record_start) WG_CUDA(cudaEventRecord(s->ev0, s->stream));
@@ -725,61 +792,92 @@ static int run_call_end(wg_sim* s, double* time_elapsed) {
   }
   s->pend_active = false;
   const double dt = s->pend_dt;
-  const int nleap = s->pend_nleap, lay0 = s->pend_lay0, cs0 = s->pend_cs0;
-  WG_CUDA(cudaStreamSynchronize(s->stream));
-  const unsigned ab[2] = {s->h_ab[0], s->h_ab[1]};
+  const int nleap = s->pend_nleap;
   int rc = WG_OK;
+  if (s->pend_compact) {
+    s->pend_compact = false;
+    WG_CUDA(cudaEventRecord(s->ev1, s->stream));
+    rc = finish_call(s, nleap, true);  // waits
+    s->out_valid = false;  // the sheets are sorted, x_out is stale
+    s->mode = 0;
+    s->pending_dt = dt;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    if (time_elapsed) *time_elapsed = ms * 1e-3;
+    double vmax;
+    std::memcpy(&vmax, &s->h_flags[nleap].max_v, 8);
+    s->st.last_max_disp = vmax * std::fabs(dt / 2.);
+    return rc;
+  }
+  int lay0 = s->pend_lay0, cs0 = s->pend_cs0, qs0 = (s->qsel - nleap) & 1;
+  WG_CUDA(cudaStreamSynchronize(s->stream));
   s->out_valid = true;
   s->mode = 1;
   s->pending_dt = dt;
-  if (ab[1] != 0) {
-    // sub-step k overflowed a bucket: its sheets are complete in the layout it
-    // wrote plus the overflow list.  Re-sort from scratch and finish the call
-    // on the compact path.
-    const int k = (int)ab[1] - 1;
-    s->st.sorts_full += 1;
-    const int lay_k = (k % 2 == 0) ? 1 - lay0 : lay0;
-    bucket_to_compact(s, lay_k, (cs0 + k + 1) % kAggSlots);
-    s->mode = 0;
-    if (k < nleap - 1) {
-      ForceArgs f;
-      f.table = s->table;
-      f.n = s->n;
-      f.T_lo = s->T_lo;
-      f.T_hi = s->T_hi;
-      f.E = s->E;
-      f.has_omega = s->omega2 >= 0;
-      f.omega2 = s->omega2;
-      f.ext = s->ext;
-      f.t_seq = s->t_seq;
-      f.epochs = s->epochs;
-      f.recs = s->recs;
-      f.err = s->err;
-      f.a_out = nullptr;
-      StepFlags one{1u, 0u, 0ull};
-      // the bucket launches of these sub-steps consumed their tickets
-      WG_CUDA(cudaMemsetAsync(s->tickets + k + 1, 0, 4 * (size_t)(nleap - k - 1), s->stream));
-      for (int i = k + 1; i < nleap; ++i) {
-        WG_CUDA(cudaMemcpyAsync(&s->flags[i], &one, sizeof(one), cudaMemcpyHostToDevice,
-                                s->stream));
-        radix_sort_state(s->table, s->n, &s->radix, &s->flags[i], s->err, s->stream);
-        f.sub = i;
-        f.dt_kick = dt;
-        f.dt_drift = (i == nleap - 1) ? dt / 2. : dt;
-        f.ticket = s->tickets + i;
-        f.flag_out = &s->flags[i + 1];
-        f.a_out = (i == nleap - 1 && s->call_a) ? s->a_sorted : nullptr;
-        launch_force(f, s->n_tiles, s->stream);
-        WG_CUDA(cudaStreamSynchronize(s->stream));  // pageable `one` stays valid
-      }
-      if (s->call_a) launch_scatter_accel(s->table, s->n, s->a_sorted, s->call_a, s->stream);
-      if (s->call_xi) store_sheets(s->table, s->n, reinterpret_cast<wg_sheet*>(s->call_xi),
-                                   s->stream);
-      s->st.launches += (int64_t)(nleap - k - 1) * (1 + kRadixLaunches);
-      s->out_valid = false;
+  int64_t window_steps = 0;
+  int from = 0;  // first sub-step of the current run of bucket launches
+  bool clean = true;
+  for (;;) {
+    const unsigned ab = s->h_ab[1];
+    if (ab == 0) {
+      window_steps += nleap - from;
+      break;
     }
+    clean = false;
+    // sub-step k overflowed a bucket: its sheets are complete in the layout
+    // it wrote plus the overflow list.  Re-sort them once, lay out fresh
+    // buckets (exact quantiles) and restart the remaining sub-steps on the
+    // bucket path; a last sub-step has already written every output.
+    const int k = (int)ab - 1;
+    window_steps += k + 1 - from;
+    s->st.sorts_full += 1;
+    const int lay_k = (lay0 + k + 1) & 1;
+    bucket_to_compact(s, lay_k, (cs0 + k + 1) % kAggSlots);
+    if (k == nleap - 1) {
+      s->mode = 0;  // the next call re-sorts
+      break;
+    }
+    if (from > 0 && k < from + 2) {
+      // overflowed again right after a re-sort: the buckets cannot follow this
+      // flow for now.  Finish the call on the compact path and keep the next
+      // calls there (back-off doubling up to 64 calls).
+      compact_continue(s, dt, nleap, k + 1);
+      s->mode = 0;
+      s->out_valid = false;
+      s->compact_calls = s->backoff;
+      s->backoff = s->backoff < 64 ? 2 * s->backoff : 64;
+      break;
+    }
+    from = k + 1;
+    WG_CUDA(cudaMemsetAsync(&s->flags[from].unsorted, 1, sizeof(unsigned), s->stream));
+    radix_sort_state(s->table, s->n, &s->radix, &s->flags[from], s->err, s->stream);
+    launch_bucketize(s->table, s->n, s->tune.target, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
+                     s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], s->stream);
+    // sub-step `from` reads layout 0, aggregate slot 0 and routes by splitter set 0
+    lay0 = from & 1;
+    qs0 = from & 1;
+    cs0 = (kAggSlots - from % kAggSlots) % kAggSlots;
+    s->lay = lay0;
+    s->qsel = qs0;
+    s->cslot = cs0;
+    fill_dev(s, dt, 0.0);
+    WG_CUDA(cudaMemcpyAsync(s->d_dev, &s->dev, sizeof(SimDev), cudaMemcpyHostToDevice,
+                            s->stream));
+    WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));
+    // the skipped launches of these sub-steps consumed their tickets
+    WG_CUDA(cudaMemsetAsync(s->tickets + from, 0, 4 * (size_t)(nleap - from), s->stream));
+    for (int i = from; i < nleap; ++i)
+      launch_bucket_step(step_launch(s, i, nleap, 0), s->grid_bucket, s->stream);
+    s->lay = (lay0 + nleap) & 1;
+    s->qsel = (qs0 + nleap) & 1;
+    s->cslot = (cs0 + nleap) % kAggSlots;
+    s->st.launches += 3 + kRadixLaunches + (nleap - from);
+    WG_CUDA(cudaGetLastError());
+    WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
+    WG_CUDA(cudaStreamSynchronize(s->stream));
   }
-  s->st.sorts_window += ab[1] ? (int64_t)ab[1] : (int64_t)nleap;
+  s->st.sorts_window += window_steps;
+  if (clean && s->backoff > 1) s->backoff /= 2;
   WG_CUDA(cudaEventRecord(s->ev1, s->stream));
   rc = finish_call(s, nleap, false);
   float ms = 0;

@@ -509,9 +509,11 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
   }
   // the kernel's view of every simulation, and the task list
   int64_t t = 0;
+  std::vector<int64_t> task0((size_t)count);  // first task of each simulation
   for (int k = 0; k < count; ++k) {
     PoolSim* s = act[(size_t)k];
     SimDev& d = p->h_dev[k];
+    task0[(size_t)k] = t;
     for (int j = 0; j < 2; ++j) {
       d.bx[j] = s->bx[j];
       d.bv[j] = s->bv[j];
@@ -621,51 +623,103 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
     s->pending_dt = dt[k];
     s->fresh = false;
     s->out_valid = true;
-    const unsigned ab = p->h_oc[2 * k + 1];
-    if (!ab) continue;
-    const int kk = (int)ab - 1;  // sub-step that overflowed
-    const int lay_k = (kk % 2 == 0) ? 1 - lay0 : lay0;
-    rc = ensure_workspace(p, s->n);
-    if (rc) return rc;
-    buckets_to_workspace(p, s, lay_k, (cs0 + kk + 1) % kAggSlots, p->ocount + 2 * k);
-    if (kk < nleap - 1) {
-      ForceArgs f;
-      f.table = p->table;
-      f.n = s->n;
-      f.T_lo = s->T_lo;
-      f.T_hi = s->T_hi;
-      f.E = s->E;
-      f.has_omega = s->omega2 >= 0;
-      f.omega2 = s->omega2;
-      f.ext = s->ext;
-      f.t_seq = p->t_seq + (size_t)k * L1;
-      f.epochs = p->epochs;
-      f.recs = p->trecs;
-      f.err = p->err;
-      f.a_out = nullptr;
-      const int64_t tiles = (s->n + kForceTile - 1) / kForceTile;
-      PC(cudaMemsetAsync(p->tickets, 0, 4 * (size_t)nleap, p->stream));
-      // the tile records are shared by every simulation recovered in this
-      // call, under the same epochs: clear them so that no tile takes
-      // another simulation's prefix
-      PC(cudaMemsetAsync(p->trecs, 0, sizeof(TileRec) * (size_t)tiles, p->stream));
-      for (int i = kk + 1; i < nleap; ++i) {
-        const StepFlags one{1u, 0u, 0ull};
-        PC(cudaMemcpyAsync(&p->wflags[i], &one, sizeof(one), cudaMemcpyHostToDevice, p->stream));
-        radix_sort_state(p->table, s->n, &p->radix, &p->wflags[i], p->err, p->stream);
-        f.sub = i;
-        f.dt_kick = dt[k];
-        f.dt_drift = (i == nleap - 1) ? dt[k] / 2. : dt[k];
-        f.ticket = p->tickets + i;
-        f.flag_out = &p->wflags[i + 1];
-        launch_force(f, tiles, p->stream);
-        PC(cudaStreamSynchronize(p->stream));
+    // A sub-step that overflowed a bucket left the sheets complete in the
+    // layout it wrote plus the overflow list: re-sort them once, lay out fresh
+    // buckets and restart the remaining sub-steps of this simulation on the
+    // bucket path (a last sub-step has already written every output).
+    unsigned ab = p->h_oc[2 * k + 1];
+    int l0 = lay0, c0 = cs0, restarted_at = -1;
+    while (ab) {
+      const int kk = (int)ab - 1;
+      rc = ensure_workspace(p, s->n);
+      if (rc) return rc;
+      buckets_to_workspace(p, s, (l0 + kk + 1) & 1, (c0 + kk + 1) % kAggSlots,
+                           p->ocount + 2 * k);
+      if (kk == nleap - 1) {
+        store_compact(p, s);
+        s->mode = 0;
+        break;
       }
-      launch_desort(p->table, s->n, s->x_out, s->v_out, p->stream);
-      p->launches += (int64_t)(nleap - kk - 1) * (1 + kRadixLaunches) + 1;
+      if (restarted_at >= 0 && kk < restarted_at + 2) {
+        // overflowed again right after a re-sort: finish on the compact path
+        // (full re-sort + fused force kernel per sub-step)
+        ForceArgs f;
+        f.table = p->table;
+        f.n = s->n;
+        f.T_lo = s->T_lo;
+        f.T_hi = s->T_hi;
+        f.E = s->E;
+        f.has_omega = s->omega2 >= 0;
+        f.omega2 = s->omega2;
+        f.ext = s->ext;
+        f.t_seq = p->t_seq + (size_t)k * L1;
+        f.epochs = p->epochs;
+        f.recs = p->trecs;
+        f.err = p->err;
+        f.a_out = nullptr;
+        const int64_t tiles = (s->n + kForceTile - 1) / kForceTile;
+        PC(cudaMemsetAsync(p->tickets, 0, 4 * (size_t)nleap, p->stream));
+        // the tile records are shared by every simulation recovered in this
+        // call, under the same epochs: clear them so that no tile takes
+        // another simulation's prefix
+        PC(cudaMemsetAsync(p->trecs, 0, sizeof(TileRec) * (size_t)tiles, p->stream));
+        for (int i = kk + 1; i < nleap; ++i) {
+          PC(cudaMemsetAsync(&p->wflags[i].unsorted, 1, sizeof(unsigned), p->stream));
+          radix_sort_state(p->table, s->n, &p->radix, &p->wflags[i], p->err, p->stream);
+          f.sub = i;
+          f.dt_kick = dt[k];
+          f.dt_drift = (i == nleap - 1) ? dt[k] / 2. : dt[k];
+          f.ticket = p->tickets + i;
+          f.flag_out = &p->wflags[i + 1];
+          launch_force(f, tiles, p->stream);
+        }
+        launch_desort(p->table, s->n, s->x_out, s->v_out, p->stream);
+        store_compact(p, s);
+        p->launches += (int64_t)(nleap - kk - 1) * (1 + kRadixLaunches) + 2;
+        s->mode = 0;
+        break;
+      }
+      const int from = kk + 1;
+      restarted_at = from;
+      PC(cudaMemsetAsync(&p->wflags[from].unsorted, 1, sizeof(unsigned), p->stream));
+      radix_sort_state(p->table, s->n, &p->radix, &p->wflags[from], p->err, p->stream);
+      launch_bucketize(p->table, s->n, s->tune.target, s->nb, s->E, s->bx[0], s->bv[0],
+                       s->bm[0], s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], p->stream);
+      // sub-step `from` reads layout 0, aggregate slot 0 and routes by splitter set 0
+      l0 = from & 1;
+      const int q0 = from & 1;
+      c0 = (kAggSlots - from % kAggSlots) % kAggSlots;
+      SimDev d = p->h_dev[k];
+      d.lay0 = l0;
+      d.qsel0 = q0;
+      d.cs0 = c0;
+      d.pre_dt = 0.0;
+      PC(cudaMemcpyAsync(p->d_dev + k, &d, sizeof(SimDev), cudaMemcpyHostToDevice, p->stream));
+      PC(cudaMemsetAsync(p->ocount + 2 * k, 0, 8, p->stream));
+      // the launches of these sub-steps consumed their tickets
+      PC(cudaMemsetAsync(p->tickets + from, 0, 4 * (size_t)(nleap - from), p->stream));
+      for (int i = from; i < nleap; ++i) {
+        StepLaunch L;
+        L.sims = p->d_dev;
+        L.tasks = p->tasks + task0[(size_t)k];
+        L.ntasks = (int)s->nb;
+        L.sub = i;
+        L.nleap = nleap;
+        L.epochs = p->epochs;
+        L.ticket = p->tickets + i;
+        L.err = p->err;
+        L.profile = 0;
+        launch_bucket_step(L, s->tune.ctas_per_sm * p->sms, p->stream);
+      }
+      p->launches += 3 + kRadixLaunches + (nleap - from);
+      s->lay = (l0 + nleap) & 1;
+      s->qsel = (q0 + nleap) & 1;
+      s->cslot = (c0 + nleap) % kAggSlots;
+      PC(cudaMemcpyAsync(p->h_oc + 2 * k, p->ocount + 2 * k, 8, cudaMemcpyDeviceToHost,
+                         p->stream));
+      PC(cudaStreamSynchronize(p->stream));
+      ab = p->h_oc[2 * k + 1];
     }
-    store_compact(p, s);
-    s->mode = 0;
   }
   PC(cudaEventRecord(p->ev1, p->stream));
   unsigned err = 0;
