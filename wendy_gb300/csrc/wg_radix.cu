@@ -191,16 +191,42 @@ __global__ void __launch_bounds__(THREADS) k_radix_pass(const PassArgs a) {
   }
   // Decoupled look-back over the same digit of earlier tiles.
   uint32_t* stat = a.status + ((int64_t)pass * a.n_tiles) * R;
+  // Each status word carries its count, so relaxed loads and stores
+  // suffice; eight predecessors are read per round, their loads in flight
+  // together, and summed in order up to the nearest inclusive one.
   uint32_t excl = 0;
   if (tile == 0) {
-    st_release_u32(&stat[d], kStatP | count);
+    st_relaxed_u32(&stat[d], kStatP | count);
   } else {
-    st_release_u32(&stat[tile * R + d], kStatA | count);
+    st_relaxed_u32(&stat[tile * R + d], kStatA | count);
+    constexpr int LB = 8;
     int64_t j = tile - 1;
     unsigned spins = 0;
     for (;;) {
-      const unsigned s = ld_acquire_u32(&stat[j * R + d]);
-      if ((s >> 30) == 0u) {
+      uint32_t sv[LB];
+#pragma unroll
+      for (int w = 0; w < LB; ++w) sv[w] = (j - w >= 0) ? ld_relaxed_u32(&stat[(j - w) * R + d]) : 0u;
+      bool done = false, blocked = false;
+      int w = 0;
+      for (; w < LB; ++w) {
+        if (j - w < 0) {
+          done = true;
+          break;
+        }
+        const uint32_t sw = sv[w];
+        if ((sw >> 30) == 0u) {
+          blocked = true;
+          break;
+        }
+        excl += sw & kCountMask;
+        if ((sw >> 30) == 2u || j - w == 0) {
+          done = true;
+          break;
+        }
+      }
+      if (done) break;
+      if (blocked) {
+        j -= w;  // resume at the tile that has not published yet
         if (++spins > kSpinLimit) {
           atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
           break;
@@ -208,11 +234,9 @@ __global__ void __launch_bounds__(THREADS) k_radix_pass(const PassArgs a) {
         __nanosleep(16);
         continue;
       }
-      excl += s & kCountMask;
-      if ((s >> 30) == 2u || j == 0) break;
-      --j;
+      j -= LB;
     }
-    st_release_u32(&stat[tile * R + d], kStatP | (excl + count));
+    st_relaxed_u32(&stat[tile * R + d], kStatP | (excl + count));
   }
   // Exclusive scan of the tile's counts over digits.
   uint32_t incl = count;
