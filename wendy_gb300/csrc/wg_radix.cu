@@ -112,29 +112,38 @@ __global__ void k_radix_plan(int64_t n, const uint32_t* hist, uint32_t* plan,
 }
 
 template <int THREADS, int ITEMS>
-__global__ void __launch_bounds__(THREADS) k_radix_pass(const PassArgs a) {
-  constexpr int TILE = THREADS * ITEMS;
-  constexpr int WARPS = THREADS / 32;
+struct PassSmem {
+  static constexpr int TILE = THREADS * ITEMS;
+  static constexpr int WARPS = THREADS / 32;
+  uint64_t keys[2][TILE];  // tile k lands in keys[k & 1] (positions on pass 0) ...
+  uint32_t vals[2][TILE];  // ... and is staged in digit order in the same buffer
+  uint32_t whist[WARPS][R];
+  uint32_t tile_excl[R];
+  uint32_t gbase[R];
+  uint32_t tmp[WARPS];
+  uint64_t mbar[2];
+  int64_t tile[2];
+};
+
+// Persistent: each CTA claims tiles in order and bulk-copies the next
+// tile's keys and slots into shared memory while it ranks the current one,
+// so the loads of one tile overlap the ranking, look-back and write-out of
+// the previous.  Claims are dynamic, so only running CTAs ever hold a tile
+// and the look-back always progresses: the smallest tile in work has every
+// predecessor finished.
+template <int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
+  using Smem = PassSmem<THREADS, ITEMS>;
+  constexpr int TILE = Smem::TILE;
+  constexpr int WARPS = Smem::WARPS;
   static_assert(THREADS == R, "one thread per digit");
-  extern __shared__ __align__(16) unsigned char smem[];
-  uint64_t* skeys = reinterpret_cast<uint64_t*>(smem);
-  uint32_t* svals = reinterpret_cast<uint32_t*>(skeys + TILE);
-  __shared__ uint32_t s_whist[WARPS][R];
-  __shared__ uint32_t s_tile_excl[R];
-  __shared__ uint32_t s_gbase[R];
-  __shared__ uint32_t s_tmp[WARPS];
-  __shared__ unsigned s_tile;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
 
   if (!a.flag->unsorted) return;
   const int pass = a.pass;
   if (!a.plan[kPlanActive + pass]) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) s_tile = atomicAdd(&a.counters[pass], 1u);
-  for (int i = tid; i < WARPS * R; i += THREADS) (&s_whist[0][0])[i] = 0;
-  __syncthreads();
-  const int64_t tile = s_tile;
-  const int64_t base = tile * TILE;
-  const int tile_n = (int)((a.n - base) < TILE ? (a.n - base) : TILE);
   const int shift = 8 * pass;
   const int srcb = (int)a.plan[kPlanSrc + pass], dstb = (int)a.plan[kPlanDst + pass];
   const uint64_t* ksrc = srcb ? a.keys1 : a.keys0;
@@ -142,160 +151,239 @@ __global__ void __launch_bounds__(THREADS) k_radix_pass(const PassArgs a) {
   uint64_t* kdst = dstb ? a.keys1 : a.keys0;
   uint32_t* pdst = dstb ? a.pos1 : a.pos0;
   const double* x = a.table->cur.x;
-
-  uint64_t key[ITEMS];
-  uint32_t val[ITEMS];
-  uint32_t rank[ITEMS];
-#pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    const int local = warp * (32 * ITEMS) + i * 32 + lane;
-    const int64_t e = base + local;
-    if (local < tile_n) {
-      if (pass == 0) {
-        key[i] = key_of(x[e]);
-        val[i] = (uint32_t)e;
-      } else {
-        key[i] = ksrc[e];
-        val[i] = psrc[e];
-      }
-    } else {
-      key[i] = 0;
-      val[i] = 0;
-    }
-  }
-  // Stable ranking inside the warp: items in order, lanes in order.
-#pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    const int local = warp * (32 * ITEMS) + i * 32 + lane;
-    const bool ok = local < tile_n;
-    const unsigned d = ok ? (unsigned)((key[i] >> shift) & 255u) : (0x100u + lane);
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    uint32_t old = 0;
-    if (ok) {
-      old = s_whist[warp][d];
-      rank[i] = old + __popc(peers & lanemask_lt());
-    }
-    __syncwarp();
-    if (ok && lane == __ffs(peers) - 1) s_whist[warp][d] = old + __popc(peers);
-    __syncwarp();
-  }
-  __syncthreads();
-  // Column of digit `tid`: exclusive offsets of the warps, tile count.
-  const int d = tid;
-  uint32_t count = 0;
-#pragma unroll
-  for (int w = 0; w < WARPS; ++w) {
-    const uint32_t c = s_whist[w][d];
-    s_whist[w][d] = count;
-    count += c;
-  }
-  // Decoupled look-back over the same digit of earlier tiles.
+  const void* kfrom = pass == 0 ? (const void*)x : (const void*)ksrc;
+  const bool bulk_ok = ((uintptr_t)kfrom & 15u) == 0 && (pass == 0 || ((uintptr_t)psrc & 15u) == 0);
   uint32_t* stat = a.status + ((int64_t)pass * a.n_tiles) * R;
-  // Each status word carries its count, so relaxed loads and stores
-  // suffice; eight predecessors are read per round, their loads in flight
-  // together, and summed in order up to the nearest inclusive one.
-  uint32_t excl = 0;
-  if (tile == 0) {
-    st_relaxed_u32(&stat[d], kStatP | count);
-  } else {
-    st_relaxed_u32(&stat[tile * R + d], kStatA | count);
-    constexpr int LB = 8;
-    int64_t j = tile - 1;
-    unsigned spins = 0;
-    for (;;) {
-      uint32_t sv[LB];
+  unsigned* claim = a.counters + pass;
+
+  // thread 0: start the copy of tile t into buffer b; partial tiles (and
+  // unaligned sources) are read with plain loads, their phase completes at once
+  auto issue = [&](int64_t t, int b) {
+    if (t >= a.n_tiles) return;
+    const int64_t base = t * TILE;
+    if (bulk_ok && a.n - base >= TILE) {
+      const uint32_t kb = TILE * 8u, vb = pass ? TILE * 4u : 0u;
+      mbar_expect_tx(&S.mbar[b], kb + vb);
+      bulk_g2s(S.keys[b], static_cast<const char*>(kfrom) + base * 8, kb, &S.mbar[b]);
+      if (pass) bulk_g2s(S.vals[b], psrc + base, vb, &S.mbar[b]);
+    } else {
+      mbar_expect_tx(&S.mbar[b], 0u);
+    }
+  };
+
+  if (tid == 0) {
+    mbar_init(&S.mbar[0], 1);
+    mbar_init(&S.mbar[1], 1);
+    fence_proxy_async_smem();
+    const int64_t t0 = atomicAdd(claim, 1u);
+    S.tile[0] = t0;
+    issue(t0, 0);
+  }
+  for (int i = tid; i < WARPS * R; i += THREADS) (&S.whist[0][0])[i] = 0;
+  __syncthreads();
+
+  for (int k = 0;; ++k) {
+    const int b = k & 1;
+    const int64_t tile = S.tile[b];
+    if (tile >= a.n_tiles) break;
+    if (tid == 0) {
+      // buffer b^1 was staged and written out by the previous tile, and the
+      // barrier that ended it orders those accesses before this copy
+      const int64_t tn = atomicAdd(claim, 1u);
+      S.tile[b ^ 1] = tn;
+      fence_proxy_async_smem();
+      issue(tn, b ^ 1);
+    }
+    const int64_t base = tile * TILE;
+    const int tile_n = (int)((a.n - base) < TILE ? (a.n - base) : TILE);
+    const bool via_bulk = bulk_ok && tile_n == TILE;
+    if (via_bulk && !mbar_wait(&S.mbar[b], (unsigned)(k >> 1) & 1u) && lane == 0)
+      atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
+
+    uint64_t key[ITEMS];
+    uint32_t val[ITEMS];
+    uint32_t rank[ITEMS];
 #pragma unroll
-      for (int w = 0; w < LB; ++w) sv[w] = (j - w >= 0) ? ld_relaxed_u32(&stat[(j - w) * R + d]) : 0u;
-      bool done = false, blocked = false;
-      int w = 0;
-      for (; w < LB; ++w) {
-        if (j - w < 0) {
-          done = true;
-          break;
+    for (int i = 0; i < ITEMS; ++i) {
+      const int local = warp * (32 * ITEMS) + i * 32 + lane;
+      const int64_t e = base + local;
+      if (local < tile_n) {
+        if (via_bulk) {
+          const uint64_t raw = S.keys[b][local];
+          key[i] = pass == 0 ? key_of(__longlong_as_double((long long)raw)) : raw;
+          val[i] = pass == 0 ? (uint32_t)e : S.vals[b][local];
+        } else if (pass == 0) {
+          key[i] = key_of(x[e]);
+          val[i] = (uint32_t)e;
+        } else {
+          key[i] = ksrc[e];
+          val[i] = psrc[e];
         }
-        const uint32_t sw = sv[w];
-        if ((sw >> 30) == 0u) {
-          blocked = true;
-          break;
-        }
-        excl += sw & kCountMask;
-        if ((sw >> 30) == 2u || j - w == 0) {
-          done = true;
-          break;
-        }
+      } else {
+        key[i] = 0;
+        val[i] = 0;
       }
-      if (done) break;
-      if (blocked) {
-        j -= w;  // resume at the tile that has not published yet
-        if (++spins > kSpinLimit) {
-          atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
-          break;
-        }
-        __nanosleep(16);
-        continue;
+    }
+    // Stable ranking inside the warp: items in order, lanes in order.
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      const int local = warp * (32 * ITEMS) + i * 32 + lane;
+      const bool ok = local < tile_n;
+      const unsigned d = ok ? (unsigned)((key[i] >> shift) & 255u) : (0x100u + lane);
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      uint32_t old = 0;
+      if (ok) {
+        old = S.whist[warp][d];
+        rank[i] = old + __popc(peers & lanemask_lt());
       }
-      j -= LB;
+      __syncwarp();
+      if (ok && lane == __ffs(peers) - 1) S.whist[warp][d] = old + __popc(peers);
+      __syncwarp();
     }
-    st_relaxed_u32(&stat[tile * R + d], kStatP | (excl + count));
-  }
-  // Exclusive scan of the tile's counts over digits.
-  uint32_t incl = count;
+    __syncthreads();
+    // Column of digit `tid`: exclusive offsets of the warps, tile count.
+    const int d = tid;
+    uint32_t count = 0;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += y;
-  }
-  if (lane == 31) s_tmp[warp] = incl;
-  __syncthreads();
-  uint32_t wpre = 0;
-#pragma unroll
-  for (int w = 0; w < WARPS; ++w) wpre += (w < warp) ? s_tmp[w] : 0u;
-  const uint32_t tex = wpre + incl - count;
-  s_tile_excl[d] = tex;
-  s_gbase[d] = a.plan[kPlanStarts + pass * R + d] + excl - tex;
-  __syncthreads();
-  // Stage the tile in digit order.
-#pragma unroll
-  for (int i = 0; i < ITEMS; ++i) {
-    const int local = warp * (32 * ITEMS) + i * 32 + lane;
-    if (local < tile_n) {
-      const unsigned dd = (unsigned)((key[i] >> shift) & 255u);
-      const uint32_t p = s_tile_excl[dd] + s_whist[warp][dd] + rank[i];
-      skeys[p] = key[i];
-      svals[p] = val[i];
+    for (int w = 0; w < WARPS; ++w) {
+      const uint32_t c = S.whist[w][d];
+      S.whist[w][d] = count;
+      count += c;
     }
-  }
-  __syncthreads();
+    // Decoupled look-back over the same digit of earlier tiles.  Each status
+    // word carries its count, so relaxed loads and stores suffice; LB
+    // predecessors are read per round, their loads in flight together, and
+    // summed in order up to the nearest inclusive one.
+    uint32_t excl = 0;
+    if (tile == 0) {
+      st_relaxed_u32(&stat[d], kStatP | count);
+    } else {
+      st_relaxed_u32(&stat[tile * R + d], kStatA | count);
+      constexpr int LB = 8;
+      int64_t j = tile - 1;
+      unsigned spins = 0;
+      for (;;) {
+        uint32_t sv[LB];
 #pragma unroll
-  for (int j = 0; j < ITEMS; ++j) {
-    const int p = j * THREADS + tid;
-    if (p < tile_n) {
-      const uint64_t k = skeys[p];
-      const unsigned dd = (unsigned)((k >> shift) & 255u);
-      const int64_t o = (int64_t)s_gbase[dd] + p;
-      kdst[o] = k;
-      pdst[o] = svals[p];
+        for (int w = 0; w < LB; ++w) sv[w] = (j - w >= 0) ? ld_relaxed_u32(&stat[(j - w) * R + d]) : 0u;
+        bool done = false, blocked = false;
+        int w = 0;
+        for (; w < LB; ++w) {
+          const uint32_t sw = sv[w];
+          if ((sw >> 30) == 0u) {
+            blocked = true;
+            break;
+          }
+          excl += sw & kCountMask;
+          if ((sw >> 30) == 2u || j - w == 0) {
+            done = true;
+            break;
+          }
+        }
+        if (done) break;
+        if (blocked) {
+          j -= w;  // resume at the tile that has not published yet
+          if (++spins > kSpinLimit) {
+            atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
+            break;
+          }
+          __nanosleep(16);
+          continue;
+        }
+        j -= LB;
+      }
+      st_relaxed_u32(&stat[tile * R + d], kStatP | (excl + count));
     }
+    // Exclusive scan of the tile's counts over digits.
+    uint32_t incl = count;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) S.tmp[warp] = incl;
+    __syncthreads();
+    uint32_t wpre = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) wpre += (w < warp) ? S.tmp[w] : 0u;
+    const uint32_t tex = wpre + incl - count;
+    S.tile_excl[d] = tex;
+    S.gbase[d] = a.plan[kPlanStarts + pass * R + d] + excl - tex;
+    __syncthreads();
+    // Stage the tile in digit order (over the buffer it arrived in).
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      const int local = warp * (32 * ITEMS) + i * 32 + lane;
+      if (local < tile_n) {
+        const unsigned dd = (unsigned)((key[i] >> shift) & 255u);
+        const uint32_t p = S.tile_excl[dd] + S.whist[warp][dd] + rank[i];
+        S.keys[b][p] = key[i];
+        S.vals[b][p] = val[i];
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < WARPS * R; i += THREADS) (&S.whist[0][0])[i] = 0;
+#pragma unroll
+    for (int jj = 0; jj < ITEMS; ++jj) {
+      const int p = jj * THREADS + tid;
+      if (p < tile_n) {
+        const uint64_t kk = S.keys[b][p];
+        const unsigned dd = (unsigned)((kk >> shift) & 255u);
+        const int64_t o = (int64_t)S.gbase[dd] + p;
+        kdst[o] = kk;
+        pdst[o] = S.vals[b][p];
+      }
+    }
+    __syncthreads();
   }
 }
 
-__global__ void k_radix_gather(StateTable* table, int64_t n, const uint64_t* keys0,
-                               const uint64_t* keys1, const uint32_t* pos0, const uint32_t* pos1,
-                               const uint32_t* plan, uint32_t* counters, const StepFlags* flag) {
+// Permute x, v, m, idx into the other set; GU sheets per thread with their
+// loads in flight together (the reads are random when the input was).
+constexpr int kGatherThreads = 256, kGatherUnroll = 4;
+__global__ void __launch_bounds__(kGatherThreads) k_radix_gather(
+    StateTable* table, int64_t n, const uint64_t* keys0, const uint64_t* keys1,
+    const uint32_t* pos0, const uint32_t* pos1, const uint32_t* plan, uint32_t* counters,
+    const StepFlags* flag) {
+  constexpr int GU = kGatherUnroll;
   if (!flag->unsorted) return;
   const int fb = (int)plan[kPlanFinal];
-  const uint64_t* keys = fb ? keys1 : keys0;
-  const uint32_t* pos = fb ? pos1 : pos0;
+  const uint64_t* __restrict__ keys = fb ? keys1 : keys0;
+  const uint32_t* __restrict__ pos = fb ? pos1 : pos0;
   const StateRef cur = table->cur, oth = table->other;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t chunk = (int64_t)gridDim.x * kGatherThreads * GU;
   bool tie = false;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += stride) {
-    const uint32_t q = pos[p];
-    oth.x[p] = cur.x[q];
-    oth.v[p] = cur.v[q];
-    oth.m[p] = cur.m[q];
-    oth.idx[p] = cur.idx[q];
-    if (p + 1 < n && keys[p] == keys[p + 1]) tie = true;
+  for (int64_t p0 = (int64_t)blockIdx.x * kGatherThreads * GU + threadIdx.x; p0 < n;
+       p0 += chunk) {
+    uint32_t q[GU];
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int64_t p = p0 + (int64_t)u * kGatherThreads;
+      q[u] = p < n ? __ldcs(pos + p) : 0u;
+    }
+    double xs[GU], vs[GU], ms[GU];
+    int32_t is[GU];
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int64_t p = p0 + (int64_t)u * kGatherThreads;
+      if (p < n) {
+        xs[u] = __ldg(cur.x + q[u]);
+        vs[u] = __ldg(cur.v + q[u]);
+        ms[u] = __ldg(cur.m + q[u]);
+        is[u] = __ldg(cur.idx + q[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < GU; ++u) {
+      const int64_t p = p0 + (int64_t)u * kGatherThreads;
+      if (p < n) {
+        oth.x[p] = xs[u];
+        oth.v[p] = vs[u];
+        oth.m[p] = ms[u];
+        oth.idx[p] = is[u];
+        if (p + 1 < n && keys[p] == keys[p + 1]) tie = true;
+      }
+    }
   }
   if (__syncthreads_or(tie) && threadIdx.x == 0) atomicOr(&counters[8], 1u);
 }
@@ -370,12 +458,19 @@ void radix_bind(RadixWork* w, void* base, int64_t n) {
 
 void radix_sort_state(StateTable* table, int64_t n, RadixWork* w, const StepFlags* flag,
                       unsigned* err, cudaStream_t s) {
-  static bool attr_set = false;
-  constexpr size_t dyn = (size_t)kRadixTile * (8 + 4);
-  if (!attr_set) {
+  static int pass_grid_per_sm = 0, sms = 0;
+  constexpr size_t dyn = sizeof(PassSmem<kRadixThreads, kRadixItems>);
+  static_assert(kRadixTile == PassSmem<kRadixThreads, kRadixItems>::TILE, "tile size");
+  if (!pass_grid_per_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaFuncSetAttribute(k_radix_pass<kRadixThreads, kRadixItems>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    attr_set = true;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &pass_grid_per_sm, k_radix_pass<kRadixThreads, kRadixItems>, kRadixThreads, dyn);
+    if (pass_grid_per_sm < 1) pass_grid_per_sm = 1;
+    if (sms < 1) sms = 1;
   }
   // the workspace may be bound for more sheets than this sort has: tiles,
   // look-back words and launches follow n
@@ -401,16 +496,22 @@ void radix_sort_state(StateTable* table, int64_t n, RadixWork* w, const StepFlag
   a.counters = w->counters;
   a.flag = flag;
   a.err = err;
+  int64_t pg = (int64_t)pass_grid_per_sm * sms;
+  if (pg > tiles) pg = tiles;
+  if (pg < 1) pg = 1;
   for (int p = 0; p < 8; ++p) {
     a.pass = p;
-    k_radix_pass<kRadixThreads, kRadixItems>
-        <<<(unsigned)tiles, kRadixThreads, dyn, s>>>(a);
+    k_radix_pass<kRadixThreads, kRadixItems><<<(unsigned)pg, kRadixThreads, dyn, s>>>(a);
   }
+  int64_t gg = (n + kGatherThreads * kGatherUnroll - 1) / (kGatherThreads * kGatherUnroll);
+  if (gg > (int64_t)sms * 8) gg = (int64_t)sms * 8;
+  if (gg < 1) gg = 1;
+  k_radix_gather<<<(unsigned)gg, kGatherThreads, 0, s>>>(table, n, w->keys[0], w->keys[1],
+                                                          w->pos[0], w->pos[1], w->plan,
+                                                          w->counters, flag);
   int g = (int)((n + 255) / 256);
   if (g > 152 * 16) g = 152 * 16;
   if (g < 1) g = 1;
-  k_radix_gather<<<g, 256, 0, s>>>(table, n, w->keys[0], w->keys[1], w->pos[0], w->pos[1],
-                                   w->plan, w->counters, flag);
   k_radix_ties<<<g, 256, 0, s>>>(table, n, w->keys[0], w->keys[1], w->plan, w->counters,
                                  flag);
   k_radix_flip<<<1, 1, 0, s>>>(table, flag);
