@@ -412,9 +412,10 @@ def main():
     value = units / elapsed
     launches = st1["launches"] - st0["launches"]
 
-    # The timed region launches k_bucket_step once per sub-step and nothing
-    # else but a few small copies per call, so its CUDA-event time divided by
-    # the launches is the kernel's average launch duration.
+    # The timed region launches k_bucket_step once per sub-step and, per
+    # call, one short k_split_out (x, v out of the last sub-step's records)
+    # and a few small copies, so its CUDA-event time divided by the sub-steps
+    # is the bucket kernel's average launch duration to within that.
     hbm, hbm_kind = peaks()
     sub_s = elapsed / (args.steps * nleap)
     bucket_gbs = 56.0 * n / sub_s / 1e9

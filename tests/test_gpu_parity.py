@@ -62,6 +62,55 @@ def test_accel_matches_oracle(n):
     assert numpy.max(numpy.abs(a - ra)) <= 1e-12 * _scale(ra, tot)
 
 
+@pytest.mark.parametrize("n,levels", [(100003, 37), (1 << 17, 1), (1 << 20, 4096)])
+def test_accel_with_many_equal_positions(n, levels):
+    # Runs of equal positions spanning many sort tiles.  Equal positions are
+    # ordered by original index (the reference's quicksort leaves their order
+    # to its pivots), so the expected order is the stable argsort and the
+    # expected force the reference formula (wendy/wendy.c:371-383) in it.
+    rng = numpy.random.default_rng(n)
+    x = rng.integers(0, levels, n) * 0.25 - 3.0
+    m = rng.lognormal(0., 0.5, n)
+    tot = numpy.sum(m)
+    a, perm = wendy_gb300.accel(x, m, tot, omega2=1.21)
+    order = numpy.argsort(x, kind="stable")
+    assert numpy.array_equal(perm, order)
+    cm = numpy.concatenate(([0.], numpy.cumsum(m[order])[:-1]))
+    ra = numpy.empty(n)
+    ra[order] = tot - 2 * cm - m[order] - 1.21 * x[order]
+    assert numpy.max(numpy.abs(a - ra)) <= 1e-12 * _scale(ra, tot)
+
+
+@pytest.mark.parametrize("n,ntied", [(50000, 30000), (300000, 20)])
+def test_dropin_unordered_coincident_sheets(n, ntied):
+    # a group of coincident sheets handed over in the caller's xi order, not
+    # in index order: the sort orders the group by index, so the force of
+    # the one evaluation (after the opening half drift) follows from the
+    # (position, index) order
+    rng = numpy.random.default_rng(n)
+    x = rng.normal(size=n)
+    v = rng.normal(size=n)
+    tied = rng.choice(n, ntied, replace=False)
+    x[tied] = 0.5
+    v[tied] = 0.0
+    m = rng.lognormal(0., 0.5, n)
+    tot = numpy.sum(m)
+    order = rng.permutation(n).astype(numpy.int32)
+    xi = numpy.zeros(n, dtype=_lib.SHEET_DTYPE)
+    xi["idx"] = order
+    xi["val"] = x[order]
+    xx, vv, a = x.copy(), v.copy(), numpy.zeros(n)
+    dt = 1e-3
+    wendy_gb300.approx_onestep(xi, xx, vv, m, a, tot, dt, 1, 0.0)
+    xf = x + v * (dt / 2.)
+    srt = numpy.argsort(xf, kind="stable")
+    assert numpy.array_equal(xi["idx"], srt)
+    cm = numpy.concatenate(([0.], numpy.cumsum(m[srt])[:-1]))
+    ra = numpy.empty(n)
+    ra[srt] = tot - 2 * cm - m[srt]
+    assert numpy.max(numpy.abs(a - ra)) <= 1e-12 * _scale(ra, tot)
+
+
 def test_accel_at_large_n_equal_masses_is_exact():
     # N = 2^24 equal masses 2^-24: every partial sum is representable, so the
     # reference's serial sum is exact and both sides must agree bit for bit.

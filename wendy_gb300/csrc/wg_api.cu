@@ -517,6 +517,9 @@ void fill_dev(wg_sim* s, double dt, double pre) {
   d.v_out = s->v_out;
   d.xi_out = s->call_xi;
   d.a_out = s->call_a;
+  // the compact sets are free while the sheets live in buckets: the last
+  // sub-step's (x, v, a) records go there (56 B/sheet >= 32)
+  d.rec_out = reinterpret_cast<OutRec*>(s->set[0].x);
   d.flags = s->flags;
   d.t_seq = s->t_seq;
   d.n = s->n;
@@ -769,10 +772,11 @@ static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool reco
   fill_dev(s, dt, pre);
   WG_CUDA(cudaMemcpyAsync(s->d_dev, &s->dev, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream));
   for (int i = 0; i < nleap; ++i) launch_bucket_step(step_launch(s, i, nleap, 0), s->grid_bucket, s->stream);
+  launch_split_out(s->dev.rec_out, s->n, s->x_out, s->v_out, s->call_a, s->stream);
   s->lay = (lay0 + nleap) & 1;
   s->qsel = (s->qsel + nleap) & 1;
   s->cslot = (cs0 + nleap) % kAggSlots;
-  s->st.launches += nleap;
+  s->st.launches += nleap + 1;
   WG_CUDA(cudaGetLastError());
   WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
   s->pend_active = true;
@@ -868,10 +872,11 @@ static int run_call_end(wg_sim* s, double* time_elapsed) {
     WG_CUDA(cudaMemsetAsync(s->tickets + from, 0, 4 * (size_t)(nleap - from), s->stream));
     for (int i = from; i < nleap; ++i)
       launch_bucket_step(step_launch(s, i, nleap, 0), s->grid_bucket, s->stream);
+    launch_split_out(s->dev.rec_out, s->n, s->x_out, s->v_out, s->call_a, s->stream);
     s->lay = (lay0 + nleap) & 1;
     s->qsel = (qs0 + nleap) & 1;
     s->cslot = (cs0 + nleap) % kAggSlots;
-    s->st.launches += 3 + kRadixLaunches + (nleap - from);
+    s->st.launches += 4 + kRadixLaunches + (nleap - from);
     WG_CUDA(cudaGetLastError());
     WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
     WG_CUDA(cudaStreamSynchronize(s->stream));
@@ -983,6 +988,13 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   if (what == WG_PROF_BUCKET && s->mode != 1) {
     set_error("wg_profile(WG_PROF_BUCKET) needs the bucket layout: run wg_step first");
     return WG_ERR_ARG;
+  }
+  // the force and sort kernels run on the compact sets, which hold other
+  // data while the sheets live in buckets: hand the current state back to
+  // them first (the next wg_step re-sorts and re-buckets, as after wg_energy)
+  if (what != WG_PROF_BUCKET && s->mode == 1) {
+    bucket_to_compact(s, s->lay, s->cslot);
+    s->mode = 0;
   }
   int rc = alloc_call_arrays(s, reps);
   if (rc) return rc;

@@ -775,8 +775,17 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
             (unsigned long long)__double_as_longlong(vn) & 0x7FFFFFFFFFFFFFFFull;
         maxv = av > maxv ? av : maxv;
         if (LAST && !L.profile) {
-          D.x_out[idv[u]] = xn;
-          D.v_out[idv[u]] = vn;
+          OutRec* const ro = D.rec_out;
+          if (ro) {
+            double2* const r2 = reinterpret_cast<double2*>(ro + idv[u]);
+            r2[0] = make_double2(xn, vn);
+            r2[1] = make_double2(acc, 0.0);
+          } else {
+            D.x_out[idv[u]] = xn;
+            D.v_out[idv[u]] = vn;
+            double* const a_out = D.a_out;
+            if (a_out) a_out[idv[u]] = acc;
+          }
           SheetRec* const xi_out = D.xi_out;
           if (xi_out) {
             SheetRec rec;
@@ -785,8 +794,6 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
             rec.val = xn;
             xi_out[r] = rec;
           }
-          double* const a_out = D.a_out;
-          if (a_out) a_out[idv[u]] = acc;
         }
         kd[u] = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, vn, xn) : xn);
       }
@@ -1089,6 +1096,28 @@ void bucket_step_prepare() {
                          (int)sizeof(StepSmem));
     attr = true;
   }
+}
+
+__global__ void __launch_bounds__(256) k_split_out(const OutRec* __restrict__ rec, int64_t n,
+                                                   double* __restrict__ x_out,
+                                                   double* __restrict__ v_out,
+                                                   double* __restrict__ a_out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double2* r2 = reinterpret_cast<const double2*>(rec + i);
+    const double2 xv = __ldcs(r2);
+    x_out[i] = xv.x;
+    v_out[i] = xv.y;
+    if (a_out) a_out[i] = __ldcs(r2 + 1).x;
+  }
+}
+
+void launch_split_out(const OutRec* rec, int64_t n, double* x_out, double* v_out, double* a_out,
+                      cudaStream_t s) {
+  int64_t g = (n + 255) / 256;
+  if (g > 152 * 8) g = 152 * 8;
+  if (g < 1) g = 1;
+  k_split_out<<<(unsigned)g, 256, 0, s>>>(rec, n, x_out, v_out, a_out);
 }
 
 void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s) {

@@ -68,6 +68,13 @@ struct SheetRec {
 // One simulation as the sub-step kernel sees it.  Arrays are the
 // simulation's own; layouts, counts and splitters come in pairs used
 // alternately from sub-step to sub-step, starting at lay0 / qsel0.
+// One sheet's output in original order: a whole 32-byte sector, so that the
+// random write of the last sub-step needs no read-modify-write of the
+// memory line it lands in (three 8-byte writes to x, v and a each did).
+struct alignas(32) OutRec {
+  double x, v, a, pad;
+};
+
 struct SimDev {
   double* bx[2];
   double* bv[2];
@@ -87,6 +94,8 @@ struct SimDev {
   double* v_out;
   SheetRec* xi_out;      // optional: (idx, x) in the last sub-step's sorted order
   double* a_out;         // optional: accelerations of the last force evaluation, original order
+  OutRec* rec_out;       // optional: if set, the last sub-step writes (x, v, a) records
+                         // here in original order instead, for launch_split_out
   StepFlags* flags;      // [nleap + 1] of this call
   const double* t_seq;   // [nleap] times of this call's force evaluations
   int64_t n;
@@ -126,6 +135,9 @@ struct StepLaunch {
 };
 
 void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s);
+// x_out, v_out (and a_out when not null) from the records of rec_out.
+void launch_split_out(const OutRec* rec, int64_t n, double* x_out, double* v_out, double* a_out,
+                      cudaStream_t s);
 // One-time kernel attribute set-up; call before any stream capture.
 void bucket_step_prepare();
 int bucket_step_grid(int sm_count);

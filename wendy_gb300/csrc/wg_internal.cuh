@@ -100,8 +100,8 @@ void launch_energy(const StateTable* table, int64_t n, const double* a_sorted, d
 void record_last_error(const char* msg);
 
 // --- launchers (wg_radix.cu) ---
-constexpr int kRadixLaunches = 13;  // kernels radix_sort_state enqueues (hist, plan, 8 passes,
-                                    // gather, ties, flip)
+constexpr int kRadixLaunches = 14;  // kernels radix_sort_state enqueues (hist, plan, 8 passes,
+                                    // gather, ties, long ties, flip)
 size_t radix_bytes(int64_t n);
 void radix_bind(RadixWork* w, void* base, int64_t n);
 // Sort table->cur by (position key, original index) unless flags->unsorted

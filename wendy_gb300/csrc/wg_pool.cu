@@ -513,6 +513,7 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
   for (int k = 0; k < count; ++k) {
     PoolSim* s = act[(size_t)k];
     SimDev& d = p->h_dev[k];
+    d.rec_out = nullptr;  // members write x_out, v_out directly
     task0[(size_t)k] = t;
     for (int j = 0; j < 2; ++j) {
       d.bx[j] = s->bx[j];

@@ -8,11 +8,14 @@
 //   hist   one read of the positions: all eight digit histograms
 //   plan   exclusive digit offsets; passes whose digit is the same for every
 //          key are skipped (decided on the device)
-//   pass   8x: rank within the tile (warp match + shared-memory counters,
-//          stable), look-back for the tile's global digit offsets, stage in
-//          shared memory, write out
+//   pass   8x, persistent: bulk-copy the tile into shared memory (the next
+//          tile's copy overlaps this one's write-out), rank within the tile
+//          (bit-plane ballots + per-warp shared-memory counters, stable),
+//          publish the tile's digit counts, stage in digit order, look back
+//          for the tile's global digit offsets, write out
 //   gather permute x, v, m, idx into the other state set
-//   ties   equal keys are ordered by original index (rare; usually no-op)
+//   ties   equal keys are ordered by original index (rare; usually no-op):
+//          short runs in place, long runs by one CTA each
 //   flip   the other set becomes the current one
 //
 // Every kernel first reads the sub-step's `unsorted` flag and returns at once
@@ -125,12 +128,14 @@ struct PassSmem {
   int64_t tile[2];
 };
 
-// Persistent: each CTA claims tiles in order and bulk-copies the next
-// tile's keys and slots into shared memory while it ranks the current one,
-// so the loads of one tile overlap the ranking, look-back and write-out of
-// the previous.  Claims are dynamic, so only running CTAs ever hold a tile
-// and the look-back always progresses: the smallest tile in work has every
-// predecessor finished.
+// Persistent: each CTA claims its next tile once the current one's global
+// offsets are known and bulk-copies it into its other shared-memory buffer
+// during the current write-out.  Claiming that late keeps claim order close
+// to processing order, which keeps look-backs short; publishing the counts
+// before staging, and looking back only after it, gives the tiles ahead the
+// staging time to finish.  Claims are dynamic, so only running CTAs ever
+// hold a tile and the look-back always progresses: the smallest tile in work
+// has every predecessor finished.
 template <int THREADS, int ITEMS>
 __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
   using Smem = PassSmem<THREADS, ITEMS>;
@@ -186,20 +191,11 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
     const int b = k & 1;
     const int64_t tile = S.tile[b];
     if (tile >= a.n_tiles) break;
-    if (tid == 0) {
-      // buffer b^1 was staged and written out by the previous tile, and the
-      // barrier that ended it orders those accesses before this copy
-      const int64_t tn = atomicAdd(claim, 1u);
-      S.tile[b ^ 1] = tn;
-      fence_proxy_async_smem();
-      issue(tn, b ^ 1);
-    }
     const int64_t base = tile * TILE;
     const int tile_n = (int)((a.n - base) < TILE ? (a.n - base) : TILE);
     const bool via_bulk = bulk_ok && tile_n == TILE;
     if (via_bulk && !mbar_wait(&S.mbar[b], (unsigned)(k >> 1) & 1u) && lane == 0)
       atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
-
     uint64_t key[ITEMS];
     uint32_t val[ITEMS];
     uint32_t rank[ITEMS];
@@ -230,7 +226,16 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
       const int local = warp * (32 * ITEMS) + i * 32 + lane;
       const bool ok = local < tile_n;
       const unsigned d = ok ? (unsigned)((key[i] >> shift) & 255u) : (0x100u + lane);
-      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      // lanes holding the same digit, from its eight bit planes (one ballot
+      // per bit: cheaper than a match instruction over 32 mostly distinct
+      // digits)
+      unsigned peers = __ballot_sync(0xffffffffu, ok);
+      if (!ok) peers = ~peers;
+#pragma unroll
+      for (int bit = 0; bit < 8; ++bit) {
+        const unsigned bal = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+        peers &= ((d >> bit) & 1u) ? bal : ~bal;
+      }
       uint32_t old = 0;
       if (ok) {
         old = S.whist[warp][d];
@@ -241,7 +246,8 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
       __syncwarp();
     }
     __syncthreads();
-    // Column of digit `tid`: exclusive offsets of the warps, tile count.
+    // Column of digit `tid`: exclusive offsets of the warps, tile count;
+    // the count is published at once for the tiles behind this one.
     const int d = tid;
     uint32_t count = 0;
 #pragma unroll
@@ -250,15 +256,44 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
       S.whist[w][d] = count;
       count += c;
     }
+    if (tile == 0)
+      st_relaxed_u32(&stat[d], kStatP | count);
+    else
+      st_relaxed_u32(&stat[tile * R + d], kStatA | count);
+    // Exclusive scan of the tile's counts over digits.
+    uint32_t incl = count;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) S.tmp[warp] = incl;
+    __syncthreads();
+    uint32_t wpre = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) wpre += (w < warp) ? S.tmp[w] : 0u;
+    const uint32_t tex = wpre + incl - count;
+    S.tile_excl[d] = tex;
+    __syncthreads();
+    // Stage the tile in digit order (over the buffer it arrived in); this
+    // needs only the tile's own offsets, and gives the tiles ahead time to
+    // finish their look-back before this one starts its own.
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) {
+      const int local = warp * (32 * ITEMS) + i * 32 + lane;
+      if (local < tile_n) {
+        const unsigned dd = (unsigned)((key[i] >> shift) & 255u);
+        const uint32_t p = S.tile_excl[dd] + S.whist[warp][dd] + rank[i];
+        S.keys[b][p] = key[i];
+        S.vals[b][p] = val[i];
+      }
+    }
     // Decoupled look-back over the same digit of earlier tiles.  Each status
     // word carries its count, so relaxed loads and stores suffice; LB
     // predecessors are read per round, their loads in flight together, and
     // summed in order up to the nearest inclusive one.
     uint32_t excl = 0;
-    if (tile == 0) {
-      st_relaxed_u32(&stat[d], kStatP | count);
-    } else {
-      st_relaxed_u32(&stat[tile * R + d], kStatA | count);
+    if (tile != 0) {
       constexpr int LB = 8;
       int64_t j = tile - 1;
       unsigned spins = 0;
@@ -294,32 +329,14 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
       }
       st_relaxed_u32(&stat[tile * R + d], kStatP | (excl + count));
     }
-    // Exclusive scan of the tile's counts over digits.
-    uint32_t incl = count;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    if (lane == 31) S.tmp[warp] = incl;
-    __syncthreads();
-    uint32_t wpre = 0;
-#pragma unroll
-    for (int w = 0; w < WARPS; ++w) wpre += (w < warp) ? S.tmp[w] : 0u;
-    const uint32_t tex = wpre + incl - count;
-    S.tile_excl[d] = tex;
     S.gbase[d] = a.plan[kPlanStarts + pass * R + d] + excl - tex;
-    __syncthreads();
-    // Stage the tile in digit order (over the buffer it arrived in).
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-      const int local = warp * (32 * ITEMS) + i * 32 + lane;
-      if (local < tile_n) {
-        const unsigned dd = (unsigned)((key[i] >> shift) & 255u);
-        const uint32_t p = S.tile_excl[dd] + S.whist[warp][dd] + rank[i];
-        S.keys[b][p] = key[i];
-        S.vals[b][p] = val[i];
-      }
+    // claim the next tile once this one's offsets are known (claim order
+    // then follows processing order) and start its copy into the other buffer
+    if (tid == 0) {
+      const int64_t tn = atomicAdd(claim, 1u);
+      S.tile[b ^ 1] = tn;
+      fence_proxy_async_smem();
+      issue(tn, b ^ 1);
     }
     __syncthreads();
     for (int i = tid; i < WARPS * R; i += THREADS) (&S.whist[0][0])[i] = 0;
@@ -388,19 +405,36 @@ __global__ void __launch_bounds__(kGatherThreads) k_radix_gather(
   if (__syncthreads_or(tie) && threadIdx.x == 0) atomicOr(&counters[8], 1u);
 }
 
-// Equal keys: order each run by original index (insertion sort of the run).
+// Equal keys: order each run by original index.  The thread at a run's
+// first sheet finds its end by binary search over the sorted keys; runs of up
+// to kShortRun sheets are insertion-sorted in place, longer ones are listed
+// (start in list_start, length in list_len, count in counters[9]) for
+// k_radix_long_ties, so no thread ever does work quadratic in a run.
+constexpr int64_t kShortRun = 32;
 __global__ void k_radix_ties(StateTable* table, int64_t n, const uint64_t* keys0,
-                             const uint64_t* keys1, const uint32_t* plan,
-                             const uint32_t* counters, const StepFlags* flag) {
+                             const uint64_t* keys1, const uint32_t* plan, uint32_t* counters,
+                             uint32_t* list_start, uint32_t* list_len, const StepFlags* flag) {
   if (!flag->unsorted || !counters[8]) return;
   const int fb = (int)plan[kPlanFinal];
   const uint64_t* keys = fb ? keys1 : keys0;
   const StateRef oth = table->other;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p + 1 < n; p += stride) {
-    if (keys[p] != keys[p + 1] || (p > 0 && keys[p - 1] == keys[p])) continue;
-    int64_t e = p + 1;
-    while (e + 1 < n && keys[e + 1] == keys[p]) ++e;
+    const uint64_t kp = keys[p];
+    if (kp != keys[p + 1] || (p > 0 && keys[p - 1] == kp)) continue;
+    // last index e with keys[e] == kp: keys[p + 1] == kp, keys are sorted
+    int64_t lo = p + 1, hi = n - 1;
+    while (lo < hi) {
+      const int64_t mid = lo + (hi - lo + 1) / 2;
+      if (keys[mid] == kp) lo = mid; else hi = mid - 1;
+    }
+    const int64_t e = lo;
+    if (e - p + 1 > kShortRun) {
+      const unsigned slot = atomicAdd(&counters[9], 1u);
+      list_start[slot] = (uint32_t)p;
+      list_len[slot] = (uint32_t)(e - p + 1);
+      continue;
+    }
     for (int64_t i = p + 1; i <= e; ++i) {
       const double xi = oth.x[i], vi = oth.v[i], mi = oth.m[i];
       const int32_t ii = oth.idx[i];
@@ -417,6 +451,87 @@ __global__ void k_radix_ties(StateTable* table, int64_t n, const uint64_t* keys0
       oth.m[j + 1] = mi;
       oth.idx[j + 1] = ii;
     }
+  }
+}
+
+// Long runs of equal keys, one CTA per run: a stable LSD radix sort (4-bit
+// digits, each thread a contiguous chunk) of (index, place in run) pairs in
+// the key buffers' slots of the run, then the run's sheets are permuted
+// through the current set (free until the flip) and copied back.  Runs
+// already in index order are left alone.  O(run length) work per digit.
+constexpr int kLongTieThreads = 256;
+__global__ void __launch_bounds__(kLongTieThreads) k_radix_long_ties(
+    StateTable* table, int64_t n, uint64_t* bufa, uint64_t* bufb, const uint32_t* counters,
+    const uint32_t* list_start, const uint32_t* list_len, const StepFlags* flag) {
+  if (!flag->unsorted || !counters[9]) return;
+  constexpr int T = kLongTieThreads;
+  __shared__ uint32_t cnt[16][T + 1];
+  __shared__ uint32_t tot[16];
+  const int tid = threadIdx.x;
+  const StateRef oth = table->other, cur = table->cur;
+  int bits = 1;
+  while (bits < 31 && ((int64_t)1 << bits) < n) ++bits;
+  const int npass = (bits + 3) / 4;
+  const unsigned nruns = counters[9];
+  for (unsigned r = blockIdx.x; r < nruns; r += gridDim.x) {
+    const int64_t s = list_start[r], L = list_len[r];
+    bool unordered = false;
+    for (int64_t j = tid; j + 1 < L; j += T) unordered |= oth.idx[s + j] > oth.idx[s + j + 1];
+    if (!__syncthreads_or(unordered)) continue;
+    uint64_t* src = bufa + s;
+    uint64_t* dst = bufb + s;
+    for (int64_t j = tid; j < L; j += T)
+      src[j] = ((uint64_t)(uint32_t)oth.idx[s + j] << 32) | (uint64_t)j;
+    const int64_t chunk = (L + T - 1) / T;
+    const int64_t c_lo = (int64_t)tid * chunk < L ? (int64_t)tid * chunk : L;
+    const int64_t c_hi = c_lo + chunk < L ? c_lo + chunk : L;
+    __syncthreads();
+    for (int ps = 0; ps < npass; ++ps) {
+      const int shift = 32 + 4 * ps;
+#pragma unroll
+      for (int d = 0; d < 16; ++d) cnt[d][tid] = 0;
+      for (int64_t j = c_lo; j < c_hi; ++j) ++cnt[(src[j] >> shift) & 15u][tid];
+      __syncthreads();
+      if (tid < 16) {  // digit-major exclusive offsets of each thread's chunk
+        uint32_t run = 0;
+        for (int t = 0; t < T; ++t) {
+          const uint32_t c = cnt[tid][t];
+          cnt[tid][t] = run;
+          run += c;
+        }
+        tot[tid] = run;
+      }
+      __syncthreads();
+      if (tid < 16) {
+        uint32_t base = 0;
+        for (int d = 0; d < tid; ++d) base += tot[d];
+        for (int t = 0; t < T; ++t) cnt[tid][t] += base;
+      }
+      __syncthreads();
+      for (int64_t j = c_lo; j < c_hi; ++j) {
+        const uint64_t w = src[j];
+        dst[cnt[(w >> shift) & 15u][tid]++] = w;
+      }
+      __syncthreads();
+      uint64_t* t2 = src;
+      src = dst;
+      dst = t2;
+    }
+    for (int64_t j = tid; j < L; j += T) {
+      const int64_t q = s + (int64_t)(uint32_t)src[j];
+      cur.x[s + j] = oth.x[q];
+      cur.v[s + j] = oth.v[q];
+      cur.m[s + j] = oth.m[q];
+      cur.idx[s + j] = oth.idx[q];
+    }
+    __syncthreads();
+    for (int64_t j = tid; j < L; j += T) {
+      oth.x[s + j] = cur.x[s + j];
+      oth.v[s + j] = cur.v[s + j];
+      oth.m[s + j] = cur.m[s + j];
+      oth.idx[s + j] = cur.idx[s + j];
+    }
+    __syncthreads();
   }
 }
 
@@ -512,9 +627,14 @@ void radix_sort_state(StateTable* table, int64_t n, RadixWork* w, const StepFlag
   int g = (int)((n + 255) / 256);
   if (g > 152 * 16) g = 152 * 16;
   if (g < 1) g = 1;
+  // pos[] is free once gathered: it holds the list of long runs
   k_radix_ties<<<g, 256, 0, s>>>(table, n, w->keys[0], w->keys[1], w->plan, w->counters,
-                                 flag);
+                                 w->pos[0], w->pos[1], flag);
+  // and, once the runs are listed, the key buffers are scratch for long ones
+  k_radix_long_ties<<<sms, kLongTieThreads, 0, s>>>(table, n, w->keys[0], w->keys[1],
+                                                    w->counters, w->pos[0], w->pos[1], flag);
   k_radix_flip<<<1, 1, 0, s>>>(table, flag);
 }
 
 }  // namespace wg
+
