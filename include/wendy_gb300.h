@@ -156,6 +156,13 @@ int wg_accel(int64_t n, const double *x, const double *m, double totmass, double
              int ext_kind, const double *ext_params, int n_ext_params, double t, double *a,
              int32_t *perm);
 
+/* out[i] = F(x[i], t) of a registered external force, evaluated on the device
+   by the force kernels' own code (for the pulsed force: the amplitude once,
+   then amp * tanh(x / h) with the integer-pipe tanh).  The device side of the
+   reference's ext_force(x, t) callables, wendy/wendy.py:389-418. */
+int wg_ext_force_eval(int64_t n, const double *x, double t, int ext_kind,
+                      const double *ext_params, int n_ext_params, double *out);
+
 /* Drop-in shape of the reference's step function: same buffers, same
    in/out meaning (xi updated to the new sorted order and positions, x
    de-sorted, v updated, a = accelerations of the last force evaluation in

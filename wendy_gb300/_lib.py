@@ -22,7 +22,7 @@ EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH = 0, 1, 2
 
 # Every symbol include/wendy_gb300.h declares.
 EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", "wg_create",
-           "wg_step", "wg_step_begin", "wg_step_end", "wg_download", "wg_energy", "wg_get_stats", "wg_destroy", "wg_accel",
+           "wg_step", "wg_step_begin", "wg_step_end", "wg_download", "wg_energy", "wg_get_stats", "wg_destroy", "wg_accel", "wg_ext_force_eval",
            "wg_nbody_approx_onestep", "wg_profile", "wg_host_register", "wg_host_unregister",
            "wg_accel_noalloc", "wg_pool_sim_bytes", "wg_pool_create", "wg_pool_add",
            "wg_pool_remove", "wg_pool_step", "wg_pool_download", "wg_pool_info",
@@ -100,6 +100,7 @@ def lib():
     L.wg_get_stats.argtypes = [_P, ctypes.POINTER(WgStats)]
     L.wg_destroy.argtypes = [_P]
     L.wg_accel.argtypes = [_I64, _F64, _F64, _D, _D, _I, _F64, _I, _D, _P, _P]
+    L.wg_ext_force_eval.argtypes = [_I64, _F64, _D, _I, _F64, _I, _F64W]
     L.wg_nbody_approx_onestep.argtypes = [_I, _P, _F64W, _F64W, _F64, _F64W, _D, _D, _I,
                                           ctypes.POINTER(_D), _D, _I, _F64, _I,
                                           ctypes.POINTER(_I), ctypes.POINTER(_D)]

@@ -1170,6 +1170,36 @@ int wg_energy(wg_sim* s, double twopiG, double omega2, double* energy, double* m
   return WG_OK;
 }
 
+int wg_ext_force_eval(int64_t n, const double* x, double t, int ext_kind,
+                      const double* ext_params, int n_ext_params, double* out) {
+  if (n < 1 || !x || !out || !std::isfinite(t)) {
+    set_error("wg_ext_force_eval needs n >= 1, x, out and a finite t");
+    return WG_ERR_ARG;
+  }
+  ExtForce ext;
+  int rc = check_ext(ext_kind, ext_params, n_ext_params, &ext);
+  if (rc) return rc;
+  double* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, 16 * (size_t)n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaMalloc of %zu bytes failed: %s", 16 * (size_t)n, cudaGetErrorString(e));
+    return WG_ERR_NOMEM;
+  }
+  e = cudaMemcpy(d, x, 8 * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    launch_ext_eval(ext, t, d, d + n, n, 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d + n, 8 * (size_t)n, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_error("wg_ext_force_eval failed: %s", cudaGetErrorString(e));
+    return WG_ERR_CUDA;
+  }
+  return WG_OK;
+}
+
 int wg_accel(int64_t n, const double* x, const double* m, double totmass, double omega2,
              int ext_kind, const double* ext_params, int n_ext_params, double t, double* a,
              int32_t* perm) {

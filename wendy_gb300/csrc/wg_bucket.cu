@@ -89,6 +89,7 @@ struct TaskMeta {
   int wlo, whi;   // splitter window [wlo, whi] of the next layout ...
   int wbuf;       // ... in wkey[wbuf], widx[wbuf]
   double amp;     // time factor of a pulsed external force at this sub-step
+  double inv_h;   // 1 / h of a pulsed external force
   uint64_t pm_lo, pm_hi;  // their fixed-point mass
 };
 
@@ -130,7 +131,7 @@ struct StepSmem {
   uint64_t red_min[WARPS], red_max[WARPS];
   TaskMeta next;
   int win_lo, win_hi, cur_wbuf;
-  double amp;
+  double amp, inv_h;
   unsigned long long maxv;
   uint64_t mbar;  // completion of the bucket's bulk copies
 };
@@ -463,8 +464,11 @@ __device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsig
   }
   int64_t j = b - 1;
   PredLoad pl = load_pred(cnt, mass, recs, j - lane);
-  double amp = 0.0;
-  if (lane == 0 && D.ext.kind == EXT_PULSE_TANH) amp = pulse_amplitude(D.ext, D.t_seq[sub]);
+  double amp = 0.0, inv_h = 0.0;
+  if (lane == 0 && D.ext.kind == EXT_PULSE_TANH) {
+    amp = pulse_amplitude(D.ext, D.t_seq[sub]);
+    inv_h = 1.0 / D.ext.p[3];
+  }
   // an earlier sub-step of this call overflowed the simulation: its host
   // side finishes the call on the compact path
   if (ab != 0 && (int)ab <= sub) {
@@ -539,6 +543,7 @@ __device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsig
     out.idx = D.bi[lay];
     out.n = n;
     out.amp = amp;
+    out.inv_h = inv_h;
     out.pm_lo = (uint64_t)pm;
     out.pm_hi = (uint64_t)(pm >> 64);
     out.pcnt = pc;
@@ -616,6 +621,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       S.prefix_mass = (((u128)tm.pm_hi) << 64) | tm.pm_lo;
       S.prefix_cnt = tm.pcnt;
       S.amp = tm.amp;
+      S.inv_h = tm.inv_h;
     }
     {
       // counting-sort bins, cleared while the copies are in flight
@@ -766,7 +772,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
         C += M;
         double acc = fixed_to_double(A, E);
         if (has_omega) acc = fma(-omega2, x, acc);
-        if (ext.kind != EXT_NONE) acc = ext_force_at(ext, S.amp, x) + acc;
+        if (ext.kind != EXT_NONE) acc = ext_force_at(ext, S.amp, S.inv_h, x) + acc;
         const double vn = fma(dt, acc, v);
         const double xn = fma(dt_drift, vn, x);
         S.x[sidx] = xn;

@@ -7,6 +7,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "wg_tanh.cuh"
+
 namespace wg {
 
 typedef unsigned __int128 u128;
@@ -247,11 +249,13 @@ __device__ __forceinline__ double pulse_amplitude(const ExtForce& f, double t) {
   return f.p[0] * exp(-(d * d) / (2.0 * (f.p[2] * f.p[2])));
 }
 
-// F(x, t) given the per-evaluation amplitude `amp` (pulse) -- harmonic:
-// -p0 x; pulse: amp * tanh(x / h).
-__device__ __forceinline__ double ext_force_at(const ExtForce& f, double amp, double x) {
+// F(x, t) given the per-evaluation amplitude `amp` and inv_h = 1 / h (pulse)
+// -- harmonic: -p0 x; pulse: amp * tanh(x / h), as amp * tanh(x * inv_h) with
+// the integer-pipe tanh (wg_tanh.cuh).
+__device__ __forceinline__ double ext_force_at(const ExtForce& f, double amp, double inv_h,
+                                               double x) {
   if (f.kind == EXT_HARMONIC) return -f.p[0] * x;
-  if (f.kind == EXT_PULSE_TANH) return amp * tanh(x / f.p[3]);
+  if (f.kind == EXT_PULSE_TANH) return amp * tanh_fixed(x * inv_h);
   return 0.0;
 }
 

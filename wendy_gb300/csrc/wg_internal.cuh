@@ -93,6 +93,8 @@ void launch_init_state(StateTable* table, int64_t n, cudaStream_t s);
 // receives sum m v^2/2, sum m x^2/2, -sum m x a, sum m v; scratch holds
 // 4 (kEnergyBlocks + 1) doubles.
 constexpr int kEnergyBlocks = 152 * 4;
+void launch_ext_eval(const ExtForce& f, double t, const double* x, double* out, int64_t n,
+                     cudaStream_t s);
 void launch_energy(const StateTable* table, int64_t n, const double* a_sorted, double* scratch,
                    cudaStream_t s);
 

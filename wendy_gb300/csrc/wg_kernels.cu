@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_force_kick_drift(const ForceArgs
   __shared__ unsigned s_tile;
   __shared__ u128 s_warp[WARPS];
   __shared__ u128 s_prefix;
-  __shared__ double s_amp;
+  __shared__ double s_amp, s_inv_h;
   __shared__ uint64_t s_first[WARPS + 1];
   __shared__ unsigned s_unsorted;
   __shared__ unsigned long long s_maxv;
@@ -102,6 +102,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_force_kick_drift(const ForceArgs
     s_maxv = 0;
     s_epoch = a.epochs[a.sub];
     s_amp = (a.ext.kind == EXT_PULSE_TANH) ? pulse_amplitude(a.ext, a.t_seq[a.sub]) : 0.0;
+    s_inv_h = (a.ext.kind == EXT_PULSE_TANH) ? 1.0 / a.ext.p[3] : 0.0;
   }
   __syncthreads();
   const int64_t tile = s_tile;
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_force_kick_drift(const ForceArgs
   const u128 tprefix = s_prefix + s_warp[warp] + (incl - tot);
 
   const i128 T = (i128)((((u128)a.T_hi) << 64) | a.T_lo);
-  const double amp = s_amp;
+  const double amp = s_amp, inv_h = s_inv_h;
   unsigned long long maxv = 0;
   bool unsorted = false;
   uint64_t first_key = ~0ull, last_key = 0, prev_key = 0;
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_force_kick_drift(const ForceArgs
     const i128 A = T - 2 * C - (i128)M;
     double acc = fixed_to_double(A, a.E);
     if (a.has_omega) acc = fma(-a.omega2, x[i], acc);
-    if (a.ext.kind != EXT_NONE) acc = ext_force_at(a.ext, amp, x[i]) + acc;
+    if (a.ext.kind != EXT_NONE) acc = ext_force_at(a.ext, amp, inv_h, x[i]) + acc;
     const double vn = fma(a.dt_kick, acc, v[i]);
     const double xn = fma(a.dt_drift, vn, x[i]);
     v[i] = vn;
@@ -319,6 +320,25 @@ void launch_desort(const StateTable* table, int64_t n, double* x_out, double* v_
 void launch_scatter_accel(const StateTable* table, int64_t n, const double* a_sorted,
                           double* a_orig, cudaStream_t s) {
   k_scatter_accel<<<grid_for(n, 256), 256, 0, s>>>(table, n, a_sorted, a_orig);
+}
+
+// F(x_i, t) of a registered external force, with the force kernels' code:
+// amplitude and 1 / h once per block, then ext_force_at per position.
+__global__ void k_ext_eval(const ExtForce f, double t, const double* x, double* out, int64_t n) {
+  __shared__ double s_amp, s_inv_h;
+  if (threadIdx.x == 0) {
+    s_amp = f.kind == EXT_PULSE_TANH ? pulse_amplitude(f, t) : 0.0;
+    s_inv_h = f.kind == EXT_PULSE_TANH ? 1.0 / f.p[3] : 0.0;
+  }
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    out[i] = ext_force_at(f, s_amp, s_inv_h, x[i]);
+}
+
+void launch_ext_eval(const ExtForce& f, double t, const double* x, double* out, int64_t n,
+                     cudaStream_t s) {
+  k_ext_eval<<<grid_for(n, 256), 256, 0, s>>>(f, t, x, out, n);
 }
 
 // Sums of the energy and momentum diagnostics over the sorted state, with

@@ -51,6 +51,20 @@ class PulseTanh(RegisteredForce):
         return self.A * numpy.exp(-(t - self.t0) ** 2 / (2 * self.tau ** 2)) * numpy.tanh(x / self.h)
 
 
+def evaluate_on_device(ext_force, x, t):
+    """F(x, t) of a registered force evaluated on the GPU by the force
+    kernels' own code (wg_ext_force_eval): the device counterpart of calling
+    the force object itself."""
+    from . import _lib
+    kind, params = resolve(ext_force)
+    x = numpy.ascontiguousarray(x, dtype=numpy.float64)
+    out = numpy.empty(len(x))
+    _lib.check(_lib.lib().wg_ext_force_eval(len(x), x, float(t), int(kind),
+                                            _lib.ext_params(params), len(params), out),
+               "wg_ext_force_eval")
+    return out
+
+
 def resolve(ext_force):
     """(kind, params) for the C ABI; rejects anything that is not registered."""
     if ext_force is None:
