@@ -28,10 +28,10 @@ def test_tanh_constants_are_correctly_rounded():
     ln2 = Decimal(2).ln()
     q62 = Decimal(2) ** 62
     src = _header()
-    table = src[src.index("kExp2Tab[64]"):src.index("};", src.index("kExp2Tab[64]"))]
+    table = src[src.index("kExp2Tab[256]"):src.index("};", src.index("kExp2Tab[256]"))]
     tab = [int(h, 16) for h in re.findall(r"0x([0-9a-f]{16})ull", table)]
-    assert tab == [int((q62 * (-(Decimal(j) / 64) * ln2).exp()).to_integral_value())
-                   for j in range(64)]
+    assert tab == [int((q62 * (-(Decimal(j) / 256) * ln2).exp()).to_integral_value())
+                   for j in range(256)]
     body = src[src.index("inv_fact_q62(int n)"):src.index("kLn2Q64")]
     fact = [int(h, 16) for h in re.findall(r"0x([0-9a-f]{16})ull", body)]
     want = [int((q62 / Decimal(f)).to_integral_value()) for f in (1, 2, 6, 24, 120, 720, 5040)]
