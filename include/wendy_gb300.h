@@ -163,12 +163,20 @@ int wg_accel(int64_t n, const double *x, const double *m, double totmass, double
 int wg_ext_force_eval(int64_t n, const double *x, double t, int ext_kind,
                       const double *ext_params, int n_ext_params, double *out);
 
+/* Counters of the state behind wg_nbody_approx_onestep (all zero before its
+   first call).  A call handed back exactly the previous call's outputs, with
+   the same masses and total, resumes from the resident sorted state and adds
+   no full sort; any other call loads, sorts and lays out the sheets anew. */
+int wg_nbody_approx_stats(wg_stats *out);
+
 /* Drop-in shape of the reference's step function: same buffers, same
    in/out meaning (xi updated to the new sorted order and positions, x
    de-sorted, v updated, a = accelerations of the last force evaluation in
    original order, *t0 advanced), with the external force given as a
    registered id instead of a function pointer.  Every call uploads its
-   inputs and downloads its outputs.
+   inputs and downloads its outputs; a call whose inputs are bit for bit the
+   previous call's outputs (the reference's generator loop) continues from
+   the resident state instead of re-sorting it, with identical results.
    Reference: _wendy_nbody_approx_onestep, wendy/wendy.c:385-418 and its
    argtypes at wendy/wendy.py:76-93. */
 int wg_nbody_approx_onestep(int n, wg_sheet *xi, double *x, double *v, const double *m,

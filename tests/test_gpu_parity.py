@@ -18,6 +18,7 @@ import wendy_gb300
 from oracle import oracle as O
 from wendy_gb300 import _lib, ics
 from wendy_gb300.extforce import Harmonic, PulseTanh
+from wendy_gb300.wendy import approx_onestep_stats
 
 pytestmark = pytest.mark.gpu
 
@@ -109,6 +110,40 @@ def test_dropin_unordered_coincident_sheets(n, ntied):
     ra = numpy.empty(n)
     ra[srt] = tot - 2 * cm - m[srt]
     assert numpy.max(numpy.abs(a - ra)) <= 1e-12 * _scale(ra, tot)
+
+
+def test_dropin_resumes_from_resident_state_with_identical_results():
+    # The reference's generator hands each call the previous call's outputs
+    # (wendy/wendy.py:425-437): such calls continue from the resident sorted
+    # state.  The same calls with xi handed over in another order are loaded
+    # and sorted anew; both give the same bits.
+    n = 200000
+    x, v, m = ics.sech2_disk(n, seed=21, masses="lognormal")
+    tot = float(numpy.sum(m))
+
+    def run(reorder):
+        xi = numpy.zeros(n, dtype=_lib.SHEET_DTYPE)
+        xi["idx"] = numpy.arange(n, dtype=numpy.int32)
+        xi["val"] = x
+        xx, vv, a = x.copy(), v.copy(), numpy.zeros(n)
+        t = 0.0
+        outs = []
+        for k in range(4):
+            if reorder:
+                xi = xi[::-1].copy()
+            t, _el = wendy_gb300.approx_onestep(xi, xx, vv, m, a, tot, 0.002, 5, t, 1.21)
+            outs.append((xx.copy(), vv.copy(), a.copy(), xi.copy()))
+            if k == 0:  # the first call (re)builds the resident state
+                s0 = approx_onestep_stats()["sorts_full"]
+        return outs, approx_onestep_stats()["sorts_full"] - s0
+
+    resumed, sorts_resumed = run(False)
+    reloaded, sorts_reloaded = run(True)
+    assert sorts_resumed == 0 and sorts_reloaded == 3
+    for (xa, va, aa, xia), (xb, vb, ab, xib) in zip(resumed, reloaded):
+        assert numpy.array_equal(xa, xb) and numpy.array_equal(va, vb)
+        assert numpy.array_equal(aa, ab)
+        assert numpy.array_equal(xia["idx"], xib["idx"]) and numpy.array_equal(xia["val"], xib["val"])
 
 
 def test_accel_at_large_n_equal_masses_is_exact():

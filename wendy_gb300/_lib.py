@@ -23,7 +23,7 @@ EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH = 0, 1, 2
 # Every symbol include/wendy_gb300.h declares.
 EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", "wg_create",
            "wg_step", "wg_step_begin", "wg_step_end", "wg_download", "wg_energy", "wg_get_stats", "wg_destroy", "wg_accel", "wg_ext_force_eval",
-           "wg_nbody_approx_onestep", "wg_profile", "wg_host_register", "wg_host_unregister",
+           "wg_nbody_approx_onestep", "wg_nbody_approx_stats", "wg_profile", "wg_host_register", "wg_host_unregister",
            "wg_accel_noalloc", "wg_pool_sim_bytes", "wg_pool_create", "wg_pool_add",
            "wg_pool_remove", "wg_pool_step", "wg_pool_download", "wg_pool_info",
            "wg_pool_destroy", "wg_set_tuning", "wg_get_tuning")
@@ -98,6 +98,7 @@ def lib():
     L.wg_download.argtypes = [_P, _P, _P]
     L.wg_energy.argtypes = [_P, _D, _D, ctypes.POINTER(_D), ctypes.POINTER(_D)]
     L.wg_get_stats.argtypes = [_P, ctypes.POINTER(WgStats)]
+    L.wg_nbody_approx_stats.argtypes = [ctypes.POINTER(WgStats)]
     L.wg_destroy.argtypes = [_P]
     L.wg_accel.argtypes = [_I64, _F64, _F64, _D, _D, _I, _F64, _I, _D, _P, _P]
     L.wg_ext_force_eval.argtypes = [_I64, _F64, _D, _I, _F64, _I, _F64W]

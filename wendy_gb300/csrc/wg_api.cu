@@ -114,8 +114,18 @@ struct wg_sim {
   double* t_seq = nullptr;       // [cap]
   unsigned* epochs = nullptr;    // [cap]
   void* stage = nullptr;         // staging of the reference-layout entry point
-  wg_sheet* stage_xi = nullptr;
+  wg_sheet* stage_xi = nullptr;  // its xi output (the last sub-step's sorted order)
   double* stage_a = nullptr;
+  wg_sheet* in_xi = nullptr;     // its inputs, uploaded every call
+  double* in_v = nullptr;
+  double* in_m = nullptr;
+  double* prev_m = nullptr;      // the masses of the previous call
+  unsigned* d_diff = nullptr;    // set when this call's inputs differ from the last outputs
+  // the previous call ended with the sheets in buckets routed for the next
+  // opening half drift; a call handed back exactly its outputs (and the
+  // same masses and total) resumes from there
+  bool resume_ok = false;
+  double resume_totmass = 0;
   double* h_t = nullptr;         // pinned host mirrors
   unsigned* h_ep = nullptr;
   StepFlags* h_flags = nullptr;
@@ -566,6 +576,23 @@ void fill_times(wg_sim* s, double dt, int nleap, double* t0) {
 // Cache of one simulation for the stateless reference-shaped entry point.
 std::mutex g_cache_mu;
 wg_sim* g_cache = nullptr;
+
+// Whether the drop-in's inputs are, bit for bit, the previous call's
+// outputs (xi, v) and masses: then the resident bucket state is the state
+// they describe.
+__global__ void k_inputs_differ(int64_t n, const wg_sheet* xi, const wg_sheet* xi_prev,
+                                const double* v, const double* v_prev, const double* m,
+                                const double* m_prev, unsigned* diff) {
+  bool d = false;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    d |= xi[i].idx != xi_prev[i].idx ||
+         __double_as_longlong(xi[i].val) != __double_as_longlong(xi_prev[i].val) ||
+         __double_as_longlong(v[i]) != __double_as_longlong(v_prev[i]) ||
+         __double_as_longlong(m[i]) != __double_as_longlong(m_prev[i]);
+  }
+  if (__syncthreads_or(d) && threadIdx.x == 0) atomicOr(diff, 1u);
+}
 
 __global__ void k_load_sheets(StateTable* table, int64_t n, const wg_sheet* xi, const double* v,
                               const double* m) {
@@ -1239,6 +1266,17 @@ int wg_accel(int64_t n, const double* x, const double* m, double totmass, double
   return rc;
 }
 
+int wg_nbody_approx_stats(wg_stats* out) {
+  if (!out) {
+    set_error("null output");
+    return WG_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_cache_mu);
+  *out = wg_stats{};
+  if (g_cache) *out = g_cache->st;
+  return WG_OK;
+}
+
 int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const double* m,
                             double* a, double totmass, double dt, int nleap, double* t0,
                             double omega2, int ext_kind, const double* ext_params,
@@ -1277,30 +1315,51 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   rc = alloc_call_arrays(s, nleap);
   if (rc) return rc;
   if (!s->stage) {
-    const size_t b = al(sizeof(wg_sheet) * (size_t)n) + al(8 * (size_t)n);
+    const size_t bx = al(sizeof(wg_sheet) * (size_t)n), bd = al(8 * (size_t)n);
+    const size_t b = 2 * bx + 4 * bd + al(16);
     WG_CUDA(cudaMalloc(&s->stage, b));
-    s->stage_xi = static_cast<wg_sheet*>(s->stage);
-    s->stage_a = reinterpret_cast<double*>(static_cast<char*>(s->stage) +
-                                           al(sizeof(wg_sheet) * (size_t)n));
+    char* q = static_cast<char*>(s->stage);
+    s->stage_xi = reinterpret_cast<wg_sheet*>(q); q += bx;
+    s->in_xi = reinterpret_cast<wg_sheet*>(q); q += bx;
+    s->stage_a = reinterpret_cast<double*>(q); q += bd;
+    s->in_v = reinterpret_cast<double*>(q); q += bd;
+    s->in_m = reinterpret_cast<double*>(q); q += bd;
+    s->prev_m = reinterpret_cast<double*>(q); q += bd;
+    s->d_diff = reinterpret_cast<unsigned*>(q);
     s->st.device_bytes += (int64_t)b;
+    s->resume_ok = false;
   }
-  // v and m arrive in original order; the desort buffers hold them until the
-  // sheets are loaded into sorted-state layout.
-  wg_sheet* d_xi = s->stage_xi;
-  double* d_v = s->x_out;
-  double* d_m = s->v_out;
-  StateTable t0tab;
-  t0tab.cur = s->set[0];
-  t0tab.other = s->set[1];
   WG_CUDA(cudaEventRecord(s->ev0, s->stream));
-  WG_CUDA(cudaMemcpyAsync(s->table, &t0tab, sizeof(t0tab), cudaMemcpyHostToDevice, s->stream));
-  WG_CUDA(cudaMemcpyAsync(d_xi, xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
-  WG_CUDA(cudaMemcpyAsync(d_v, v, 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
-  WG_CUDA(cudaMemcpyAsync(d_m, m, 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
-  k_load_sheets<<<152 * 8, 256, 0, s->stream>>>(s->table, n, d_xi, d_v, d_m);
-  // the sheets are compact with the opening half drift pending: run the call
-  // on the bucket path, which also leaves xi (last sort order) and a
-  s->mode = 0;
+  WG_CUDA(cudaMemcpyAsync(s->in_xi, xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->in_v, v, 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->in_m, m, 8 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+  // The previous call left the sheets in buckets routed for this call's
+  // opening half drift.  If this call's inputs are bit for bit that call's
+  // outputs (xi, v) with the same masses and total, that state is the state
+  // they describe and the call resumes from it: no load, re-sort or
+  // re-bucketing.  Otherwise the sheets are loaded in xi's order and sorted.
+  bool resume = s->resume_ok && s->mode == 1 &&
+                std::memcmp(&totmass, &s->resume_totmass, sizeof(double)) == 0;
+  s->resume_ok = false;
+  if (resume) {
+    WG_CUDA(cudaMemsetAsync(s->d_diff, 0, 4, s->stream));
+    k_inputs_differ<<<152 * 8, 256, 0, s->stream>>>(n, s->in_xi, s->stage_xi, s->in_v, s->v_out,
+                                                     s->in_m, s->prev_m, s->d_diff);
+    WG_CUDA(cudaMemcpyAsync(s->h_ab, s->d_diff, 4, cudaMemcpyDeviceToHost, s->stream));
+    WG_CUDA(cudaStreamSynchronize(s->stream));
+    resume = s->h_ab[0] == 0;
+  }
+  if (!resume) {
+    StateTable t0tab;
+    t0tab.cur = s->set[0];
+    t0tab.other = s->set[1];
+    WG_CUDA(cudaMemcpyAsync(s->table, &t0tab, sizeof(t0tab), cudaMemcpyHostToDevice, s->stream));
+    k_load_sheets<<<152 * 8, 256, 0, s->stream>>>(s->table, n, s->in_xi, s->in_v, s->in_m);
+    // the sheets are compact with the opening half drift pending: the call
+    // sorts them and runs on the bucket path
+    s->mode = 0;
+  }
+  wg_sheet* const d_xi = s->stage_xi;  // the xi output (last sort order), also the next comparison
   s->call_xi = reinterpret_cast<SheetRec*>(d_xi);
   s->call_a = s->stage_a;
   rc = run_call(s, dt, nleap, t0, time_elapsed, false);
@@ -1319,6 +1378,10 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   WG_CUDA(cudaMemcpyAsync(v, s->v_out, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
   WG_CUDA(cudaMemcpyAsync(a, s->stage_a, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
   WG_CUDA(cudaStreamSynchronize(s->stream));
+  // this call's masses are the next call's reference
+  std::swap(s->in_m, s->prev_m);
+  s->resume_ok = s->mode == 1;
+  s->resume_totmass = totmass;
   if (rc && err) *err = rc;
   return rc;
 }

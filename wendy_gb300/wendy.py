@@ -201,3 +201,12 @@ def approx_onestep(xi, x, v, m, a, totmass, dt, nleap, t0, omega2=-1., ext_force
                                          ctypes.byref(err), ctypes.byref(el)),
                "wg_nbody_approx_onestep")
     return tc.value, el.value
+
+
+def approx_onestep_stats():
+    """Counters of the state behind approx_onestep (wg_nbody_approx_stats):
+    a call handed back exactly the previous call's outputs resumes from the
+    resident sorted state and adds no full sort."""
+    st = _lib.WgStats()
+    _lib.check(_lib.lib().wg_nbody_approx_stats(ctypes.byref(st)), "wg_nbody_approx_stats")
+    return {k: getattr(st, k) for k, _ in st._fields_}
