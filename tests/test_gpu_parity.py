@@ -115,8 +115,10 @@ def test_dropin_unordered_coincident_sheets(n, ntied):
 def test_dropin_resumes_from_resident_state_with_identical_results():
     # The reference's generator hands each call the previous call's outputs
     # (wendy/wendy.py:425-437): such calls continue from the resident sorted
-    # state.  The same calls with xi handed over in another order are loaded
-    # and sorted anew; both give the same bits.
+    # state (after one that did, the next computes while its inputs are
+    # compared, and is redone if they differ).  The same calls with xi
+    # handed over in another order are loaded and sorted anew; both give the
+    # same bits.  The 5th call changes one velocity after resumed calls.
     n = 200000
     x, v, m = ics.sech2_disk(n, seed=21, masses="lognormal")
     tot = float(numpy.sum(m))
@@ -126,21 +128,24 @@ def test_dropin_resumes_from_resident_state_with_identical_results():
         xi["idx"] = numpy.arange(n, dtype=numpy.int32)
         xi["val"] = x
         xx, vv, a = x.copy(), v.copy(), numpy.zeros(n)
-        t = 0.0
+        t = 4.2
         outs = []
-        for k in range(4):
+        for k in range(6):
             if reorder:
                 xi = xi[::-1].copy()
-            t, _el = wendy_gb300.approx_onestep(xi, xx, vv, m, a, tot, 0.002, 5, t, 1.21)
-            outs.append((xx.copy(), vv.copy(), a.copy(), xi.copy()))
+            if k == 4:
+                vv[7] *= 1.0001
+            t, _el = wendy_gb300.approx_onestep(xi, xx, vv, m, a, tot, 0.002, 5, t, 1.21, PULSE)
+            outs.append((t, xx.copy(), vv.copy(), a.copy(), xi.copy()))
             if k == 0:  # the first call (re)builds the resident state
                 s0 = approx_onestep_stats()["sorts_full"]
         return outs, approx_onestep_stats()["sorts_full"] - s0
 
     resumed, sorts_resumed = run(False)
     reloaded, sorts_reloaded = run(True)
-    assert sorts_resumed == 0 and sorts_reloaded == 3
-    for (xa, va, aa, xia), (xb, vb, ab, xib) in zip(resumed, reloaded):
+    assert sorts_resumed == 1 and sorts_reloaded == 5
+    for (ta, xa, va, aa, xia), (tb, xb, vb, ab, xib) in zip(resumed, reloaded):
+        assert ta == tb
         assert numpy.array_equal(xa, xb) and numpy.array_equal(va, vb)
         assert numpy.array_equal(aa, ab)
         assert numpy.array_equal(xia["idx"], xib["idx"]) and numpy.array_equal(xia["val"], xib["val"])
