@@ -11,6 +11,8 @@ Tolerances (FP64 throughout):
   * long runs: the maximum relative energy error matches the reference's
     within 10 %.
 """
+import ctypes
+
 import numpy
 import pytest
 
@@ -110,6 +112,34 @@ def test_dropin_unordered_coincident_sheets(n, ntied):
     ra = numpy.empty(n)
     ra[srt] = tot - 2 * cm - m[srt]
     assert numpy.max(numpy.abs(a - ra)) <= 1e-12 * _scale(ra, tot)
+
+
+@pytest.mark.parametrize("copies", [5, 20])
+def test_bucket_step_orders_coincident_sheets_by_index(copies):
+    # Groups of `copies` sheets at one position: inside a bucket they share a
+    # counting-sort bin (up to 8: ordered by one thread; more: by the block).
+    # v = 0, so one sub-step's velocities are dt times the force in
+    # (position, index) order (reference formula, wendy/wendy.c:371-383).
+    n = 1 << 18
+    rng = numpy.random.default_rng(copies)
+    levels = n // copies
+    x = (rng.integers(0, levels, n) - levels / 2) * (4.0 / levels)
+    v = numpy.zeros(n)
+    m = rng.lognormal(0., 0.5, n)
+    tot = float(numpy.sum(m))
+    dt = 1e-3
+    sim = wendy_gb300.Simulation(x, v, m, tot, 1.21)
+    t = ctypes.c_double(0.)
+    sim.step(dt, 1, t)
+    assert sim.stats()["sorts_window"] == 1  # the sub-step ran on buckets
+    gx, gv = numpy.empty(n), numpy.empty(n)
+    sim.download(gx, gv)
+    sim.close()
+    order = numpy.argsort(x, kind="stable")
+    cm = numpy.concatenate(([0.], numpy.cumsum(m[order])[:-1]))
+    a = numpy.empty(n)
+    a[order] = tot - 2 * cm - m[order] - 1.21 * x[order]
+    assert numpy.max(numpy.abs(gv - dt * a)) <= 1e-12 * dt * _scale(a, tot)
 
 
 def test_dropin_resumes_from_resident_state_with_identical_results():

@@ -104,6 +104,7 @@ struct StepSmem {
       uint32_t bins[NBIN_PAD];
       uint64_t skey[CAP];  // key and index of each position in bin order
       int32_t sidx[CAP];
+      uint32_t nlong;      // bins too full for one thread's insertion sort
     } srt;
     LsdSmem lsd;
     struct {
@@ -283,6 +284,7 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
   uint32_t* bins = S.u.srt.bins;
   uint64_t* skey = S.u.srt.skey;
   int32_t* sidx = S.u.srt.sidx;
+  if (tid == 0) S.u.srt.nlong = 0;  // read after the barriers below
   uint16_t qv[MAXI], rk[MAXI];
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
@@ -333,24 +335,66 @@ __device__ __forceinline__ void bucket_sort(StepSmem& S, int n, int ipt, uint64_
     }
   }
   __syncthreads();
-  // The order inside a bin came from atomics: every sheet of a bin with two
-  // or more counts the sheets of its bin that precede it in (key, idx) order,
-  // on the keys and indices laid out in bin order, and takes that place.
-  // Only perm is written here, each place by exactly one sheet.
+  // The order inside a bin came from atomics.  A bin holds two or more
+  // sheets exactly when one of them took rank 1 in it: that sheet puts the
+  // bin's few places in (key, idx) order, an insertion sort of their keys,
+  // indices and slots in shared memory; every other sheet has nothing to do.
+  // Bins of more than kOwnerSort sheets (rare) are counted and then ordered by
+  // the whole block, each of their sheets counting the bin-mates that precede
+  // it (owners never touch those bins).
+  constexpr uint32_t kOwnerSort = 8;
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
     const int j = tid + i * BT;
+    if (i < ipt && j < n && rk[i] == 1) {
+      const uint32_t lo = bin_get(bins, qv[i]), hi = bin_get(bins, qv[i] + 1);
+      if (hi - lo <= kOwnerSort) {
+        for (uint32_t a = lo + 1; a < hi; ++a) {
+          const uint64_t ka = skey[a];
+          const int32_t ia = sidx[a];
+          const uint16_t pa = S.perm[a];
+          uint32_t b = a;
+          while (b > lo && pair_less(ka, ia, skey[b - 1], sidx[b - 1])) {
+            skey[b] = skey[b - 1];
+            sidx[b] = sidx[b - 1];
+            S.perm[b] = S.perm[b - 1];
+            --b;
+          }
+          skey[b] = ka;
+          sidx[b] = ia;
+          S.perm[b] = pa;
+        }
+      } else {
+        atomicAdd(&S.u.srt.nlong, 1u);
+      }
+    }
+  }
+  __syncthreads();
+  if (S.u.srt.nlong == 0) return;
+  // the full bins: each of their sheets counts the sheets of its bin that
+  // precede it, then takes that place (keys and indices read-only here)
+  uint32_t place[MAXI];
+  uint16_t slot[MAXI];
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i) {
+    place[i] = 0xffffffffu;
+    const int j = tid + i * BT;
     if (i < ipt && j < n) {
       const uint32_t lo = bin_get(bins, qv[i]), hi = bin_get(bins, qv[i] + 1);
-      if (hi - lo > 1) {
+      if (hi - lo > kOwnerSort) {
         const uint64_t kj = skey[lo + rk[i]];
         const int32_t ij = sidx[lo + rk[i]];
         uint32_t r = 0;
         for (uint32_t b = lo; b < hi; ++b) r += pair_less(skey[b], sidx[b], kj, ij) ? 1u : 0u;
-        S.perm[lo + r] = (uint16_t)j;
+        place[i] = lo + r;
+        slot[i] = (uint16_t)j;
       }
     }
   }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i)
+    if (place[i] != 0xffffffffu) S.perm[place[i]] = slot[i];
   __syncthreads();
 }
 
