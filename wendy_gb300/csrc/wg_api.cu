@@ -113,24 +113,36 @@ struct wg_sim {
   unsigned* tickets = nullptr;   // [cap]
   double* t_seq = nullptr;       // [cap]
   unsigned* epochs = nullptr;    // [cap]
-  void* stage = nullptr;         // staging of the reference-layout entry point
-  wg_sheet* stage_xi = nullptr;  // its xi output (the last sub-step's sorted order)
-  double* stage_a = nullptr;
-  wg_sheet* in_xi = nullptr;     // its inputs, uploaded every call
+  // The reference-layout entry point (wg_nbody_approx_onestep): two output
+  // sets (xi in the last sub-step's sorted order, x, v, a in original order)
+  // used alternately, its inputs uploaded every call, and the masses of the
+  // previous call.
+  void* stage = nullptr;
+  struct OutSet {
+    wg_sheet* xi = nullptr;
+    double *x = nullptr, *v = nullptr, *a = nullptr;
+  } outs[2];
+  int out_last = 0;              // the set returned by the previous call
+  wg_sheet* in_xi = nullptr;
   double* in_v = nullptr;
   double* in_m = nullptr;
-  wg_sheet* prev_xi = nullptr;   // the previous call's outputs and masses
-  double* prev_v = nullptr;
   double* prev_m = nullptr;
-  unsigned* d_diff = nullptr;    // set when this call's inputs differ from them
-  cudaStream_t up_stream = nullptr;  // uploads and the comparison
+  unsigned* d_diff = nullptr;    // set when this call's inputs differ from those outputs
+  cudaStream_t up_stream = nullptr;    // uploads and the comparison
+  cudaStream_t down_stream = nullptr;  // downloads of the outputs
   cudaEvent_t ev_up = nullptr;
-  // the previous call ended with the sheets in buckets routed for the next
-  // opening half drift; a call handed back exactly its outputs (and the
-  // same masses and total) resumes from there
+  // The previous call ended with the sheets in buckets routed for the next
+  // opening half drift (resume_ok); a call handed back exactly its outputs
+  // (and the same masses and total) continues from there.  After such a
+  // call, the next one's sub-steps are enqueued at once (spec_*), assuming
+  // the same scalars and the outputs as inputs; the next call checks both.
   bool resume_ok = false;
   double resume_totmass = 0;
-  int resume_streak = 0;         // consecutive calls that resumed
+  bool spec_enabled = true;
+  bool spec_pending = false;
+  int spec_set = 0, spec_nleap = 0;
+  double spec_dt = 0, spec_t0_in = 0, spec_t0_out = 0, spec_totmass = 0, spec_omega2 = 0;
+  ExtForce spec_ext{};
   double* h_t = nullptr;         // pinned host mirrors
   unsigned* h_ep = nullptr;
   StepFlags* h_flags = nullptr;
@@ -240,11 +252,13 @@ void free_sim(wg_sim* s) {
   if (s->h_flags) cudaFreeHost(s->h_flags);
   if (s->h_ab) cudaFreeHost(s->h_ab);
   if (s->up_stream) cudaStreamSynchronize(s->up_stream);
+  if (s->down_stream) cudaStreamSynchronize(s->down_stream);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->ev_up) cudaEventDestroy(s->ev_up);
   if (s->stream) cudaStreamDestroy(s->stream);
   if (s->up_stream) cudaStreamDestroy(s->up_stream);
+  if (s->down_stream) cudaStreamDestroy(s->down_stream);
   delete s;
 }
 
@@ -1306,6 +1320,40 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
     if (rc) return rc;
     g_cache = s;
   }
+  auto bits_eq = [](double p, double q) { return std::memcmp(&p, &q, sizeof(double)) == 0; };
+  auto point_at = [&](int set) {
+    wg_sim::OutSet& o = s->outs[set];
+    s->x_out = o.x;
+    s->v_out = o.v;
+    s->call_xi = reinterpret_cast<SheetRec*>(o.xi);
+    s->call_a = o.a;
+  };
+  auto clear_call = [&]() {
+    s->call_xi = nullptr;
+    s->call_a = nullptr;
+  };
+  // The sub-steps the previous call enqueued for this one are usable only
+  // with this call's scalars; otherwise they are completed and dropped first
+  // (they hold the per-call arrays and the physics).
+  auto drop_spec = [&]() {
+    point_at(s->spec_set);
+    double ignored = 0;
+    run_call_end(s, &ignored);
+    clear_call();
+    s->spec_pending = false;
+    s->spec_enabled = false;
+  };
+  bool spec = s->spec_pending;
+  if (spec) {
+    const bool same = t0 && bits_eq(dt, s->spec_dt) && nleap == s->spec_nleap &&
+                      bits_eq(*t0, s->spec_t0_in) && bits_eq(totmass, s->spec_totmass) &&
+                      bits_eq(omega2, s->spec_omega2) &&
+                      std::memcmp(&ext, &s->spec_ext, sizeof(ExtForce)) == 0;
+    if (!same) {
+      drop_spec();
+      spec = false;
+    }
+  }
   // physics of this call
   s->totmass = totmass;
   s->omega2 = omega2;
@@ -1324,102 +1372,90 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   if (rc) return rc;
   if (!s->stage) {
     const size_t bx = al(sizeof(wg_sheet) * (size_t)n), bd = al(8 * (size_t)n);
-    const size_t b = 3 * bx + 5 * bd + al(16);
+    const size_t b = 3 * bx + 9 * bd + al(16);
     WG_CUDA(cudaMalloc(&s->stage, b));
     char* q = static_cast<char*>(s->stage);
-    s->stage_xi = reinterpret_cast<wg_sheet*>(q); q += bx;
-    s->prev_xi = reinterpret_cast<wg_sheet*>(q); q += bx;
+    for (int k = 0; k < 2; ++k) {
+      s->outs[k].xi = reinterpret_cast<wg_sheet*>(q); q += bx;
+      s->outs[k].x = reinterpret_cast<double*>(q); q += bd;
+      s->outs[k].v = reinterpret_cast<double*>(q); q += bd;
+      s->outs[k].a = reinterpret_cast<double*>(q); q += bd;
+    }
     s->in_xi = reinterpret_cast<wg_sheet*>(q); q += bx;
-    s->stage_a = reinterpret_cast<double*>(q); q += bd;
     s->in_v = reinterpret_cast<double*>(q); q += bd;
     s->in_m = reinterpret_cast<double*>(q); q += bd;
     s->prev_m = reinterpret_cast<double*>(q); q += bd;
-    s->prev_v = reinterpret_cast<double*>(q); q += bd;
     s->d_diff = reinterpret_cast<unsigned*>(q);
     s->st.device_bytes += (int64_t)b;
     WG_CUDA(cudaStreamCreateWithFlags(&s->up_stream, cudaStreamNonBlocking));
+    WG_CUDA(cudaStreamCreateWithFlags(&s->down_stream, cudaStreamNonBlocking));
     WG_CUDA(cudaEventCreateWithFlags(&s->ev_up, cudaEventDisableTiming));
     s->resume_ok = false;
-    s->resume_streak = 0;
   }
-  // The previous call left the sheets in buckets routed for this call's
-  // opening half drift.  If this call's inputs are bit for bit that call's
-  // outputs (xi, v) with the same masses and total, that state is the state
-  // they describe and the call resumes from it: no load, re-sort or
-  // re-bucketing.  The inputs are uploaded and compared on a second stream;
-  // after a call that resumed, the next one computes from the resident state
-  // meanwhile (it does not read the inputs) and is redone from the inputs
-  // if they turn out to differ.  Otherwise the sheets are loaded in xi's
-  // order and sorted.
-  const bool candidate = s->resume_ok && s->mode == 1 &&
-                         std::memcmp(&totmass, &s->resume_totmass, sizeof(double)) == 0;
-  const bool speculate = candidate && s->resume_streak > 0;
-  s->resume_ok = false;
-  if (candidate) {
-    // the previous outputs become the reference; this call writes fresh buffers
-    std::swap(s->stage_xi, s->prev_xi);
-    std::swap(s->v_out, s->prev_v);
-  }
+  // This call's inputs are uploaded on their own stream and compared bit for
+  // bit with the previous call's outputs and masses.  The previous call left
+  // the sheets in buckets routed for this call's opening half drift: when
+  // the inputs are exactly its outputs, the call continues from there (the
+  // same arithmetic as loading, re-sorting and re-bucketing them), and its
+  // sub-steps may already have run (enqueued by the previous call).
+  // Otherwise the sheets are loaded in xi's order and sorted.
+  const bool candidate = s->resume_ok && bits_eq(totmass, s->resume_totmass);
   unsigned* const h_diff = s->h_ab + 8;
   cudaStream_t up = s->up_stream;
-  WG_CUDA(cudaEventRecord(s->ev0, s->stream));
-  // the inputs' upload (and comparison) on the second stream
-  auto upload = [&]() -> cudaError_t {
-    cudaError_t e = cudaStreamWaitEvent(up, s->ev0, 0);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(s->in_xi, xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyHostToDevice, up);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s->in_v, v, 8 * (size_t)n, cudaMemcpyHostToDevice, up);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s->in_m, m, 8 * (size_t)n, cudaMemcpyHostToDevice, up);
-    if (candidate && e == cudaSuccess) {
-      e = cudaMemsetAsync(s->d_diff, 0, 4, up);
-      k_inputs_differ<<<152 * 8, 256, 0, up>>>(n, s->in_xi, s->prev_xi, s->in_v, s->prev_v,
-                                               s->in_m, s->prev_m, s->d_diff);
-      if (e == cudaSuccess) e = cudaGetLastError();
-      if (e == cudaSuccess) e = cudaMemcpyAsync(h_diff, s->d_diff, 4, cudaMemcpyDeviceToHost, up);
+  const int prev = s->out_last;
+  WG_CUDA(cudaMemcpyAsync(s->in_xi, xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyHostToDevice, up));
+  WG_CUDA(cudaMemcpyAsync(s->in_v, v, 8 * (size_t)n, cudaMemcpyHostToDevice, up));
+  WG_CUDA(cudaMemcpyAsync(s->in_m, m, 8 * (size_t)n, cudaMemcpyHostToDevice, up));
+  if (candidate) {
+    WG_CUDA(cudaMemsetAsync(s->d_diff, 0, 4, up));
+    k_inputs_differ<<<152 * 8, 256, 0, up>>>(n, s->in_xi, s->outs[prev].xi, s->in_v,
+                                             s->outs[prev].v, s->in_m, s->prev_m, s->d_diff);
+    WG_CUDA(cudaGetLastError());
+    WG_CUDA(cudaMemcpyAsync(h_diff, s->d_diff, 4, cudaMemcpyDeviceToHost, up));
+  }
+  WG_CUDA(cudaEventRecord(s->ev_up, up));
+  int out = prev ^ 1;  // the set this call's outputs go to
+  bool resumed = false;
+  if (spec) {
+    WG_CUDA(cudaEventSynchronize(s->ev_up));
+    if (candidate && *h_diff == 0) {
+      point_at(s->spec_set);
+      rc = run_call_end(s, time_elapsed);
+      s->spec_pending = false;
+      if (rc == WG_OK && !s->out_valid) {
+        launch_desort(s->table, n, s->x_out, s->v_out, s->stream);
+        s->out_valid = true;
+      }
+      clear_call();
+      if (rc) {
+        if (err) *err = rc;
+        return rc;
+      }
+      *t0 = s->spec_t0_out;
+      out = s->spec_set;
+      resumed = true;
+    } else {
+      drop_spec();
     }
-    if (e == cudaSuccess) e = cudaEventRecord(s->ev_up, up);
-    return e;
-  };
-  const double t0_in = t0 ? *t0 : 0.0;
-  bool resume = speculate;
-  if (!speculate) {
-    WG_CUDA(upload());
-    if (candidate) {
-      WG_CUDA(cudaEventSynchronize(s->ev_up));
-      resume = *h_diff == 0;
+  } else if (candidate && s->mode == 1) {
+    WG_CUDA(cudaEventSynchronize(s->ev_up));
+    if (*h_diff == 0) {
+      point_at(out);
+      rc = run_call(s, dt, nleap, t0, time_elapsed, true);
+      if (rc == WG_OK && !s->out_valid) {
+        launch_desort(s->table, n, s->x_out, s->v_out, s->stream);
+        s->out_valid = true;
+      }
+      clear_call();
+      if (rc) {
+        if (err) *err = rc;
+        return rc;
+      }
+      resumed = true;
+      s->spec_enabled = true;
     }
   }
-  if (resume) {
-    s->call_xi = reinterpret_cast<SheetRec*>(s->stage_xi);
-    s->call_a = s->stage_a;
-    // the call's own small uploads and its launches are enqueued first, so
-    // that on the copy engine they go ahead of the inputs' upload
-    rc = run_call_begin(s, dt, nleap, t0, false);
-    if (rc == WG_OK && speculate) {
-      const cudaError_t e = upload();
-      if (e != cudaSuccess) {
-        cudaStreamSynchronize(s->stream);
-        set_error("upload failed: %s", cudaGetErrorString(e));
-        rc = WG_ERR_CUDA;
-      }
-    }
-    if (rc == WG_OK) rc = run_call_end(s, time_elapsed);
-    s->call_xi = nullptr;
-    s->call_a = nullptr;
-    if (rc) {
-      cudaStreamSynchronize(up);
-      if (err) *err = rc;
-      return rc;
-    }
-    if (speculate) {
-      WG_CUDA(cudaEventSynchronize(s->ev_up));
-      if (*h_diff != 0) {  // the inputs differ: this result is discarded
-        resume = false;
-        if (t0) *t0 = t0_in;
-      }
-    }
-  }
-  if (!resume) {
+  if (!resumed) {
     WG_CUDA(cudaStreamWaitEvent(s->stream, s->ev_up, 0));
     StateTable t0tab;
     t0tab.cur = s->set[0];
@@ -1429,35 +1465,54 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
     // the sheets are compact with the opening half drift pending: the call
     // sorts them and runs on the bucket path
     s->mode = 0;
-    s->call_xi = reinterpret_cast<SheetRec*>(s->stage_xi);
-    s->call_a = s->stage_a;
-    rc = run_call(s, dt, nleap, t0, time_elapsed, false);
-    s->call_xi = nullptr;
-    s->call_a = nullptr;
+    point_at(out);
+    rc = run_call(s, dt, nleap, t0, time_elapsed, true);
+    if (rc == WG_OK && !s->out_valid) {
+      launch_desort(s->table, n, s->x_out, s->v_out, s->stream);
+      s->out_valid = true;
+    }
+    clear_call();
     if (rc) {
       if (err) *err = rc;
       return rc;
     }
   }
-  // the caller's buffers are read by the uploads before they are written here
-  WG_CUDA(cudaStreamWaitEvent(s->stream, s->ev_up, 0));
-  WG_CUDA(cudaMemcpyAsync(xi, s->stage_xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyDeviceToHost,
-                          s->stream));
-  if (!s->out_valid) {
-    launch_desort(s->table, n, s->x_out, s->v_out, s->stream);
-    s->out_valid = true;
-  }
-  WG_CUDA(cudaMemcpyAsync(x, s->x_out, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
-  WG_CUDA(cudaMemcpyAsync(v, s->v_out, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
-  WG_CUDA(cudaMemcpyAsync(a, s->stage_a, 8 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+  // desorts above ran on the main stream: done before the downloads
   WG_CUDA(cudaStreamSynchronize(s->stream));
-  s->resume_streak = resume ? s->resume_streak + 1 : 0;
-  // this call's masses are the next call's reference
-  std::swap(s->in_m, s->prev_m);
   s->resume_ok = s->mode == 1;
   s->resume_totmass = totmass;
-  if (rc && err) *err = rc;
-  return rc;
+  // the next call's sub-steps, enqueued now on the main stream: they run
+  // while this call's outputs download and the caller works on them
+  if (s->spec_enabled && s->resume_ok && s->compact_calls == 0 && t0) {
+    s->spec_set = out ^ 1;
+    point_at(s->spec_set);
+    double t_spec = *t0;
+    const int rs = run_call_begin(s, dt, nleap, &t_spec, true);
+    clear_call();
+    if (rs == WG_OK) {
+      s->spec_pending = true;
+      s->spec_dt = dt;
+      s->spec_nleap = nleap;
+      s->spec_t0_in = *t0;
+      s->spec_t0_out = t_spec;
+      s->spec_totmass = totmass;
+      s->spec_omega2 = omega2;
+      s->spec_ext = ext;
+    }
+  }
+  // the caller's buffers were read by the uploads before they are written here
+  cudaStream_t down = s->down_stream;
+  const wg_sim::OutSet& o = s->outs[out];
+  WG_CUDA(cudaStreamWaitEvent(down, s->ev_up, 0));
+  WG_CUDA(cudaMemcpyAsync(xi, o.xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyDeviceToHost, down));
+  WG_CUDA(cudaMemcpyAsync(x, o.x, 8 * (size_t)n, cudaMemcpyDeviceToHost, down));
+  WG_CUDA(cudaMemcpyAsync(v, o.v, 8 * (size_t)n, cudaMemcpyDeviceToHost, down));
+  WG_CUDA(cudaMemcpyAsync(a, o.a, 8 * (size_t)n, cudaMemcpyDeviceToHost, down));
+  WG_CUDA(cudaStreamSynchronize(down));
+  // this call's masses are the next call's reference
+  std::swap(s->in_m, s->prev_m);
+  s->out_last = out;
+  return WG_OK;
 }
 
 }  // extern "C"
