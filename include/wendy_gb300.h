@@ -176,7 +176,10 @@ int wg_nbody_approx_stats(wg_stats *out);
    registered id instead of a function pointer.  Every call uploads its
    inputs and downloads its outputs; a call whose inputs are bit for bit the
    previous call's outputs (the reference's generator loop) continues from
-   the resident state instead of re-sorting it, with identical results.
+   the resident state instead of re-sorting it, and after such a call the
+   next one's sub-steps are enqueued before returning (kept if the next
+   call's scalars and inputs match, dropped otherwise): identical results,
+   with the transfers under the sub-steps.
    Reference: _wendy_nbody_approx_onestep, wendy/wendy.c:385-418 and its
    argtypes at wendy/wendy.py:76-93. */
 int wg_nbody_approx_onestep(int n, wg_sheet *xi, double *x, double *v, const double *m,
