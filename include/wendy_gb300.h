@@ -89,14 +89,18 @@ int wg_step(wg_sim *s, double dt, int nleap, double *t0, double *time_elapsed);
    simulation's stream and returns at once (*t0 is advanced immediately);
    wg_step_end waits for it, completes it (a sub-step that overflowed a
    bucket is finished on the full re-sort path here) and reports its device
-   time.  Between the two, every other entry on the simulation except
-   wg_destroy returns WG_ERR_ARG.  Lets a caller overlap its own work on the
-   previous output with the device computing the next one.
+   time.  Between the two, wg_download returns the output completed before
+   wg_step_begin (the step writes a second pair of output buffers), copied on
+   a stream of its own while the step runs; every other entry on the
+   simulation except wg_destroy returns WG_ERR_ARG.  Lets a caller overlap its
+   own work on the previous output, and its download, with the device
+   computing the next one.
    Reference: _wendy_nbody_approx_onestep, wendy/wendy.c:385-418. */
 int wg_step_begin(wg_sim *s, double dt, int nleap, double *t0);
 int wg_step_end(wg_sim *s, double *time_elapsed);
 
-/* Copy positions and velocities back in original particle order.
+/* Copy positions and velocities back in original particle order (during a
+   split step: those of the output completed before it).
    Reference: the de-sort at wendy/wendy.c:413-415 and the in-place yield
    of wendy/wendy.py:434-437. */
 int wg_download(wg_sim *s, double *x, double *v);

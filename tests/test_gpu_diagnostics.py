@@ -75,12 +75,22 @@ def test_step_begin_end_equals_step_and_guards_the_handle():
     a = wendy_gb300.Simulation(x, v, m, float(numpy.sum(m)), 1.21)
     b = wendy_gb300.Simulation(x, v, m, float(numpy.sum(m)), 1.21)
     ta, tb = ctypes.c_double(1.0), ctypes.c_double(1.0)
+    prev = None
     for _ in range(3):
-        a.step(0.002, 5, ta)
         b.step_begin(0.002, 5, tb)
-        # every other entry refuses a handle with a step in flight
-        with pytest.raises(wendy_gb300._lib.WendyGPUError):
-            b.download(numpy.empty(n), numpy.empty(n))
+        # with a step in flight, download returns the output completed before
+        # it (none before the first), and every other entry refuses the handle
+        bx, bv = numpy.empty(n), numpy.empty(n)
+        if prev is None:
+            with pytest.raises(wendy_gb300._lib.WendyGPUError):
+                b.download(bx, bv)
+        else:
+            b.download(bx, bv)
+            assert numpy.array_equal(bx, prev[0]) and numpy.array_equal(bv, prev[1])
+        a.step(0.002, 5, ta)
+        ax, av = numpy.empty(n), numpy.empty(n)
+        a.download(ax, av)
+        prev = (ax, av)
         with pytest.raises(wendy_gb300._lib.WendyGPUError):
             b.step(0.002, 5, tb)
         with pytest.raises(wendy_gb300._lib.WendyGPUError):

@@ -381,6 +381,24 @@ def test_changing_dt_between_outputs():
     assert numpy.max(numpy.abs(gv - vv)) <= 1e-10
 
 
+def test_generator_through_overflow_and_the_compact_path():
+    # as below, through the generator: each output downloads while the next
+    # one runs, including outputs the compact path left in sorted order
+    n = 50000
+    rng = numpy.random.default_rng(11)
+    x = rng.uniform(-1, 1, size=n)
+    v = -x / 0.02
+    m = numpy.full(n, 1.0 / n)
+    g = wendy_gb300.nbody(x, v, m, 0.05, approx=True, nleap=5)
+    r = O.nbody_approx(x, v, m, 0.05, 5)
+    for _ in range(8):
+        gx, gv = next(g)
+        rx, rv = next(r)
+        assert numpy.max(numpy.abs(gx - rx)) <= 1e-9
+        assert numpy.max(numpy.abs(gv - rv)) <= 1e-9
+    g.close()
+
+
 def test_repeated_overflow_falls_back_and_recovers():
     # the sheets converge on the origin, cross and spread again: buckets
     # overflow on consecutive sub-steps (re-sort, restart, then the compact

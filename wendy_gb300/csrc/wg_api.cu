@@ -181,6 +181,16 @@ struct wg_sim {
   int backoff = 1;
   double pending_dt = 0; // dt of the half drift the bucket layout was routed for
   bool out_valid = false;  // x_out / v_out hold the last call's output
+  // Split steps (wg_step_begin): a second pair of output buffers, so that the
+  // output completed before a step was begun can be downloaded (on its own
+  // stream) while that step runs and writes the other pair.
+  double* out2 = nullptr;        // [2n]: x, v of the second pair
+  double* x_keep = nullptr;      // the first pair (x_out, v_out as allocated)
+  double* v_keep = nullptr;
+  double* done_x = nullptr;      // the completed output during a split step
+  double* done_v = nullptr;
+  cudaStream_t dl_stream = nullptr;
+  cudaEvent_t ev_done = nullptr; // that output is materialised
   int grid_bucket = 0;
   BucketTuning tune;             // bucket size, window, sort bits, CTAs per SM
   SheetRec* call_xi = nullptr;    // extra outputs of the reference-shaped entry (this call)
@@ -253,6 +263,10 @@ void free_sim(wg_sim* s) {
   if (s->h_ab) cudaFreeHost(s->h_ab);
   if (s->up_stream) cudaStreamSynchronize(s->up_stream);
   if (s->down_stream) cudaStreamSynchronize(s->down_stream);
+  if (s->dl_stream) cudaStreamSynchronize(s->dl_stream);
+  if (s->out2) cudaFree(s->out2);
+  if (s->ev_done) cudaEventDestroy(s->ev_done);
+  if (s->dl_stream) cudaStreamDestroy(s->dl_stream);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->ev_up) cudaEventDestroy(s->ev_up);
@@ -324,6 +338,8 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
   s->x_out = reinterpret_cast<double*>(p); p += nd;
   s->v_out = reinterpret_cast<double*>(p); p += nd;
   s->a_sorted = reinterpret_cast<double*>(p); p += nd;
+  s->x_keep = s->x_out;
+  s->v_keep = s->v_out;
   if (cudaMemsetAsync(s->recs, 0, recs_b, s->stream) != cudaSuccess) {
     set_error("memset failed");
     return fail(WG_ERR_CUDA);
@@ -989,6 +1005,29 @@ int wg_step_begin(wg_sim* s, double dt, int nleap, double* t0) {
   }
   s->call_xi = nullptr;
   s->call_a = nullptr;
+  if (!s->out2) {
+    WG_CUDA(cudaMalloc(&s->out2, 16 * (size_t)s->n));
+    WG_CUDA(cudaStreamCreateWithFlags(&s->dl_stream, cudaStreamNonBlocking));
+    WG_CUDA(cudaEventCreateWithFlags(&s->ev_done, cudaEventDisableTiming));
+    s->st.device_bytes += 16 * s->n;
+  }
+  // the output completed so far stays downloadable while this step runs:
+  // materialised now if the last call left it in the sorted state, then the
+  // step writes the other pair of buffers
+  s->done_x = nullptr;
+  s->done_v = nullptr;
+  if (s->st.substeps > 0) {
+    if (!s->out_valid) {
+      launch_desort(s->table, s->n, s->x_out, s->v_out, s->stream);
+      s->out_valid = true;
+    }
+    WG_CUDA(cudaEventRecord(s->ev_done, s->stream));
+    s->done_x = s->x_out;
+    s->done_v = s->v_out;
+  }
+  double* const other_x = s->x_out == s->out2 ? s->x_keep : s->out2;
+  s->x_out = other_x;
+  s->v_out = other_x == s->out2 ? s->out2 + s->n : s->v_keep;
   return run_call_begin(s, dt, nleap, t0, true);
 }
 
@@ -1001,6 +1040,15 @@ int wg_step_end(wg_sim* s, double* time_elapsed) {
 }
 
 int wg_download(wg_sim* s, double* x, double* v) {
+  if (s && s->pend_active && s->done_x) {
+    // a split step is running: the output completed before it, on its own stream
+    cudaStream_t d = s->dl_stream;
+    WG_CUDA(cudaStreamWaitEvent(d, s->ev_done, 0));
+    if (x) WG_CUDA(cudaMemcpyAsync(x, s->done_x, 8 * s->n, cudaMemcpyDeviceToHost, d));
+    if (v) WG_CUDA(cudaMemcpyAsync(v, s->done_v, 8 * s->n, cudaMemcpyDeviceToHost, d));
+    WG_CUDA(cudaStreamSynchronize(d));
+    return WG_OK;
+  }
   int rc = check_idle(s);
   if (rc) return rc;
   if (!s->out_valid) {

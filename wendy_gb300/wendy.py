@@ -144,8 +144,9 @@ def _nbody_approx(x, v, m, dt, nleap, t0=0., omega=None, ext_force=None, sort="c
         sim.step_begin(dt_leap, nleap, t)
         while True:
             elapsed = sim.step_end()
-            sim.download(x, v)
+            # the next output is enqueued first; this one downloads while it runs
             sim.step_begin(dt_leap, nleap, t)
+            sim.download(x, v)
             if full_output:
                 yield (x, v, elapsed)
             else:
