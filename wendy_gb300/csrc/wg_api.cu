@@ -1395,8 +1395,9 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   if (spec) {
     const bool same = t0 && bits_eq(dt, s->spec_dt) && nleap == s->spec_nleap &&
                       bits_eq(*t0, s->spec_t0_in) && bits_eq(totmass, s->spec_totmass) &&
-                      bits_eq(omega2, s->spec_omega2) &&
-                      std::memcmp(&ext, &s->spec_ext, sizeof(ExtForce)) == 0;
+                      bits_eq(omega2, s->spec_omega2) && ext.kind == s->spec_ext.kind &&
+                      bits_eq(ext.p[0], s->spec_ext.p[0]) && bits_eq(ext.p[1], s->spec_ext.p[1]) &&
+                      bits_eq(ext.p[2], s->spec_ext.p[2]) && bits_eq(ext.p[3], s->spec_ext.p[3]);
     if (!same) {
       drop_spec();
       spec = false;
