@@ -216,7 +216,16 @@ int wg_pool_remove(wg_pool *p, int sim_id);
    simulation k's dt_leap; t0[k] advances as in wg_step; t0 may be NULL). */
 int wg_pool_step(wg_pool *p, int count, const int *ids, const double *dt, int nleap, double *t0,
                  double *time_elapsed);
-/* Positions and velocities of the last step, original order. */
+/* wg_pool_step in two halves (enqueue, then wait and complete), as
+   wg_step_begin / wg_step_end.  While a step is in flight, wg_pool_download
+   returns each simulation's output completed before it (the step writes a
+   second pair of output buffers), on a stream of its own, and wg_pool_add,
+   wg_pool_remove and wg_pool_step return WG_ERR_ARG. */
+int wg_pool_step_begin(wg_pool *p, int count, const int *ids, const double *dt, int nleap,
+                       double *t0);
+int wg_pool_step_end(wg_pool *p, double *time_elapsed);
+/* Positions and velocities of the last step, original order (during a step:
+   of the last step completed before it). */
 int wg_pool_download(wg_pool *p, int sim_id, double *x, double *v);
 int wg_pool_info(wg_pool *p, int64_t *used_bytes, int64_t *budget_bytes, int *n_sims,
                  int64_t *launches);

@@ -126,3 +126,35 @@ def test_members_overflowing_in_one_call_recover_independently():
             assert numpy.max(numpy.abs(gx - rx)) <= 1e-9
             assert numpy.max(numpy.abs(gv - rv)) <= 1e-9
     pool.close()
+
+
+def test_download_during_a_step_returns_the_previous_output():
+    # wg_pool_step_begin / wg_pool_step_end: while a step runs, each member's
+    # download is its output before that step (none before the first); the
+    # pool refuses to change its members; results equal synchronous steps
+    members = [ics.sech2_disk(20000, seed=s, masses="lognormal") for s in (1, 2)]
+    p, q = Pool(), Pool()
+    ids = [p.add(x, v, m, omega=1.1) for x, v, m in members]
+    qids = [q.add(x, v, m, omega=1.1) for x, v, m in members]
+    for k in range(3):
+        p.step_begin(ids, 0.002, 5)
+        for sid, qid in zip(ids, qids):
+            if k == 0:
+                with pytest.raises(wendy_gb300._lib.WendyGPUError):
+                    p.download(sid)
+            else:
+                x, v = p.download(sid)
+                qx, qv = q.download(qid)
+                assert numpy.array_equal(x, qx) and numpy.array_equal(v, qv)
+        with pytest.raises(wendy_gb300._lib.WendyGPUError):
+            p.remove(ids[0])
+        with pytest.raises(wendy_gb300._lib.WendyGPUError):
+            p.add(*members[0])
+        assert p.step_end() > 0.0
+        q.step(qids, 0.002, 5)
+    for sid, qid in zip(ids, qids):
+        x, v = p.download(sid)
+        qx, qv = q.download(qid)
+        assert numpy.array_equal(x, qx) and numpy.array_equal(v, qv)
+    p.close()
+    q.close()

@@ -25,7 +25,7 @@ EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", 
            "wg_step", "wg_step_begin", "wg_step_end", "wg_download", "wg_energy", "wg_get_stats", "wg_destroy", "wg_accel", "wg_ext_force_eval",
            "wg_nbody_approx_onestep", "wg_nbody_approx_stats", "wg_profile", "wg_host_register", "wg_host_unregister",
            "wg_accel_noalloc", "wg_pool_sim_bytes", "wg_pool_create", "wg_pool_add",
-           "wg_pool_remove", "wg_pool_step", "wg_pool_download", "wg_pool_info",
+           "wg_pool_remove", "wg_pool_step", "wg_pool_step_begin", "wg_pool_step_end", "wg_pool_download", "wg_pool_info",
            "wg_pool_destroy", "wg_set_tuning", "wg_get_tuning")
 
 # Largest n wg_accel_noalloc accepts (its fixed device scratch array).
@@ -115,6 +115,8 @@ def lib():
                               ctypes.POINTER(_I)]
     L.wg_pool_remove.argtypes = [_P, _I]
     L.wg_pool_step.argtypes = [_P, _I, _P, _P, _I, _P, ctypes.POINTER(_D)]
+    L.wg_pool_step_begin.argtypes = [_P, _I, _P, _P, _I, _P]
+    L.wg_pool_step_end.argtypes = [_P, ctypes.POINTER(_D)]
     L.wg_pool_download.argtypes = [_P, _I, _P, _P]
     L.wg_pool_info.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                ctypes.POINTER(_I), ctypes.POINTER(_I64)]

@@ -83,7 +83,9 @@ struct PoolSim {
   BucketRec* recs;
   double *ox, *ov, *om;  // overflow list; also the compact (unsorted) store in mode 0
   int32_t* oi;
-  double *x_out, *v_out;
+  double *x_out, *v_out;     // output of the last step (during a step: being written)
+  double *x_out2, *v_out2;   // the other pair; steps alternate between them
+  double *done_x = nullptr, *done_v = nullptr;  // during a step: the output before it
   uint64_t T_lo = 0, T_hi = 0;
   int E = 0;
   double totmass = 0, omega2 = -1;
@@ -105,7 +107,7 @@ size_t sim_bytes(int64_t n) {
          kAggSlots * (al(4 * (size_t)nb) + al(32 * (size_t)nb)) +
          2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
          al(sizeof(BucketRec) * (size_t)nb) + 3 * al(8 * (size_t)n) + al(4 * (size_t)n) +
-         2 * al(8 * (size_t)n);
+         4 * al(8 * (size_t)n);
 }
 
 void carve(PoolSim* s) {
@@ -132,6 +134,8 @@ void carve(PoolSim* s) {
   s->oi = reinterpret_cast<int32_t*>(p); p += al(4 * (size_t)s->n);
   s->x_out = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
   s->v_out = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
+  s->x_out2 = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
+  s->v_out2 = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
 }
 
 __global__ void k_set_table(StateTable* t, StateRef cur, StateRef other) {
@@ -199,6 +203,13 @@ struct wg_pool {
   // back) captured once per (simulations, buckets, nleap) and replayed
   cudaGraphExec_t gexec = nullptr;
   int g_count = -1, g_nleap = -1;
+  // a step begun (wg_pool_step_begin) and not yet completed
+  bool pend_active = false;
+  int pend_count = 0, pend_nleap = 0;
+  std::vector<PoolSim*> pend_act;
+  std::vector<double> pend_dt;
+  std::vector<int64_t> pend_task0;
+  cudaStream_t dl_stream = nullptr;  // downloads while a step runs
   int64_t g_ntasks = -1;
   void* g_small = nullptr;
   int64_t graph_builds = 0;
@@ -347,6 +358,7 @@ int wg_pool_create(int64_t budget_bytes, wg_pool** out) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
   if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&p->dl_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess) {
     delete p;
     return pool_fail(WG_ERR_CUDA, "stream/event creation failed");
@@ -364,6 +376,8 @@ int wg_pool_create(int64_t budget_bytes, wg_pool** out) {
 int wg_pool_add(wg_pool* p, int64_t n, const double* x, const double* v, const double* m,
                 double totmass, double omega2, int ext_kind, const double* ext_params,
                 int n_ext_params, int* sim_id) {
+  if (p && p->pend_active)
+    return pool_fail(WG_ERR_ARG, "a step is in flight: call wg_pool_step_end first");
   if (!p || !sim_id) return pool_fail(WG_ERR_ARG, "null argument");
   if (n < 1 || n >= (1ll << 30)) return pool_fail(WG_ERR_ARG, "n outside [1, 2^30)");
   if (!x || !v || !m) return pool_fail(WG_ERR_ARG, "null array");
@@ -440,6 +454,7 @@ int wg_pool_add(wg_pool* p, int64_t n, const double* x, const double* v, const d
 int wg_pool_remove(wg_pool* p, int sim_id) {
   if (!p || sim_id < 0 || (size_t)sim_id >= p->sims.size() || !p->sims[(size_t)sim_id])
     return pool_fail(WG_ERR_ARG, "no simulation %d in the pool", sim_id);
+  if (p->pend_active) return pool_fail(WG_ERR_ARG, "a step is in flight: call wg_pool_step_end first");
   PoolSim* s = p->sims[(size_t)sim_id];
   cudaFreeAsync(s->mem, p->stream);
   p->used -= (int64_t)s->bytes;
@@ -448,10 +463,13 @@ int wg_pool_remove(wg_pool* p, int sim_id) {
   return WG_OK;
 }
 
-int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nleap, double* t0,
-                 double* time_elapsed) {
+// The first half of a pool step: everything up to the launch of the
+// sub-steps (or the replay of their graph); pool_step_end completes it.
+static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* dt, int nleap,
+                           double* t0) {
   if (!p || count < 1 || !ids || !dt || nleap < 1 || nleap > kMaxLeap)
     return pool_fail(WG_ERR_ARG, "bad arguments to wg_pool_step");
+  if (p->pend_active) return pool_fail(WG_ERR_ARG, "a step is in flight: call wg_pool_step_end first");
   std::vector<PoolSim*> act((size_t)count);
   int64_t ntasks = 0;
   for (int k = 0; k < count; ++k) {
@@ -506,6 +524,15 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
       if (rc) return rc;
       s->fresh = true;
     }
+  }
+  // the output of each simulation's last step stays downloadable while this
+  // one runs: the step writes the other pair of output buffers
+  for (int k = 0; k < count; ++k) {
+    PoolSim* s = act[(size_t)k];
+    s->done_x = s->out_valid ? s->x_out : nullptr;
+    s->done_v = s->out_valid ? s->v_out : nullptr;
+    std::swap(s->x_out, s->x_out2);
+    std::swap(s->v_out, s->v_out2);
   }
   // the kernel's view of every simulation, and the task list
   int64_t t = 0;
@@ -612,6 +639,25 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
   }
   PC(cudaGraphLaunch(p->gexec, p->stream));
   p->launches += nleap;
+  p->pend_active = true;
+  p->pend_count = count;
+  p->pend_nleap = nleap;
+  p->pend_act = act;
+  p->pend_dt.assign(dt, dt + count);
+  p->pend_task0 = task0;
+  return WG_OK;
+}
+
+// The second half: waits for the sub-steps, then the bookkeeping and the
+// recovery of simulations that overflowed a bucket.
+static int pool_step_end(wg_pool* p, double* time_elapsed) {
+  if (!p || !p->pend_active) return pool_fail(WG_ERR_ARG, "no pool step in flight");
+  p->pend_active = false;
+  const int count = p->pend_count, nleap = p->pend_nleap, L1 = p->cap_leap;
+  const std::vector<PoolSim*>& act = p->pend_act;
+  const double* dt = p->pend_dt.data();
+  const std::vector<int64_t>& task0 = p->pend_task0;
+  int rc = WG_OK;
   PC(cudaStreamSynchronize(p->stream));
   // bookkeeping, and recovery of simulations that overflowed a bucket
   for (int k = 0; k < count; ++k) {
@@ -736,10 +782,38 @@ int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nl
   return WG_OK;
 }
 
+int wg_pool_step(wg_pool* p, int count, const int* ids, const double* dt, int nleap, double* t0,
+                 double* time_elapsed) {
+  const int rc = pool_step_begin(p, count, ids, dt, nleap, t0);
+  if (rc) return rc;
+  return pool_step_end(p, time_elapsed);
+}
+
+int wg_pool_step_begin(wg_pool* p, int count, const int* ids, const double* dt, int nleap,
+                       double* t0) {
+  return pool_step_begin(p, count, ids, dt, nleap, t0);
+}
+
+int wg_pool_step_end(wg_pool* p, double* time_elapsed) { return pool_step_end(p, time_elapsed); }
+
 int wg_pool_download(wg_pool* p, int sim_id, double* x, double* v) {
   if (!p || sim_id < 0 || (size_t)sim_id >= p->sims.size() || !p->sims[(size_t)sim_id])
     return pool_fail(WG_ERR_ARG, "no simulation %d in the pool", sim_id);
   PoolSim* s = p->sims[(size_t)sim_id];
+  if (p->pend_active) {
+    // a step is running: the output completed before it (the step writes the
+    // other pair), or the current one of a simulation it does not advance,
+    // on a stream of its own
+    bool stepping = false;
+    for (PoolSim* a : p->pend_act) stepping |= a == s;
+    const double* sx = stepping ? s->done_x : (s->out_valid ? s->x_out : nullptr);
+    const double* sv = stepping ? s->done_v : (s->out_valid ? s->v_out : nullptr);
+    if (!sx) return pool_fail(WG_ERR_ARG, "simulation %d has no completed output", sim_id);
+    if (x) PC(cudaMemcpyAsync(x, sx, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->dl_stream));
+    if (v) PC(cudaMemcpyAsync(v, sv, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->dl_stream));
+    PC(cudaStreamSynchronize(p->dl_stream));
+    return WG_OK;
+  }
   if (!s->out_valid) return pool_fail(WG_ERR_ARG, "simulation %d has not been stepped", sim_id);
   if (x) PC(cudaMemcpyAsync(x, s->x_out, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->stream));
   if (v) PC(cudaMemcpyAsync(v, s->v_out, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->stream));
@@ -774,6 +848,10 @@ int wg_pool_destroy(wg_pool* p) {
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   if (p->stream) cudaStreamDestroy(p->stream);
+  if (p->dl_stream) {
+    cudaStreamSynchronize(p->dl_stream);
+    cudaStreamDestroy(p->dl_stream);
+  }
   delete p;
   return WG_OK;
 }

@@ -65,6 +65,26 @@ class Pool:
                                         ctypes.byref(el)), "wg_pool_step")
         return el.value
 
+    def step_begin(self, ids, dt_leap, nleap, t0=None):
+        """Enqueue ``step`` and return at once (``t0`` advances now).  Until
+        ``step_end``, ``download`` returns each simulation's previous output."""
+        ids = numpy.ascontiguousarray(ids, dtype=numpy.int32)
+        dts = numpy.ascontiguousarray(numpy.broadcast_to(dt_leap, ids.shape), dtype=numpy.float64)
+        if t0 is not None and (t0.dtype != numpy.float64 or not t0.flags.c_contiguous
+                               or t0.shape != ids.shape):
+            raise ValueError("t0 must be a contiguous float64 array, one entry per id")
+        self._pend = (ids, dts)  # the arrays must outlive the call
+        _lib.check(self._L.wg_pool_step_begin(self._h, len(ids), ids.ctypes.data, dts.ctypes.data,
+                                              int(nleap), None if t0 is None else t0.ctypes.data),
+                   "wg_pool_step_begin")
+
+    def step_end(self):
+        """Complete the step enqueued by ``step_begin``; returns its device time."""
+        el = ctypes.c_double(0.)
+        _lib.check(self._L.wg_pool_step_end(self._h, ctypes.byref(el)), "wg_pool_step_end")
+        self._pend = None
+        return el.value
+
     def download(self, sim_id, x=None, v=None):
         n = self._n[sim_id]
         x = numpy.empty(n) if x is None else x

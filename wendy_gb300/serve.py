@@ -7,7 +7,8 @@ keeps every admitted simulation resident in HBM inside one
 requests that have arrived while the memory budget allows, advances *all*
 resident simulations by one output interval (one launch of the fused
 sub-step kernel per leapfrog sub-step, covering every simulation), streams
-each simulation's output back, and retires the simulations that are done.
+each simulation's previous output back while that runs, and retires the
+simulations that are done.
 Requests that arrive while a round is on the GPU join at the next round, so
 work of new and old requests overlaps on the device.
 
@@ -83,12 +84,35 @@ class Server:
         self.rounds = 0
 
     def run(self, requests, clock=time.perf_counter):
-        """Serve `requests` (sorted by arrival) in real time; returns them."""
+        """Serve `requests` (sorted by arrival) in real time; returns them.
+
+        Each round begins the pool step, then downloads and hands over the
+        previous round's outputs while that step runs (the pool keeps each
+        simulation's last output in a second pair of buffers), then completes
+        the step.  Admission and retirement happen between steps.
+        """
         pending = sorted(requests, key=lambda r: r.arrival)
-        active = {}  # sim id -> [request, outputs left, t0 array slot]
+        # sim id -> [request, outputs left to compute, t0, page-locked buffers,
+        #            outputs delivered]
+        active = {}
+        unread = []  # simulations whose latest output is not delivered yet
         start = clock()
         i = 0
         used = 0
+
+        def deliver(sids):
+            for sid in sids:
+                r, left, t, buf, done = active[sid]
+                x, v = self.pool.download(sid, buf.x, buf.v)
+                if r.keep_outputs:
+                    r.outputs.append((x.copy(), v.copy()))
+                if self.on_output:
+                    self.on_output(r, x, v)
+                active[sid][4] = done = done + 1
+                if done == r.noutputs:
+                    r.last_x, r.last_v = x.copy(), v.copy()
+                    r.done_at = clock() - start
+
         while i < len(pending) or active:
             now = clock() - start
             # admit everything that has arrived and fits
@@ -100,39 +124,43 @@ class Server:
                 sid = self.pool.add(r.x, r.v, r.m, omega=r.omega, ext_force=r.ext_force,
                                     twopiG=1.)
                 r.admitted_at = now
-                active[sid] = [r, r.noutputs, r.t0, _Pinned(r.n)]
+                active[sid] = [r, r.noutputs, r.t0, _Pinned(r.n), 0]
                 used += need
                 i += 1
-            if not active:
+            stepping = [sid for sid, a in active.items() if a[1] > 0]
+            if not stepping and not unread:
+                if i >= len(pending):
+                    break
                 # idle until the next arrival
                 wait = pending[i].arrival - (clock() - start)
                 if wait > 0:
                     time.sleep(min(wait, 0.05))
                 continue
-            # one round: every resident simulation advances one output interval
+            # one round: every resident simulation with outputs left advances
+            # one output interval; the previous round's outputs are delivered
+            # while the first of its pool steps runs
             by_nleap = {}
-            for sid, (r, left, t, buf) in active.items():
-                by_nleap.setdefault(r.nleap, []).append(sid)
+            for sid in stepping:
+                by_nleap.setdefault(active[sid][0].nleap, []).append(sid)
+            to_read, unread = unread, []
             for nleap, ids in by_nleap.items():
                 dts = numpy.array([active[s][0].dt / nleap for s in ids])
                 t0 = numpy.array([active[s][2] for s in ids], dtype=numpy.float64)
-                self.pool.step(ids, dts, nleap, t0)
+                self.pool.step_begin(ids, dts, nleap, t0)
+                deliver(to_read)
+                to_read = []
+                self.pool.step_end()
                 for s, t in zip(ids, t0):
                     active[s][2] = float(t)
-            self.rounds += 1
-            now = clock() - start
+                    active[s][1] -= 1
+                unread.extend(ids)
+            deliver(to_read)  # a round with nothing left to step
+            if by_nleap:
+                self.rounds += 1
+            # retire the simulations whose last output has been delivered
             for sid in list(active):
-                r, left, t, buf = active[sid]
-                x, v = self.pool.download(sid, buf.x, buf.v)
-                if r.keep_outputs:
-                    r.outputs.append((x.copy(), v.copy()))
-                if self.on_output:
-                    self.on_output(r, x, v)
-                left -= 1
-                active[sid][1] = left
-                if left == 0:
-                    r.last_x, r.last_v = x.copy(), v.copy()
-                    r.done_at = clock() - start
+                r, left, t, buf, done = active[sid]
+                if done == r.noutputs:
                     buf.release()
                     self.pool.remove(sid)
                     used -= Pool.sim_bytes(r.n)
