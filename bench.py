@@ -115,14 +115,28 @@ def run_ensemble(args, w):
     launches = pool.info()["launches"] - launches0
     value = total * nleap * args.steps / el
     # end to end: every output also copied back (x, v of every simulation)
-    xb = {sid: (numpy.empty(mem[k][0]), numpy.empty(mem[k][0])) for k, sid in enumerate(ids)}
+    # into page-locked host memory, each step's downloads running while the
+    # next step computes (wg_pool_step_begin / wg_pool_step_end)
+    from wendy_gb300 import _lib as LL
+    LLL = LL.lib()
+    xall, vall = numpy.empty(total), numpy.empty(total)
+    pinned = [a for a in (xall, vall) if LLL.wg_host_register(a.ctypes.data, a.nbytes) == 0]
+    offs = numpy.cumsum([0] + [mem[k][0] for k in range(len(ids))])
+    xb = {sid: (xall[offs[k]:offs[k + 1]], vall[offs[k]:offs[k + 1]])
+          for k, sid in enumerate(ids)}
     t_start = time.perf_counter()
     k_e2e = max(1, min(args.steps, 3))
-    for _ in range(k_e2e):
-        pool.step(ids, dts, nleap, t0)
-        for sid in ids:
-            pool.download(sid, *xb[sid])
+    for k in range(k_e2e):
+        pool.step_begin(ids, dts, nleap, t0)
+        if k:
+            for sid in ids:
+                pool.download(sid, *xb[sid])
+        pool.step_end()
+    for sid in ids:
+        pool.download(sid, *xb[sid])
     wall = time.perf_counter() - t_start
+    for a in pinned:
+        LLL.wg_host_unregister(a.ctypes.data)
     pool.close()
     # the plain path: a sample of the same simulations, one at a time
     rng = numpy.random.default_rng(1)
@@ -150,7 +164,9 @@ def run_ensemble(args, w):
                        "nleap": nleap, "n_range": [w["nmin"], w["nmax"]],
                        "l2": "resident state larger than L2; no flush"},
             "e2e": {"value": total * nleap * k_e2e / wall, "unit": "particle-steps/s",
-                    "h2d_bytes_per_step": 16 * len(ids), "d2h_bytes_per_step": 16 * total},
+                    "h2d_bytes_per_step": 16 * len(ids), "d2h_bytes_per_step": 16 * total,
+                    "overlap": "every member's x, v downloaded every step into page-locked "
+                               "memory while the next step runs; the last step's after it"},
             "plain_one_at_a_time": {"value": solo, "unit": "particle-steps/s",
                                     "sample_sims": int(len(sample)),
                                     "ratio_batched_over_plain": value / solo},
