@@ -225,7 +225,8 @@ def peaks():
 
 
 class Clocks:
-    """Samples nvidia-smi every 200 ms while the timed region runs."""
+    """Samples the GPU's clocks and throttle reasons every 50 ms (one
+    `nvidia-smi -lms 50` process) while the timed region runs."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -233,41 +234,61 @@ class Clocks:
 
     def __init__(self, index):
         self.index = index
-        self.rows = []
-        self._stop = threading.Event()
-        self._t = threading.Thread(target=self._run, daemon=True)
+        self.rows = []  # (time, fields)
+        self._p = None
+        self._t = None
+        self._t_in = self._t_out = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index),
-                                      "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits"],
-                                     capture_output=True, text=True, timeout=5).stdout
-                for line in out.strip().splitlines():
-                    self.rows.append([c.strip() for c in line.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+    def _read(self):
+        for line in self._p.stdout:
+            self.rows.append((time.perf_counter(), [c.strip() for c in line.split(",")]))
 
     def __enter__(self):
-        self._t.start()
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.index),
+                                        "--query-gpu=" + self.QUERY,
+                                        "--format=csv,noheader,nounits", "-lms", "50"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._p = None
+        if self._p is not None:
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+            # the sampler is running before the timed region starts
+            t0 = time.perf_counter()
+            while not self.rows and self._p.poll() is None and time.perf_counter() - t0 < 5:
+                time.sleep(0.005)
+        self._t_in = time.perf_counter()
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        self._t_out = time.perf_counter()
+        if self._p is not None:
+            self._p.terminate()  # the process this object started
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
+            self._t.join(timeout=5)
 
     def summary(self):
-        if not self.rows:
+        inside = [r for t, r in self.rows if self._t_in is not None and self._t_in <= t
+                  and (self._t_out is None or t <= self._t_out)]
+        if not inside and self.rows:
+            # a region shorter than the sampling interval: the sample nearest to it
+            ref = self._t_in if self._t_in is not None else 0.0
+            inside = [min(self.rows, key=lambda tr: abs(tr[0] - ref))[1]]
+        rows = inside
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        sm = [float(r[1]) for r in rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4)
+        reasons = sorted({names[i] for r in rows for i in range(4)
                           if len(r) > 5 + i and r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.rows)}
+                "samples": len(rows), "interval_ms": 50}
 
 
 def make_inputs(w, seed=0):
