@@ -148,7 +148,8 @@ def test_dropin_resumes_from_resident_state_with_identical_results():
     # state (after one that did, the next computes while its inputs are
     # compared, and is redone if they differ).  The same calls with xi
     # handed over in another order are loaded and sorted anew; both give the
-    # same bits.  The 5th call changes one velocity after resumed calls.
+    # same bits.  The 5th call changes one velocity after resumed calls; the
+    # 7th changes nleap while the sub-steps enqueued for it are pending.
     n = 200000
     x, v, m = ics.sech2_disk(n, seed=21, masses="lognormal")
     tot = float(numpy.sum(m))
@@ -160,12 +161,13 @@ def test_dropin_resumes_from_resident_state_with_identical_results():
         xx, vv, a = x.copy(), v.copy(), numpy.zeros(n)
         t = 4.2
         outs = []
-        for k in range(6):
+        for k in range(7):
             if reorder:
                 xi = xi[::-1].copy()
             if k == 4:
                 vv[7] *= 1.0001
-            t, _el = wendy_gb300.approx_onestep(xi, xx, vv, m, a, tot, 0.002, 5, t, 1.21, PULSE)
+            nl = 3 if k == 6 else 5
+            t, _el = wendy_gb300.approx_onestep(xi, xx, vv, m, a, tot, 0.002, nl, t, 1.21, PULSE)
             outs.append((t, xx.copy(), vv.copy(), a.copy(), xi.copy()))
             if k == 0:  # the first call (re)builds the resident state
                 s0 = approx_onestep_stats()["sorts_full"]
@@ -173,7 +175,8 @@ def test_dropin_resumes_from_resident_state_with_identical_results():
 
     resumed, sorts_resumed = run(False)
     reloaded, sorts_reloaded = run(True)
-    assert sorts_resumed == 1 and sorts_reloaded == 5
+    # the 5th and 7th calls reload (a dropped speculation advanced the state)
+    assert sorts_resumed == 2 and sorts_reloaded == 6
     for (ta, xa, va, aa, xia), (tb, xb, vb, ab, xib) in zip(resumed, reloaded):
         assert ta == tb
         assert numpy.array_equal(xa, xb) and numpy.array_equal(va, vb)

@@ -1382,7 +1382,9 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   };
   // The sub-steps the previous call enqueued for this one are usable only
   // with this call's scalars; otherwise they are completed and dropped first
-  // (they hold the per-call arrays and the physics).
+  // (they hold the per-call arrays and the physics).  They advanced the
+  // resident state past the previous call's outputs, so this call cannot
+  // continue from it: it loads its inputs.
   auto drop_spec = [&]() {
     point_at(s->spec_set);
     double ignored = 0;
@@ -1390,6 +1392,7 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
     clear_call();
     s->spec_pending = false;
     s->spec_enabled = false;
+    s->resume_ok = false;
   };
   bool spec = s->spec_pending;
   if (spec) {
