@@ -211,8 +211,8 @@ def run_serve(args, w):
 
 HBM_FALLBACK_GBS = 6800.0
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_bucket_step launch at
-# N = 2^23 (237.7 MB + 186.0 MB), per sheet
-TRAFFIC_PER_SHEET = (237.672448e6 + 186.041856e6) / (1 << 23)
+# N = 2^23 (237.5 MB + 185.9 MB), per sheet
+TRAFFIC_PER_SHEET = (237.496576e6 + 185.93152e6) / (1 << 23)
 
 
 def peaks():
