@@ -408,10 +408,9 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
     return fail(WG_ERR_CUDA);
   }
   {
-    int dev = 0, sms = 0, per_sm = 0;
+    int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    (void)per_sm;
     s->grid_bucket = s->tune.ctas_per_sm * sms;
   }
   rc = alloc_call_arrays(s, 64);
