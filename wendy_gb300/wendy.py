@@ -51,7 +51,8 @@ class Simulation:
         return elapsed.value
 
     def step_begin(self, dt_leap, nleap, t0):
-        """Enqueue one output interval and return at once (``t0`` advances now)."""
+        """Enqueue one output interval and return at once (``t0`` advances now).
+        Until ``step_end``, ``download`` returns the output completed before it."""
         _lib.check(self._L.wg_step_begin(self._h, float(dt_leap), int(nleap), ctypes.byref(t0)),
                    "wg_step_begin")
 
@@ -76,6 +77,9 @@ class Simulation:
         return e.value, p.value
 
     def download(self, x, v):
+        """Positions and velocities of the last output, in original order, into
+        ``x`` and ``v`` (float64[n]); during a step begun with ``step_begin``,
+        those of the output completed before it, while the step runs."""
         for arr in (x, v):
             if not (arr.flags.c_contiguous and arr.flags.writeable and arr.dtype == numpy.float64
                     and len(arr) == self.n):
