@@ -3,24 +3,34 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload sech2_2p24|sech2_1e4|tophat_2p27]
 
-Workload (default, the large single-simulation configuration): N = 2^24
-sheets, isothermal sech^2 disk (z0 = 1, sigma^2 = 2 pi G Sigma z0 = 1.0 with
-twopiG = 1), lognormal masses (sigma_ln = 0.5) normalised to 1, harmonic
-omega = 1.1, dt = 0.02 per output, nleap = 20 sub-steps.  Seeded synthetic
-inputs (numpy default_rng(0), draw order x, v, m).
+Workload (default, the HBM-scale single-simulation configuration): N = 2^27
+equal-mass sheets (total mass 1, twopiG = 1) in a cold top-hat, x ~ U(-1, 1),
+v ~ N(0, 1e-3^2), no harmonic term, the registered pulsed external force
+F(x, t) = 0.3 exp(-(t - 5)^2 / 2) tanh(x / 0.5), dt = 0.01 per output,
+nleap = 10 sub-steps, 500 outputs from t = 0.  The slab collapses at
+t = pi/2 (inside it a = -x) and relaxes violently afterwards.  Seeded
+synthetic inputs (numpy default_rng(0), draw order x, v, m).  The other
+single-simulation workloads (--workload sech2_2p24 ...) follow the same
+rules.
 
-A step is one output interval (nleap sub-steps).  `value` is particle-steps/s
+A step is one output interval (nleap sub-steps); steps are counted from
+t = 0, the first W of them untimed.  `value` is particle-steps/s
 (N x nleap x steps / device time) with the sheets resident in HBM, timed with
-CUDA events on the library's stream; `e2e` is the same metric through the
-reference-shaped C-ABI call wg_nbody_approx_onestep with page-locked host
-buffers, so every step uploads its inputs and downloads x, v, a and the
-sorted records.  The resident state (28 B/sheet x 2^24 = 470 MB) is larger
-than L2, so no flush is needed between steps.
+CUDA events on the library's stream.  `full_run` then continues the same
+simulation through all of the configuration's outputs (for the top-hat: the
+collapse and the relaxation after it) and reports its particle-steps/s over
+the whole run, per phase, and how many sub-steps ran on the bucket path and
+how many on the compact (full re-sort) path.  `e2e` is the same metric
+through the reference-shaped C-ABI call wg_nbody_approx_onestep with
+page-locked host buffers, so every step uploads its inputs and downloads x,
+v, a and the sorted records.  The resident state (28 B/sheet, 3.8 GB at
+2^27) is larger than L2, so no flush is needed between steps.
 
 --impl reference times the CPU implementation of the same path on this
 host's cores: the oracle restatement of wendy's C (oracle/), with all host
 threads and the task-parallel merge sort, on a bounded sample of the same
-workload.
+workload (the sheets sorted once, then timed sub-steps in the steady state,
+as in the reference's generator loop).
 """
 import argparse
 import ctypes
@@ -40,13 +50,15 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     # name: (n, ics, ics kwargs, dt, nleap, omega, ext)
     "sech2_2p24": dict(n=1 << 24, family="sech2", kw=dict(masses="lognormal", sigma_ln=0.5),
-                       dt=0.02, nleap=20, omega=1.1, ext=None),
+                       dt=0.02, nleap=20, omega=1.1, ext=None, outputs=200),
     "sech2_2p23": dict(n=1 << 23, family="sech2", kw=dict(masses="lognormal", sigma_ln=0.5),
-                       dt=0.02, nleap=20, omega=1.1, ext=None),
+                       dt=0.02, nleap=20, omega=1.1, ext=None, outputs=200),
     "sech2_1e4": dict(n=10000, family="sech2", kw=dict(masses="equal"), dt=0.05, nleap=10,
-                      omega=None, ext=None),
+                      omega=None, ext=None, outputs=1000),
     "tophat_2p27": dict(n=1 << 27, family="tophat", kw=dict(masses="equal"), dt=0.01,
-                        nleap=10, omega=None, ext=("pulse", (0.3, 5.0, 1.0, 0.5))),
+                        nleap=10, omega=None, ext=("pulse", (0.3, 5.0, 1.0, 0.5)), outputs=500),
+    "tophat_2p23": dict(n=1 << 23, family="tophat", kw=dict(masses="equal"), dt=0.01,
+                        nleap=10, omega=None, ext=("pulse", (0.3, 5.0, 1.0, 0.5)), outputs=500),
     # ensemble / serving workloads (see run_ensemble, run_serve)
     "ensemble_4096": dict(sims=4096, nmin=1e3, nmax=1e6, nleap=10),
     "serve_poisson": dict(rate=200.0, nmin=1e3, nmax=4e6, smin=100, smax=10000, nleap=10,
@@ -210,9 +222,12 @@ def run_serve(args, w):
     print(json.dumps(line))
 
 HBM_FALLBACK_GBS = 6800.0
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_bucket_step launch at
-# N = 2^23 (237.5 MB + 185.9 MB), per sheet
-TRAFFIC_PER_SHEET = (237.496576e6 + 185.93152e6) / (1 << 23)
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_bucket_step launch
+# from an ncu capture of a smaller case of the same family, per sheet
+TRAFFIC_PER_SHEET = {
+    "sech2": ((237.496576e6 + 185.93152e6) / (1 << 23),
+              "ncu capture of one sub-step of the sech2 disk at N = 2^23"),
+}
 
 
 def peaks():
@@ -303,37 +318,67 @@ def ext_of(w):
     return PulseTanh(*w["ext"][1])
 
 
-def cpu_run(w, x, v, m, nleap_sample, sort, threads):
-    """Time the oracle on one output of nleap_sample sub-steps (seconds)."""
-    from oracle import oracle as O
-    O.set_parallel_sort(threads)
-    ext = None if w["ext"] is None else (O.EXT_PULSE_TANH, list(w["ext"][1]))
-    omega2 = -1.0 if w["omega"] is None else w["omega"] ** 2
-    xx, vv = x.copy(), v.copy()
-    a = numpy.zeros(len(x))
-    xi = O.make_sheets(xx)
-    _t0, el = O.onestep(xi, xx, vv, m, a, numpy.sum(m), w["dt"] / w["nleap"], nleap_sample, 4.0,
-                        omega2, ext, sort)
-    return el
+class CpuSample:
+    """The oracle (C restatement of wendy's approximate step) on this host's
+    cores, in the reference's steady state: one untimed call sorts the sheets
+    (the reference's generator does that once, on its first call), then
+    timed calls continue from the sorted records, as wendy's loop does."""
+
+    def __init__(self, w, x, v, m):
+        from oracle import oracle as O
+        O.load()
+        self.O = O
+        self.w = w
+        self.ext = None if w["ext"] is None else (O.EXT_PULSE_TANH, list(w["ext"][1]))
+        self.omega2 = -1.0 if w["omega"] is None else w["omega"] ** 2
+        self.dt_leap = w["dt"] / w["nleap"]
+        self.m = m
+        self.tot = numpy.sum(m)
+        self.x, self.v = x.copy(), v.copy()
+        self.a = numpy.zeros(len(x))
+        self.xi = O.make_sheets(self.x)
+        self.t = 0.0
+        self.cores = os.cpu_count() or 1
+        O.set_parallel_sort(self.cores)
+        self.t, _ = O.onestep(self.xi, self.x, self.v, m, self.a, self.tot, self.dt_leap, 1,
+                              self.t, self.omega2, self.ext, "parallel")
+
+    def snapshot(self):
+        return (self.xi.copy(), self.x.copy(), self.v.copy(), self.t)
+
+    def restore(self, snap):
+        xi, x, v, t = snap
+        self.xi[:] = xi
+        self.x[:] = x
+        self.v[:] = v
+        self.t = t
+
+    def run(self, nsub, sort):
+        """nsub sub-steps in one call; returns the call's own elapsed time."""
+        self.O.set_parallel_sort(self.cores)
+        self.t, el = self.O.onestep(self.xi, self.x, self.v, self.m, self.a, self.tot,
+                                    self.dt_leap, nsub, self.t, self.omega2, self.ext, sort)
+        return el
 
 
 def cpu_baseline(w, x, v, m, budget_s=20.0):
     """Bounded sample of the CPU path on this host (rank 0 only)."""
-    from oracle import oracle as O
-    O.load()
-    cores = os.cpu_count() or 1
+    cs = CpuSample(w, x, v, m)
+    snap = cs.snapshot()
     res = {}
     for sort in ("parallel", "quick"):
+        cs.restore(snap)
         # one sub-step first, to size the sample within the budget
-        el1 = cpu_run(w, x, v, m, 1, sort, cores)
+        el1 = cs.run(1, sort)
         k = int(max(1, min(w["nleap"], (budget_s / 2) // max(el1, 1e-9))))
-        el = cpu_run(w, x, v, m, k, sort, cores) if k > 1 else el1
+        el = cs.run(k, sort) if k > 1 else el1
         res[sort] = (w["n"] * k / el, k, el)
     best = max(res, key=lambda s: res[s][0])
     val, k, el = res[best]
-    return {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+    return {"value": val, "unit": "particle-steps/s", "cores": cs.cores, "kind": "port",
             "sample": "oracle (C restatement of wendy's approx step), sort=%s, OMP threads=%d, "
-                      "N=%d, one output of %d sub-steps (%.1f s)" % (best, cores, w["n"], k, el),
+                      "N=%d, %d sub-steps in one call from sorted records (%.1f s)"
+                      % (best, cs.cores, w["n"], k, el),
             "variants": {s: {"value": r[0], "substeps": r[1], "seconds": r[2]}
                          for s, r in res.items()}}
 
@@ -342,35 +387,75 @@ def run_reference(args, w):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from oracle import oracle as O
-    O.load()
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     x, v, m = make_inputs(w)
-    per_step = 2  # sub-steps per timed step: keeps K + W steps within minutes at N = 2^24
-    if w["n"] <= 100000:
-        per_step = w["nleap"]
+    # sub-steps per timed step: keeps K + W steps within minutes at N = 2^24 .. 2^27
+    per_step = w["nleap"] if w["n"] <= 100000 else (2 if w["n"] <= (1 << 24) else 1)
+    cs = CpuSample(w, x, v, m)
     for _ in range(args.warmup):
-        cpu_run(w, x, v, m, per_step, "parallel", cores)
+        cs.run(per_step, "parallel")
     tot = 0.0
     for _ in range(args.steps):
-        tot += cpu_run(w, x, v, m, per_step, "parallel", cores)
+        tot += cs.run(per_step, "parallel")
     val = w["n"] * per_step * args.steps / tot
     line = {"metric": "particle-steps/s", "value": val, "unit": "particle-steps/s",
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload, "n": w["n"], "nleap": w["nleap"],
-                       "dt": w["dt"], "omega": w["omega"],
+                       "dt": w["dt"], "omega": w["omega"], "ext_force": w["ext"],
                        "timed_substeps_per_step": per_step},
             "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores,
                              "kind": "port",
                              "sample": "oracle restatement of wendy's approx step, "
-                                       "sort=parallel, %d threads, %d sub-steps per step"
-                                       % (cores, per_step)},
+                                       "sort=parallel, %d threads, %d sub-steps per step, "
+                                       "from sorted records (steady state)" % (cores, per_step)},
             "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def full_run_summary(w, per_output, world):
+    """particle-steps/s of a whole run (every output from t = 0), per phase of
+    100 outputs, and which path its sub-steps took."""
+    n, nleap = w["n"], w["nleap"]
+    dev = sum(r[0] for r in per_output)
+    wall = sum(r[1] for r in per_output)
+    nout = len(per_output)
+    last = per_output[-1][2]
+    phases = []
+    prev = {"substeps_compact": 0, "sorts_full": 0}
+    for lo in range(0, nout, 100):
+        rows = per_output[lo:lo + 100]
+        st = rows[-1][2]
+        d = sum(r[0] for r in rows)
+        phases.append({"outputs": [lo, lo + len(rows)],
+                       "t": [lo * w["dt"], (lo + len(rows)) * w["dt"]],
+                       "ms_per_substep": d / (len(rows) * nleap) * 1e3,
+                       "particle_steps_per_s": n * nleap * len(rows) / d,
+                       "substeps_compact": st["substeps_compact"] - prev["substeps_compact"],
+                       "resorts": st["sorts_full"] - prev["sorts_full"],
+                       "largest_bucket_count": max(r[2]["last_max_count"] for r in rows)})
+        prev = st
+    out = {"outputs": nout, "substeps": nout * nleap, "t_end": nout * w["dt"],
+           "value": world * n * nleap * nout / dev, "unit": "particle-steps/s",
+           "device_s": dev, "wall_s": wall, "wall_value": world * n * nleap * nout / wall,
+           "substeps_bucket": nout * nleap - last["substeps_compact"],
+           "substeps_compact": last["substeps_compact"], "sorts_full": last["sorts_full"],
+           "phases": phases}
+    if w["family"] == "tophat":
+        # inside the uniform slab a = -x (total mass 1): it collapses at t = pi/2
+        kc = int(numpy.ceil((numpy.pi / 2) / w["dt"]))
+        post = per_output[kc - 1:] if kc < nout else []
+        if post:
+            c0 = per_output[kc - 1][2]["substeps_compact"]
+            out["post_collapse"] = {
+                "from_output": kc, "substeps": len(post[1:]) * nleap,
+                "substeps_compact": last["substeps_compact"] - c0,
+                "particle_steps_per_s": n * nleap * len(post[1:]) /
+                                        max(sum(r[0] for r in post[1:]), 1e-12)}
+    return out
 
 
 def main():
@@ -379,9 +464,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sech2_2p24", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="tophat_2p27", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-full-run", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -415,17 +501,25 @@ def main():
     ext = ext_of(w)
     tot = numpy.sum(m)
     sim = wendy_gb300.Simulation(x, v, m, tot, omega2, ext)
-    t0 = ctypes.c_double(4.0 if ext else 0.0)
+    t0 = ctypes.c_double(0.0)  # steps are outputs counted from t = 0
     dt_leap = dt / nleap
+    per_output = []  # (device s, wall s, stats) of every output from t = 0
+
+    def one_output():
+        tw = time.perf_counter()
+        el = sim.step(dt_leap, nleap, t0)
+        per_output.append((el, time.perf_counter() - tw, sim.stats()))
+        return el
+
     for _ in range(args.warmup):
-        sim.step(dt_leap, nleap, t0)
+        one_output()
     st0 = sim.stats()
     if world > 1:
         dist.barrier()
     with Clocks(local) as clk:
         elapsed = 0.0
         for _ in range(args.steps):
-            elapsed += sim.step(dt_leap, nleap, t0)
+            elapsed += one_output()
     st1 = sim.stats()
     # energy / momentum of the last output: on the device (wg_energy) and with
     # the reference's formula on the host, outside the timed region
@@ -469,17 +563,25 @@ def main():
                                     "achieved_gbs": 40.0 * n / f_s / 1e9},
              "radix_resort": {"ms": s_s * 1e3, "algorithmic_bytes_per_sheet": 250,
                               "achieved_gbs": 250.0 * n / s_s / 1e9}}
-    # DRAM bytes (read + write) of one k_bucket_step launch from an ncu capture
-    # of one sub-step at N = 2^23, scaled by the sheets of this workload: the
-    # traffic grows in proportion to the sheets
-    traffic = TRAFFIC_PER_SHEET * n
+    traffic_per_sheet, traffic_src = TRAFFIC_PER_SHEET.get(
+        w["family"], TRAFFIC_PER_SHEET["sech2"])
+    traffic = traffic_per_sheet * n
     roof = {"bound": "hbm", "kernel": "k_bucket_step", "achieved": bucket_gbs, "peak": hbm,
             "unit": "GB/s", "frac": bucket_gbs / hbm, "peak_kind": hbm_kind,
             "traffic": traffic, "traffic_unit": "bytes per launch",
-            "traffic_source": "ncu capture at N = 2^23, scaled to N",
+            "traffic_source": traffic_src + ", scaled to N by the sheets",
             "algorithmic_bytes_per_launch": 56.0 * n,
             "components": comps, "substep_ms": sub_s * 1e3,
-            "stats": {k: st1[k] - st0[k] for k in ("sorts_full", "sorts_window", "substeps")}}
+            "stats": {k: st1[k] - st0[k] for k in ("sorts_full", "sorts_window", "substeps",
+                                                   "substeps_compact")}}
+
+    # the same simulation on through all of the configuration's outputs: the
+    # whole run from t = 0, collapse and relaxation included
+    full = None
+    if not args.no_full_run and w.get("outputs"):
+        while len(per_output) < w["outputs"]:
+            one_output()
+        full = full_run_summary(w, per_output, world)
     sim.close()
 
     # end to end through the reference-shaped call, page-locked host buffers
@@ -494,14 +596,15 @@ def main():
         bufs = [xi, xx, vv, a, mm]
         for b in bufs:
             _lib.check(L.wg_host_register(b.ctypes.data, b.nbytes), "wg_host_register")
-        tt = 4.0 if ext else 0.0
-        for _ in range(2):
+        # outputs counted from t = 0 as above: W untimed, then K timed
+        tt = 0.0
+        for _ in range(args.warmup):
             tt, _el = wendy_gb300.approx_onestep(xi, xx, vv, mm, a, tot, dt_leap, nleap, tt,
                                                  omega2, ext)
         from wendy_gb300.wendy import approx_onestep_stats
         sorts0 = approx_onestep_stats()["sorts_full"]
         t_start = time.perf_counter()
-        k_e2e = max(3, min(args.steps, 5))
+        k_e2e = args.steps
         for _ in range(k_e2e):
             tt, _el = wendy_gb300.approx_onestep(xi, xx, vv, mm, a, tot, dt_leap, nleap, tt,
                                                  omega2, ext)
@@ -532,8 +635,8 @@ def main():
                            "omega": w["omega"], "ext_force": w["ext"], "ics": w["family"],
                            "parallelism": "replicas" if world > 1 else "single",
                            "l2": "resident state larger than L2; no flush"},
-                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
-                "diagnostics": diag,
+                "e2e": e2e, "roofline": roof, "full_run": full, "cpu_baseline": cpu,
+                "clocks": clk.summary(), "diagnostics": diag,
                 "gpu_launches": launches}
         print(json.dumps(line))
     if world > 1:

@@ -30,7 +30,8 @@ extern "C" {
 #define WG_ERR_ARG (-1)      /* invalid argument (sizes, non-finite or negative masses, ...) */
 #define WG_ERR_CUDA (-2)     /* a CUDA runtime call failed; see wg_last_error() */
 #define WG_ERR_NOMEM (-3)    /* device allocation failed */
-#define WG_ERR_DEVICE (-4)   /* a kernel raised its error word (e.g. a bounded wait expired) */
+#define WG_ERR_DEVICE (-4)   /* a kernel raised its error word (e.g. a bounded wait expired);
+                                the simulation it ran on is unusable afterwards */
 #define WG_ERR_EXT (-5)      /* unknown external-force id or bad parameter count */
 #define WG_ERR_BUDGET (-6)   /* request exceeds the memory budget it was admitted under */
 #define WG_ERR_NODEV (-7)    /* no CUDA device */
@@ -57,6 +58,8 @@ typedef struct wg_stats {
   double last_max_disp;      /* largest |dx| of the last drift */
   int64_t device_bytes;      /* device memory held by the simulation */
   int64_t launches;          /* kernels this handle has launched */
+  int64_t last_max_count;    /* most sheets any bucket received during the last call */
+  int64_t substeps_compact;  /* sub-steps run on the compact path (full re-sort + force) */
 } wg_stats;
 
 /* Library and device information. */
@@ -143,6 +146,17 @@ typedef struct wg_tuning {
 } wg_tuning;
 int wg_set_tuning(const wg_tuning *rows, int nrows);
 int wg_get_tuning(int64_t n, wg_tuning *out);
+
+/* Test hook for the bounded waits (no reference counterpart).  The force
+   kernel of the compact path finds each tile's mass prefix by looking back
+   over earlier tiles; spin_limit bounds each of its waits (0 = the production
+   limit, well above a second) and withhold_tile names a tile whose look-back
+   record is never published (-1 = none), so that the waits on it run out.
+   A call whose waits ran out returns WG_ERR_DEVICE (its message names the
+   expired wait) and leaves its simulation unusable: every later call on it
+   except wg_destroy returns WG_ERR_DEVICE.  The setting is process-wide and
+   applies to launches made after the call. */
+int wg_set_debug_wait(unsigned spin_limit, int64_t withhold_tile);
 
 /* Page-lock (or release) caller memory so that downloads and uploads run
    at full link speed.  No reference counterpart (wendy's buffers are plain
@@ -245,7 +259,10 @@ int wg_pool_destroy(wg_pool *p);
    WG_NOALLOC_MAX_SHEETS; larger n returns WG_ERR_ARG.  The first call on a
    device looks up the array's device address (cudaGetSymbolAddress): make
    that first call before any stream capture.  All calls share the array:
-   calls that overlap on the GPU (other streams or host threads) race. */
+   calls that overlap on the GPU (other streams or host threads) race.  The
+   inputs are checked on the device (they are device memory): a non-finite
+   position or mass, or a negative mass, returns WG_ERR_ARG after the call's
+   launches have run (the sort is skipped, `a` and `perm` are then undefined). */
 #define WG_NOALLOC_MAX_SHEETS 65536
 int wg_accel_noalloc(int64_t n, const double *x, const double *m, double totmass,
                      double omega2, int ext_kind, const double *ext_params, int n_ext_params,

@@ -63,7 +63,7 @@ def load():
         ctypes.c_int, _F64R, ctypes.c_int, ctypes.POINTER(ctypes.c_double), _F64]
     lib.wo_approx_onestep.restype = None
     lib.wo_accel.argtypes = [ctypes.c_int, _F64R, _F64R, ctypes.c_double, ctypes.c_double,
-                             ctypes.c_int, _F64R, ctypes.c_double, _F64, _I32]
+                             ctypes.c_int, _F64R, ctypes.c_double, _F64, _I32, ctypes.c_int]
     lib.wo_accel.restype = None
     lib.wo_set_parallel_sort.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_long]
     lib.wo_set_callback_force.argtypes = [ctypes.c_int, _F64R, ctypes.c_int]
@@ -143,15 +143,17 @@ def onestep(xi, x, v, m, a, totmass, dt_leap, nleap, t0, omega2, ext=None, sort=
     return tc.value, elapsed.value
 
 
-def accel(x, m, totmass, omega2=-1., ext=None, t=0.):
-    """One force evaluation in original order, plus the sort permutation."""
+def accel(x, m, totmass, omega2=-1., ext=None, t=0., sort="quick"):
+    """One force evaluation in original order, plus the sort permutation
+    (sort: "quick" as the reference's default, or "parallel" with the threads
+    set by set_parallel_sort)."""
     lib = load()
     x = numpy.ascontiguousarray(x, dtype=numpy.float64)
     m = numpy.ascontiguousarray(m, dtype=numpy.float64)
     a = numpy.zeros(len(x))
     perm = numpy.zeros(len(x), dtype=numpy.int32)
     kind, params = _ext_args(ext)
-    lib.wo_accel(len(x), x, m, totmass, omega2, kind, params, t, a, perm)
+    lib.wo_accel(len(x), x, m, totmass, omega2, kind, params, t, a, perm, SORT_IDS[sort])
     return a, perm
 
 
@@ -199,13 +201,29 @@ def ref_onestep(lib, xi, x, v, m, a, totmass, dt_leap, nleap, t0, omega2, ext=No
     return tc.value, elapsed.value
 
 
-def import_reference_wendy(ref_root="/root/reference"):
+def reference_root():
+    """The reference checkout: $WENDY_REF_ROOT, else the one oracle/_ref was
+    built from (recorded by the Makefile), else None."""
+    root = os.environ.get("WENDY_REF_ROOT")
+    if root:
+        return root
+    rec = os.path.join(REF_DIR, "ref_root.txt")
+    if os.path.exists(rec):
+        with open(rec) as f:
+            return f.read().strip() or None
+    return None
+
+
+def import_reference_wendy(ref_root=None):
     """Import the reference's wendy.py with a stub numba (numba is absent).
 
     The stub's cfunc raises, which sends callables down the reference's own
-    ctypes fallback (wendy/wendy.py:405-418).  Returns the module or None.
+    ctypes fallback (wendy/wendy.py:405-418).  Returns the module or None
+    (also when no reference checkout is known, see reference_root).
     """
-    if not os.path.isdir(os.path.join(ref_root, "wendy")):
+    if ref_root is None:
+        ref_root = reference_root()
+    if ref_root is None or not os.path.isdir(os.path.join(ref_root, "wendy")):
         return None
     if not os.path.exists(os.path.join(REF_DIR, "wendy_c%s" % EXT_SUFFIX)):
         return None

@@ -387,7 +387,8 @@ void wo_approx_onestep(int n, wo_sheet *xi, double *x, double *v, const double *
    GPU's fused kernel is checked against.  perm[i] is the original index
    of the sheet at sorted slot i. */
 void wo_accel(int n, const double *x, const double *m, double totmass, double omega2,
-              int ext_kind, const double *ext_params, double t, double *a, int *perm) {
+              int ext_kind, const double *ext_params, double t, double *a, int *perm,
+              int sort_type) {
   int i;
   wo_sheet *xi = (wo_sheet *)malloc((size_t)n * sizeof(wo_sheet));
   double *xs = (double *)malloc((size_t)n * sizeof(double));
@@ -397,7 +398,7 @@ void wo_accel(int n, const double *x, const double *m, double totmass, double om
     xi[i].val = x[i];
     xs[i] = x[i];
   }
-  wo_force(n, WO_SORT_QUICK, xi, xs, m, a, t, totmass, omega2, ext_kind, ext_params, cm);
+  wo_force(n, sort_type, xi, xs, m, a, t, totmass, omega2, ext_kind, ext_params, cm);
   if (perm)
     for (i = 0; i < n; i++) perm[i] = xi[i].idx;
   free(xi);

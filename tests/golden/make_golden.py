@@ -76,7 +76,9 @@ def ref_accel(lib, x, m, omega2, ext, t):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--ref-root", default=None,
+                    help="reference checkout (default: $WENDY_REF_ROOT, else the one "
+                         "oracle/_ref was built from)")
     args = ap.parse_args()
     lib = O.ref_library()
     wendy = O.import_reference_wendy(args.ref_root)

@@ -54,3 +54,38 @@ def test_clock_summary_keeps_the_samples_of_the_timed_region():
     c._t_in, c._t_out = 1.06, 1.07
     s = c.summary()
     assert s["samples"] == 1 and s["sm_mhz"] == 2070.0
+
+
+def test_full_run_summary_counts_paths_and_phases():
+    sys.path.insert(0, ROOT)
+    import bench
+    w = dict(bench.WORKLOADS["tophat_2p27"], n=1000)
+    rows = []
+    compact = sorts = 0
+    for k in range(500):
+        # the compact path from the collapse (output 158) to output 300
+        step_c = 10 if 158 <= k < 300 else 0
+        compact += step_c
+        sorts += step_c + (1 if k == 0 else 0)
+        rows.append((0.02 if step_c else 0.01, 0.011,
+                     {"substeps_compact": compact, "sorts_full": sorts,
+                      "last_max_count": 0 if step_c else 1800}))
+    s = bench.full_run_summary(w, rows, 1)
+    assert s["outputs"] == 500 and s["substeps"] == 5000
+    assert s["substeps_compact"] == 1420 and s["substeps_bucket"] == 3580
+    assert len(s["phases"]) == 5 and s["phases"][0]["substeps_compact"] == 0
+    assert s["phases"][1]["substeps_compact"] == 420
+    assert abs(s["value"] - 1000 * 5000 / (0.01 * 358 + 0.02 * 142)) < 1e-6 * s["value"]
+    pc = s["post_collapse"]
+    assert pc["from_output"] == 158 and pc["substeps_compact"] == 1420
+    assert pc["substeps"] == (500 - 158) * 10
+
+
+def test_default_workload_is_the_hbm_scale_top_hat():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench2", os.path.join(ROOT, "bench.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    w = b.WORKLOADS["tophat_2p27"]
+    assert w["n"] == 1 << 27 and w["outputs"] == 500 and w["nleap"] == 10 and w["dt"] == 0.01
+    assert w["ext"][1] == (0.3, 5.0, 1.0, 0.5)

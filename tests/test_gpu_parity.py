@@ -210,12 +210,16 @@ def test_trajectories_match_reference_golden(golden):
             tx, tv = next(gen)
             if k in keep:
                 rx, rv = g["%s/x%d" % (name, k)], g["%s/v%d" % (name, k)]
-                # one output of nleap sub-steps: 1e-10; later outputs allow the
-                # (chaotic) growth of the rounding differences by 10x per output
-                tol = 1e-10 * (10.0 ** (k - 1)) if k > 1 else 1e-10
-                tol = min(tol, 1e-6)
-                assert numpy.max(numpy.abs(tx - rx)) <= tol, (name, k)
-                assert numpy.max(numpy.abs(tv - rv)) <= tol, (name, k)
+                # The only difference from the reference is the rounding of its
+                # serial mass sum (the GPU's is exact): ~1e-16 relative in the
+                # accelerations per sub-step.  Measured on a GB300 over these
+                # runs (up to 10 outputs, 10 000 sub-steps): at most 3.5e-14 in
+                # x and 1.0e-13 in v (cfg1, output 10).  The bar is 1e-11 for
+                # every output: two orders of magnitude above that for the
+                # growth of rounding differences in these (chaotic) systems,
+                # and below the 1e-10 required after one output.
+                assert numpy.max(numpy.abs(tx - rx)) <= 1e-11, (name, k)
+                assert numpy.max(numpy.abs(tv - rv)) <= 1e-11, (name, k)
 
 
 def test_stateless_step_matches_oracle():
@@ -425,3 +429,43 @@ def test_repeated_overflow_falls_back_and_recovers():
         assert numpy.max(numpy.abs(gv - rv)) <= 1e-9
     assert sim.stats()["sorts_full"] > 2
     sim.close()
+
+
+def test_generator_in_place_edits_of_v():
+    # wendy's C step reads the yielded v on every call (wendy/wendy.c:318-333)
+    # and only writes x (wendy/wendy.c:413-415).  By default the GPU
+    # generator ignores edits of v (its next output is computed ahead);
+    # follow_edits=True honours them like the reference, and edits of x are
+    # ignored either way.
+    n = 20000
+    x, v, m = ics.sech2_disk(n, seed=41, masses="lognormal")
+    runs = {}
+    for mode in ("oracle", "follow", "default"):
+        if mode == "oracle":
+            g = O.nbody_approx(x, v, m, 0.02, 10, omega=1.1)
+        else:
+            g = wendy_gb300.nbody(x, v, m, 0.02, approx=True, nleap=10, omega=1.1,
+                                  follow_edits=(mode == "follow"))
+        out = []
+        for k in range(4):
+            tx, tv = next(g)
+            out.append((tx.copy(), tv.copy()))
+            if k == 1:
+                tv *= 0.5          # edit v in place
+                tx += 0.25         # and x, which has no effect
+        runs[mode] = out
+        if mode != "oracle":
+            g.close()
+    for (fx, fv), (rx, rv) in zip(runs["follow"], runs["oracle"]):
+        assert numpy.max(numpy.abs(fx - rx)) <= 1e-10
+        assert numpy.max(numpy.abs(fv - rv)) <= 1e-10
+    # without follow_edits the edits are ignored: outputs 3 and 4 are those of
+    # an undisturbed run
+    g = wendy_gb300.nbody(x, v, m, 0.02, approx=True, nleap=10, omega=1.1)
+    for k in range(4):
+        ux, uv = next(g)
+        if k >= 2:
+            dx, dv = runs["default"][k]
+            assert numpy.array_equal(dx, ux) and numpy.array_equal(dv, uv)
+    g.close()
+    assert numpy.max(numpy.abs(runs["follow"][3][1] - runs["default"][3][1])) > 1e-3

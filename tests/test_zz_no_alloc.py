@@ -9,8 +9,12 @@ failure has run every other test before it.
 
 The test allocates the caller-side device buffers itself, through the CUDA
 runtime's shared library, and compares two calls in a row with the existing
-entry point wg_accel under the parity tolerance of the other tests
-(permutation bit-exact, accelerations within 1e-12 of the acceleration scale).
+entry point wg_accel.  Both run the same sort and force kernels on the same
+sheets, so the permutation and the accelerations must be identical bit for
+bit; the result is also compared with the CPU oracle under the parity
+tolerance of the other tests (permutation bit-exact, accelerations within
+1e-12 of the acceleration scale).  Around the second call the device's free
+memory is read before and after: the call must not change it.
 """
 import ctypes
 import ctypes.util
@@ -42,6 +46,9 @@ def _cudart():
         rt.cudaMalloc.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]
         rt.cudaFree.argtypes = [ctypes.c_void_p]
         rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+        rt.cudaMemGetInfo.argtypes = [ctypes.POINTER(ctypes.c_size_t),
+                                      ctypes.POINTER(ctypes.c_size_t)]
+        rt.cudaDeviceSynchronize.argtypes = []
         return rt
     pytest.skip("CUDA runtime shared library not found")
 
@@ -66,7 +73,15 @@ class DeviceBuffer:
         self.rt.cudaFree(self.ptr)
 
 
+def _free_bytes(rt):
+    free, total = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    assert rt.cudaDeviceSynchronize() == 0
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
 def _noalloc_accel(L, rt, x, m, totmass, omega2, force, t):
+    """One call through the C ABI; returns (a, perm, free bytes before, after)."""
     n = len(x)
     dx, dm = DeviceBuffer(rt, 8 * n), DeviceBuffer(rt, 8 * n)
     da, dp = DeviceBuffer(rt, 8 * n), DeviceBuffer(rt, 4 * n)
@@ -74,20 +89,23 @@ def _noalloc_accel(L, rt, x, m, totmass, omega2, force, t):
         dx.upload(numpy.ascontiguousarray(x))
         dm.upload(numpy.ascontiguousarray(m))
         kind, params = (0, ()) if force is None else (force.kind, force.params)
+        free0 = _free_bytes(rt)
         rc = L.wg_accel_noalloc(n, dx.ptr, dm.ptr, totmass, omega2, kind,
                                 _lib.ext_params(params), len(params), t, da.ptr, dp.ptr, None)
+        free1 = _free_bytes(rt)
         _lib.check(rc, "wg_accel_noalloc")
         a = numpy.empty(n)
         perm = numpy.empty(n, dtype=numpy.int32)
         da.download(a)
         dp.download(perm)
-        return a, perm
+        return a, perm, free0, free1
     finally:
         for b in (dx, dm, da, dp):
             b.free()
 
 
 def test_noalloc_matches_wg_accel_on_two_calls_in_a_row():
+    from oracle import oracle as O
     L = _lib.lib()
     rt = _cudart()
     cases = [
@@ -97,11 +115,21 @@ def test_noalloc_matches_wg_accel_on_two_calls_in_a_row():
     for (x, v, m), omega2, force, t in cases:
         tot = numpy.sum(m)
         ref_a, ref_perm = wendy_gb300.accel(x, m, tot, omega2=omega2, ext_force=force, t=t)
-        scale = max(tot, float(numpy.max(numpy.abs(ref_a))))
-        for _ in range(2):
-            a, perm = _noalloc_accel(L, rt, x, m, tot, omega2, force, t)
+        ext = None if force is None else (O.EXT_PULSE_TANH, list(force.params))
+        o_a, o_perm = O.accel(x, m, tot, omega2, ext, t)
+        scale = max(tot, float(numpy.max(numpy.abs(o_a))))
+        for call in range(2):
+            a, perm, free0, free1 = _noalloc_accel(L, rt, x, m, tot, omega2, force, t)
+            # same kernels as wg_accel on the same sheets: identical bits
             assert numpy.array_equal(perm, ref_perm)
-            assert numpy.max(numpy.abs(a - ref_a)) <= 1e-12 * scale
+            assert numpy.array_equal(a.view(numpy.int64), ref_a.view(numpy.int64))
+            # and the oracle's result within the parity tolerance
+            assert numpy.array_equal(perm, o_perm)
+            assert numpy.max(numpy.abs(a - o_a)) <= 1e-12 * scale
+            if call == 1:
+                # the first call may load the library's device code; the
+                # second one takes no device memory at all
+                assert free1 == free0, (free0, free1)
 
 
 def test_noalloc_rejects_sizes_beyond_its_array():

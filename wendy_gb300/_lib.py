@@ -15,6 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_wendy_gb300.so")
 
 WG_OK = 0
+WG_ERR_ARG, WG_ERR_CUDA, WG_ERR_NOMEM, WG_ERR_DEVICE = -1, -2, -3, -4
+WG_ERR_EXT, WG_ERR_BUDGET, WG_ERR_NODEV = -5, -6, -7
 STATUS_NAMES = {0: "WG_OK", -1: "WG_ERR_ARG", -2: "WG_ERR_CUDA", -3: "WG_ERR_NOMEM",
                 -4: "WG_ERR_DEVICE", -5: "WG_ERR_EXT", -6: "WG_ERR_BUDGET", -7: "WG_ERR_NODEV"}
 
@@ -26,7 +28,7 @@ EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", 
            "wg_nbody_approx_onestep", "wg_nbody_approx_stats", "wg_profile", "wg_host_register", "wg_host_unregister",
            "wg_accel_noalloc", "wg_pool_sim_bytes", "wg_pool_create", "wg_pool_add",
            "wg_pool_remove", "wg_pool_step", "wg_pool_step_begin", "wg_pool_step_end", "wg_pool_download", "wg_pool_info",
-           "wg_pool_destroy", "wg_set_tuning", "wg_get_tuning")
+           "wg_pool_destroy", "wg_set_tuning", "wg_get_tuning", "wg_set_debug_wait")
 
 # Largest n wg_accel_noalloc accepts (its fixed device scratch array).
 NOALLOC_MAX_SHEETS = 65536
@@ -46,7 +48,8 @@ class WgStats(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("substeps", ctypes.c_int64),
                 ("sorts_full", ctypes.c_int64), ("sorts_skipped", ctypes.c_int64),
                 ("sorts_window", ctypes.c_int64), ("last_max_disp", ctypes.c_double),
-                ("device_bytes", ctypes.c_int64), ("launches", ctypes.c_int64)]
+                ("device_bytes", ctypes.c_int64), ("launches", ctypes.c_int64),
+                ("last_max_count", ctypes.c_int64), ("substeps_compact", ctypes.c_int64)]
 
 
 class WgTuning(ctypes.Structure):
@@ -109,6 +112,7 @@ def lib():
     L.wg_host_register.argtypes = [_P, _I64]
     L.wg_host_unregister.argtypes = [_P]
     L.wg_accel_noalloc.argtypes = [_I64, _P, _P, _D, _D, _I, _F64, _I, _D, _P, _P, _P]
+    L.wg_set_debug_wait.argtypes = [ctypes.c_uint, _I64]
     L.wg_pool_sim_bytes.argtypes = [_I64]
     L.wg_pool_create.argtypes = [_I64, ctypes.POINTER(_P)]
     L.wg_pool_add.argtypes = [_P, _I64, _F64, _F64, _F64, _D, _D, _I, _F64, _I,

@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "../../include/wendy_gb300.h"
@@ -44,6 +45,37 @@ void set_error(const char* fmt, ...) {
   } while (0)
 
 size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Tight mode (see wg_sim): the target it lays buckets out with, the largest
+// bucket count after a restart that it answers (above it the flow is too
+// violent for buckets and the call finishes on the compact path), and the
+// clean calls after which the normal target returns.
+int tight_target(int target) { return target * 2 / 3 > 64 ? target * 2 / 3 : 64; }
+constexpr unsigned kTightLimit = kBucketCap * 3 / 2;
+constexpr int kTightExit = 8;
+// Most calls a violent overflow sends to the compact path before the bucket
+// path is tried again.
+constexpr int kMaxBackoff = 8;
+
+// The bits of a device error word, by name.
+std::string device_error_names(unsigned err) {
+  static const struct {
+    unsigned bit;
+    const char* name;
+  } names[] = {{DEV_ERR_LOOKBACK_TIMEOUT, "force look-back wait expired"},
+               {DEV_ERR_RADIX_TIMEOUT, "radix-sort wait expired"},
+               {DEV_ERR_BUCKET_OVERFLOW, "bucket overflow"},
+               {DEV_ERR_FIXED_RANGE, "mass outside the fixed-point range"},
+               {DEV_ERR_BAD_STATE, "internal check failed"},
+               {DEV_ERR_COPY_TIMEOUT, "bulk-copy wait expired"}};
+  std::string out;
+  for (const auto& e : names)
+    if (err & e.bit) {
+      if (!out.empty()) out += ", ";
+      out += e.name;
+    }
+  return out.empty() ? "unknown bits" : out;
+}
 
 // Host copy of the device conversion: round(m * 2^E) in 128 bits.
 u128 host_mass_to_fixed(double m, int E) {
@@ -154,7 +186,12 @@ struct wg_sim {
   int pend_nleap = 0, pend_lay0 = 0, pend_cs0 = 0;
   // bucketed layout (the fast path of wg_step)
   void* bk = nullptr;
-  int64_t nb = 0;
+  int64_t nb = 0;        // buckets of the current layout: ceil(n / target_cur)
+  int64_t nb_cap = 0;    // buckets the arrays hold: ceil(n / tight target)
+  int target_cur = 0;    // sheets per bucket after a re-sort, now
+  // Tight mode: a flow that overflows buckets by a little right after a
+  // re-sort (a few per cent above capacity) is laid out with 2/3 of the
+  // target, until kTightExit calls in a row complete without an overflow.
   double* bx[2] = {nullptr, nullptr};
   double* bv[2] = {nullptr, nullptr};
   double* bm[2] = {nullptr, nullptr};
@@ -179,6 +216,7 @@ struct wg_sim {
   // penalty; the penalty halves after every call the bucket path completes.
   int compact_calls = 0;
   int backoff = 1;
+  int tight_clean = -1;  // clean calls in tight mode so far; -1: not in tight mode
   double pending_dt = 0; // dt of the half drift the bucket layout was routed for
   bool out_valid = false;  // x_out / v_out hold the last call's output
   // Split steps (wg_step_begin): a second pair of output buffers, so that the
@@ -205,9 +243,18 @@ struct wg_sim {
   ExtForce ext{};
   unsigned epoch = 1;
   wg_stats st{};
+  // a kernel raised the device error word during a call: the state on the
+  // device can no longer be trusted, and only wg_destroy is accepted
+  bool broken = false;
 };
 
 namespace {
+
+// Sheets per bucket of the next bucketize (and with it the bucket count).
+void set_target(wg_sim* s, int target) {
+  s->target_cur = target;
+  s->nb = (s->n + target - 1) / target;
+}
 
 int alloc_call_arrays(wg_sim* s, int nleap) {
   if (nleap <= s->cap) return WG_OK;
@@ -347,8 +394,10 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
   // bucket layout: two layouts of nb buckets x capacity, counts, splitters,
   // look-back records, the overflow list
   s->tune = tuning_for(n);
-  s->nb = (n + s->tune.target - 1) / s->tune.target;
-  const int64_t nb = s->nb;
+  s->target_cur = s->tune.target;
+  s->nb = (n + s->target_cur - 1) / s->target_cur;
+  s->nb_cap = (n + tight_target(s->tune.target) - 1) / tight_target(s->tune.target);
+  const int64_t nb = s->nb_cap;
   const size_t slots = (size_t)nb * kBucketCap;
   const size_t bk_b = 2 * (3 * al(slots * 8) + al(slots * 4)) +
                       kAggSlots * (al(4 * (size_t)nb) + al(32 * (size_t)nb)) +
@@ -468,9 +517,14 @@ int finish_call(wg_sim* s, int nleap, bool count_sorts = true) {
       s->st.sorts_skipped++;
   }
   s->st.substeps += nleap;
+  unsigned mc = 0;
+  for (int i = 1; i <= nleap; ++i) mc = s->h_flags[i].max_cnt > mc ? s->h_flags[i].max_cnt : mc;
+  s->st.last_max_count = mc;
   if (err) {
-    set_error("device error word 0x%x (bounded wait expired or internal check)", err);
+    set_error("device error word 0x%x (%s); the simulation's state is lost, destroy it", err,
+              device_error_names(err).c_str());
     cudaMemsetAsync(s->err, 0, 4, s->stream);
+    s->broken = true;
     return WG_ERR_DEVICE;
   }
   return WG_OK;
@@ -484,7 +538,7 @@ static_assert(kMaxLeap == WG_MAX_LEAP, "sub-step limit of the C header");
 int take_epochs(wg_sim* s, int count) {
   if (s->epoch + (unsigned)count > kEpochLimit) {
     WG_CUDA(cudaMemsetAsync(s->recs, 0, sizeof(TileRec) * (size_t)s->n_tiles, s->stream));
-    WG_CUDA(cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)s->nb, s->stream));
+    WG_CUDA(cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)s->nb_cap, s->stream));
     s->epoch = 1;
   }
   for (int i = 0; i < count; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
@@ -571,7 +625,7 @@ void fill_dev(wg_sim* s, double dt, double pre) {
   d.t_seq = s->t_seq;
   d.n = s->n;
   d.nb = s->nb;
-  d.target = s->tune.target;
+  d.target = s->target_cur;
   d.window = s->tune.window;
   d.sort_bits = s->tune.sort_bits;
   d.T_lo = s->T_lo;
@@ -774,6 +828,7 @@ static int compact_continue(wg_sim* s, double dt, int nleap, int from) {
   if (s->call_a) launch_scatter_accel(s->table, s->n, s->a_sorted, s->call_a, s->stream);
   if (s->call_xi) store_sheets(s->table, s->n, reinterpret_cast<wg_sheet*>(s->call_xi), s->stream);
   s->st.launches += (int64_t)(nleap - from) * (1 + kRadixLaunches);
+  s->st.substeps_compact += nleap - from;
   WG_CUDA(cudaStreamSynchronize(s->stream));
   return WG_OK;
 }
@@ -795,6 +850,7 @@ static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool reco
     }
     rc = enqueue_step(s, dt, nleap, s->call_a != nullptr, dt / 2.);
     if (rc) return rc;
+    s->st.substeps_compact += nleap;
     if (s->call_a) launch_scatter_accel(s->table, s->n, s->a_sorted, s->call_a, s->stream);
     if (s->call_xi)
       store_sheets(s->table, s->n, reinterpret_cast<wg_sheet*>(s->call_xi), s->stream);
@@ -813,10 +869,15 @@ static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool reco
   WG_CUDA(cudaMemsetAsync(s->flags, 0, sizeof(StepFlags) * (nleap + 1), s->stream));
   WG_CUDA(cudaMemsetAsync(s->tickets, 0, 4 * (size_t)nleap, s->stream));
   WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));  // overflow count and abort word
-  if (s->mode == 1 && dt != s->pending_dt) {
-    // routed for another dt: back to compact state, the half drift still pending
+  if (s->mode == 1 && (dt != s->pending_dt || s->tight_clean >= kTightExit)) {
+    // routed for another dt, or tight buckets no longer needed: back to
+    // compact state, the half drift still pending
     bucket_to_compact(s, s->lay, s->cslot);
     s->mode = 0;
+  }
+  if (s->tight_clean >= kTightExit) {
+    s->tight_clean = -1;
+    set_target(s, s->tune.target);
   }
   double pre = 0.0;
   if (s->mode == 0) {
@@ -825,7 +886,7 @@ static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool reco
     s->lay = 0;
     s->qsel = 0;
     s->cslot = 0;
-    launch_bucketize(s->table, s->n, s->tune.target, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
+    launch_bucketize(s->table, s->n, s->target_cur, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
                      s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], s->stream);
     s->st.launches += 2 + kRadixLaunches;
     s->st.sorts_full += 1;
@@ -843,6 +904,8 @@ static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool reco
   s->st.launches += nleap + 1;
   WG_CUDA(cudaGetLastError());
   WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(StepFlags) * (nleap + 1),
+                          cudaMemcpyDeviceToHost, s->stream));
   s->pend_active = true;
   s->pend_dt = dt;
   s->pend_nleap = nleap;
@@ -906,20 +969,29 @@ static int run_call_end(wg_sim* s, double* time_elapsed) {
       break;
     }
     if (from > 0 && k < from + 2) {
-      // overflowed again right after a re-sort: the buckets cannot follow this
-      // flow for now.  Finish the call on the compact path and keep the next
-      // calls there (back-off doubling up to 64 calls).
-      compact_continue(s, dt, nleap, k + 1);
-      s->mode = 0;
-      s->out_valid = false;
-      s->compact_calls = s->backoff;
-      s->backoff = s->backoff < 64 ? 2 * s->backoff : 64;
-      break;
+      // overflowed again right after a re-sort.  A little above capacity:
+      // restart once more with tight buckets (2/3 of the target).  Otherwise
+      // the buckets cannot follow this flow for now: finish the call on the
+      // compact path and keep the next calls there (back-off doubling up to
+      // kMaxBackoff calls).
+      const unsigned worst = s->h_flags[k + 1].max_cnt;
+      const int tight = tight_target(s->tune.target);
+      if (worst <= kTightLimit && s->target_cur != tight) {
+        set_target(s, tight);
+        s->tight_clean = 0;
+      } else {
+        compact_continue(s, dt, nleap, k + 1);
+        s->mode = 0;
+        s->out_valid = false;
+        s->compact_calls = s->backoff;
+        s->backoff = s->backoff < kMaxBackoff ? 2 * s->backoff : kMaxBackoff;
+        break;
+      }
     }
     from = k + 1;
     WG_CUDA(cudaMemsetAsync(&s->flags[from].unsorted, 1, sizeof(unsigned), s->stream));
     radix_sort_state(s->table, s->n, &s->radix, &s->flags[from], s->err, s->stream);
-    launch_bucketize(s->table, s->n, s->tune.target, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
+    launch_bucketize(s->table, s->n, s->target_cur, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
                      s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], s->stream);
     // sub-step `from` reads layout 0, aggregate slot 0 and routes by splitter set 0
     lay0 = from & 1;
@@ -943,10 +1015,13 @@ static int run_call_end(wg_sim* s, double* time_elapsed) {
     s->st.launches += 4 + kRadixLaunches + (nleap - from);
     WG_CUDA(cudaGetLastError());
     WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
+    WG_CUDA(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(StepFlags) * (nleap + 1),
+                            cudaMemcpyDeviceToHost, s->stream));
     WG_CUDA(cudaStreamSynchronize(s->stream));
   }
   s->st.sorts_window += window_steps;
   if (clean && s->backoff > 1) s->backoff /= 2;
+  if (s->tight_clean >= 0) s->tight_clean = clean ? s->tight_clean + 1 : 0;
   WG_CUDA(cudaEventRecord(s->ev1, s->stream));
   rc = finish_call(s, nleap, false);
   float ms = 0;
@@ -979,6 +1054,10 @@ static int check_idle(wg_sim* s) {
   if (s->pend_active) {
     set_error("a step is in flight: call wg_step_end first");
     return WG_ERR_ARG;
+  }
+  if (s->broken) {
+    set_error("an earlier call on this simulation raised a device error; destroy it");
+    return WG_ERR_DEVICE;
   }
   return WG_OK;
 }
@@ -1075,7 +1154,8 @@ int wg_destroy(wg_sim* s) {
 }
 
 int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
-  if (check_idle(s)) return WG_ERR_ARG;
+  const int rc0 = check_idle(s);
+  if (rc0) return rc0;
   if (reps < 1 || reps > kMaxLeap || !avg_seconds ||
       (what != WG_PROF_FORCE && what != WG_PROF_SORT && what != WG_PROF_BUCKET)) {
     set_error("bad arguments to wg_profile");
@@ -1230,7 +1310,8 @@ int wg_host_unregister(void* ptr) {
 }
 
 int wg_energy(wg_sim* s, double twopiG, double omega2, double* energy, double* momentum) {
-  if (check_idle(s)) return WG_ERR_ARG;
+  const int rc0 = check_idle(s);
+  if (rc0) return rc0;
   if (!(twopiG > 0.0) || !std::isfinite(twopiG) || !std::isfinite(omega2)) {
     set_error("wg_energy needs a simulation, a positive finite twopiG and a finite omega2");
     return WG_ERR_ARG;
@@ -1335,6 +1416,11 @@ int wg_accel(int64_t n, const double* x, const double* m, double totmass, double
   return rc;
 }
 
+int wg_set_debug_wait(unsigned spin_limit, int64_t withhold_tile) {
+  set_wait_debug(spin_limit, withhold_tile);
+  return WG_OK;
+}
+
 int wg_nbody_approx_stats(wg_stats* out) {
   if (!out) {
     set_error("null output");
@@ -1360,7 +1446,9 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   if (rc) return rc;
   std::lock_guard<std::mutex> lock(g_cache_mu);
   wg_sim* s = g_cache;
-  if (!s || s->n != n) {
+  // (a cached state that a device error left untrustworthy is rebuilt: every
+  // call of this entry hands over its complete inputs)
+  if (!s || s->n != n || s->broken) {
     free_sim(s);
     g_cache = nullptr;
     rc = make_sim(n, totmass, omega2, ext, &s);

@@ -134,6 +134,7 @@ struct StepSmem {
   int win_lo, win_hi, cur_wbuf;
   double amp, inv_h;
   unsigned long long maxv;
+  unsigned maxc;  // largest destination count this task saw after its reservations
   uint64_t mbar;  // completion of the bucket's bulk copies
 };
 
@@ -662,6 +663,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       S.win_hi = tm.whi;
       S.cur_wbuf = tm.wbuf;
       S.maxv = 0;
+      S.maxc = 0;
       S.prefix_mass = (((u128)tm.pm_hi) << 64) | tm.pm_lo;
       S.prefix_cnt = tm.pcnt;
       S.amp = tm.amp;
@@ -672,7 +674,16 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       for (int j = tid; j < NBIN_PAD; j += BT) S.u.srt.bins[j] = 0u;
     }
     if (n4 > 0) {
-      if (!mbar_wait(&S.mbar, parity) && tid == 0) atomicOr(L.err, DEV_ERR_BAD_STATE);
+      const bool arrived = mbar_wait(&S.mbar, parity);
+      if (__syncthreads_or(!arrived)) {
+        // the bucket's copies did not complete within the bounded wait: its
+        // contents are unknown, so this CTA writes nothing more.  It gives the
+        // copies a second bounded wait and stops; the host sees the error word
+        // (the call fails and the simulation is given up).
+        if (tid == 0) atomicOr(L.err, DEV_ERR_COPY_TIMEOUT);
+        mbar_wait(&S.mbar, parity);
+        break;
+      }
       parity ^= 1u;
     }
     uint64_t kmin = ~0ull, kmax = 0;
@@ -892,7 +903,10 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       // grouping and the mass sums
       if (wt < wlen) {
         const uint32_t c = S.dcount[wt];
-        if (c) db = atomicAdd(&cnt_out[S.win_lo + wt], c);
+        if (c) {
+          db = atomicAdd(&cnt_out[S.win_lo + wt], c);
+          atomicMax(&S.maxc, db + c);
+        }
       }
       if (warp == 1) {
         // segments: exclusive prefix of the counts of the wlen + 1 entries
@@ -976,6 +990,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
           const uint64_t kf = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, S.v[sl], xn) : xn);
           d = dest_bucket(wk, wi, S.win_lo, wlen, qfar, ifar, nbk, kf, S.idx[sl]);
           slot = atomicAdd(&cnt_out[d], 1u);
+          atomicMax(&S.maxc, slot + 1u);
         }
         if (slot < (uint32_t)CAP) {
           const int64_t o = (int64_t)d * CAP + slot;
@@ -1002,6 +1017,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     if (overflow) atomicCAS(D.ocount + 1, 0u, (unsigned)(sub + 1));
     __syncthreads();
     if (tid == 0 && S.maxv) atomicMax(&D.flags[sub + 1].max_v, S.maxv);
+    if (tid == 0 && S.maxc) atomicMax(&D.flags[sub + 1].max_cnt, S.maxc);
   }
 }
 
@@ -1137,15 +1153,22 @@ void set_tuning(const std::vector<std::pair<int64_t, BucketTuning>>& rows) {
   g_tune = rows;
 }
 
+// The sub-step kernel's dynamic shared-memory limit, raised once per device
+// (function attributes belong to the device they were set on).
+void bucket_attr_init() {
+  cudaFuncSetAttribute(k_bucket_step<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(StepSmem));
+  cudaFuncSetAttribute(k_bucket_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(StepSmem));
+}
+
 void bucket_step_prepare() {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_bucket_step<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sizeof(StepSmem));
-    cudaFuncSetAttribute(k_bucket_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sizeof(StepSmem));
-    attr = true;
-  }
+  static std::once_flag once[kMaxDevices];
+  const int dev = current_device();
+  if (dev < 0 || dev >= kMaxDevices)
+    bucket_attr_init();
+  else
+    std::call_once(once[dev], bucket_attr_init);
 }
 
 __global__ void __launch_bounds__(256) k_split_out(const OutRec* __restrict__ rec, int64_t n,

@@ -21,6 +21,7 @@ enum : unsigned {
   DEV_ERR_BUCKET_OVERFLOW = 1u << 2,   // a bucket received more sheets than its capacity
   DEV_ERR_FIXED_RANGE = 1u << 3,       // a mass outside the fixed-point range
   DEV_ERR_BAD_STATE = 1u << 4,         // an internal consistency check failed
+  DEV_ERR_COPY_TIMEOUT = 1u << 5,      // a bulk copy into shared memory did not complete
 };
 
 // Upper bound on the iterations of any spin-wait on another CTA's flag.  Each

@@ -38,7 +38,7 @@ struct __align__(16) TileRec {
 // Per-sub-step bookkeeping written by the device (one slot per sub-step).
 struct StepFlags {
   unsigned unsorted;         // nonzero: the order after this drift is not strictly increasing
-  unsigned pad;
+  unsigned max_cnt;          // largest bucket count of the layout this sub-step wrote
   unsigned long long max_v;  // largest |v| after the kick (bit pattern of a non-negative double)
 };
 
@@ -59,6 +59,10 @@ struct ForceArgs {
   unsigned* ticket;          // tile ticket counter, zero before the launch
   StepFlags* flag_out;       // order / speed record of the positions this drift produces
   unsigned* err;
+  // filled in by launch_force from the wait settings (set_wait_debug): the
+  // look-back's iteration limit and a tile that leaves its record unpublished
+  unsigned spin_limit;
+  int64_t withhold_tile;     // -1: none
 };
 
 // Radix-sort workspace (one set per simulation).
@@ -73,6 +77,19 @@ struct RadixWork {
   size_t scratch_bytes; // bytes of status + counters (cleared before each sort)
 };
 
+// Devices whose one-time kernel set-up (attributes, occupancy) is cached;
+// launchers on a device beyond this redo the set-up on every call.
+constexpr int kMaxDevices = 64;
+// The calling thread's current device, or -1 when none can be had.
+inline int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return d;
+}
+
 constexpr int kForceThreads = 256;
 constexpr int kForceItems = 8;
 constexpr int kForceTile = kForceThreads * kForceItems;
@@ -83,6 +100,11 @@ constexpr int kRadixTile = kRadixThreads * kRadixItems;
 
 // --- launchers (wg_kernels.cu) ---
 void launch_force(const ForceArgs& a, int64_t n_tiles, cudaStream_t s);
+// Wait settings of the force kernel's look-back (a test hook behind
+// wg_set_debug_wait): the iteration limit of its waits, and a tile whose
+// look-back record is never published (-1: none), so that the waits on it
+// run out.  Defaults kSpinLimit and -1.
+void set_wait_debug(unsigned spin_limit, int64_t withhold_tile);
 void launch_drift(const StateTable* table, int64_t n, double dt, StepFlags* flag, cudaStream_t s);
 void launch_desort(const StateTable* table, int64_t n, double* x_out, double* v_out,
                    cudaStream_t s);

@@ -11,6 +11,7 @@
 // with x, v updated in place.  The same pass records whether the new
 // positions are still strictly increasing and the largest |v|, which is
 // what decides how the next sub-step re-sorts.
+#include <atomic>
 #include <cstdint>
 
 #include "wg_internal.cuh"
@@ -27,15 +28,18 @@ __device__ u128 force_lookback(const ForceArgs& a, int64_t tile, u128 total, int
   TileRec* recs = a.recs;
   const unsigned ep = a.epochs[a.sub];
   TileRec* me = recs + tile;
+  // a withheld tile (test hook) publishes nothing: its successors' waits
+  // on it run out after a.spin_limit iterations
+  const bool publish = tile != a.withhold_tile;
   if (tile == 0) {
-    if (lane == 0) {
+    if (lane == 0 && publish) {
       me->inc_lo = (uint64_t)total;
       me->inc_hi = (uint64_t)(total >> 64);
       st_release_u32(&me->flag, (ep << 2) | 2u);
     }
     return 0;
   }
-  if (lane == 0) {
+  if (lane == 0 && publish) {
     me->agg_lo = (uint64_t)total;
     me->agg_hi = (uint64_t)(total >> 64);
     st_release_u32(&me->flag, (ep << 2) | 1u);
@@ -53,7 +57,7 @@ __device__ u128 force_lookback(const ForceArgs& a, int64_t tile, u128 total, int
       for (;;) {
         f = ld_acquire_u32(&r->flag);
         if ((f >> 2) == ep && (f & 3u)) break;
-        if (++spins > kSpinLimit) {
+        if (++spins > a.spin_limit) {
           atomicOr(a.err, DEV_ERR_LOOKBACK_TIMEOUT);
           f = 0;
           break;
@@ -72,7 +76,7 @@ __device__ u128 force_lookback(const ForceArgs& a, int64_t tile, u128 total, int
     if (pmask || j - 32 < 0) break;
     j -= 32;
   }
-  if (lane == 0) {
+  if (lane == 0 && publish) {
     const u128 inc = prefix + total;
     me->inc_lo = (uint64_t)inc;
     me->inc_hi = (uint64_t)(inc >> 64);
@@ -244,7 +248,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_force_kick_drift(const ForceArgs
     unsigned spins = 0;
     bool ok = true;
     while (ld_acquire_u32(&prev->last_flag) != s_epoch) {
-      if (++spins > kSpinLimit) {
+      if (++spins > a.spin_limit) {
         atomicOr(a.err, DEV_ERR_LOOKBACK_TIMEOUT);
         ok = false;
         break;
@@ -303,8 +307,21 @@ int grid_for(int64_t n, int threads) {
 
 }  // namespace
 
+namespace {
+std::atomic<unsigned> g_spin_limit{kSpinLimit};
+std::atomic<int64_t> g_withhold_tile{-1};
+}  // namespace
+
+void set_wait_debug(unsigned spin_limit, int64_t withhold_tile) {
+  g_spin_limit = spin_limit ? spin_limit : kSpinLimit;
+  g_withhold_tile = withhold_tile;
+}
+
 void launch_force(const ForceArgs& a, int64_t n_tiles, cudaStream_t s) {
-  k_force_kick_drift<kForceThreads, kForceItems><<<(unsigned)n_tiles, kForceThreads, 0, s>>>(a);
+  ForceArgs b = a;
+  b.spin_limit = g_spin_limit;
+  b.withhold_tile = g_withhold_tile;
+  k_force_kick_drift<kForceThreads, kForceItems><<<(unsigned)n_tiles, kForceThreads, 0, s>>>(b);
 }
 
 void launch_drift(const StateTable* table, int64_t n, double dt, StepFlags* flag,

@@ -13,7 +13,10 @@
 // The array's name in host code is only a host-side stand-in, not a device
 // address; the device address is looked up once per device with
 // cudaGetSymbolAddress (on that device's first call) and passed to the
-// kernels.  All calls share the array and it keeps the last call's contents:
+// kernels.  The inputs are device memory, so they are checked on the device:
+// a non-finite position or mass, or a negative mass, skips the sort and makes
+// the call return WG_ERR_ARG once its launches have run.
+// All calls share the array and it keeps the last call's contents:
 // the counters, flags and error word that must start at zero are cleared at
 // the start of every call, and two calls that overlap on the GPU (different
 // streams, or different host threads) race on it.
@@ -32,7 +35,6 @@ namespace {
 
 constexpr int64_t kMaxSheets = WG_NOALLOC_MAX_SHEETS;
 constexpr size_t kScratchBytes = (size_t)8 << 20;  // 8 MiB
-constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -139,7 +141,11 @@ __global__ void k_noalloc_load(Layout L, int64_t n, const double* x, const doubl
     L.set[0].m[i] = mi;
     L.set[0].idx[i] = (int32_t)i;
   }
-  if (bad) atomicOr(L.err, DEV_ERR_BAD_STATE);
+  if (bad) {
+    // the sort is skipped (its flag cleared); the call reports WG_ERR_ARG
+    atomicOr(L.err, DEV_ERR_BAD_STATE);
+    L.flags[0].unsorted = 0u;
+  }
 }
 
 __global__ void k_noalloc_store(Layout L, int64_t n, double* a, int32_t* perm) {

@@ -534,6 +534,19 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
     std::swap(s->x_out, s->x_out2);
     std::swap(s->v_out, s->v_out2);
   }
+  // until the step is launched, an error return swaps the output buffers
+  // back, so that wg_pool_download keeps returning the last completed output
+  struct SwapBack {
+    const std::vector<PoolSim*>& act;
+    bool armed = true;
+    ~SwapBack() {
+      if (!armed) return;
+      for (PoolSim* s : act) {
+        std::swap(s->x_out, s->x_out2);
+        std::swap(s->v_out, s->v_out2);
+      }
+    }
+  } swap_back{act};
   // the kernel's view of every simulation, and the task list
   int64_t t = 0;
   std::vector<int64_t> task0((size_t)count);  // first task of each simulation
@@ -638,6 +651,7 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
     p->graph_builds++;
   }
   PC(cudaGraphLaunch(p->gexec, p->stream));
+  swap_back.armed = false;
   p->launches += nleap;
   p->pend_active = true;
   p->pend_count = count;

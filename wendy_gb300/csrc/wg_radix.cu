@@ -22,6 +22,8 @@
 // when the sheets are already in order, so the sequence can be captured in a
 // CUDA graph and still cost nothing when no sort is needed.
 #include <cstdint>
+#include <functional>
+#include <mutex>
 
 #include "wg_internal.cuh"
 
@@ -30,7 +32,11 @@ namespace wg {
 namespace {
 
 constexpr int R = 256;
-constexpr unsigned kStatA = 1u << 30, kStatP = 2u << 30, kCountMask = (1u << 30) - 1;
+// Look-back status words: top two bits 0 = not yet published, kStatA = the
+// tile's own count, kStatP = inclusive count, kStatX = poisoned (a wait of
+// this tile or of one it depends on expired: its offsets are unknown).
+constexpr unsigned kStatA = 1u << 30, kStatP = 2u << 30, kStatX = 3u << 30,
+                   kCountMask = (1u << 30) - 1;
 
 // plan layout (uint32 words)
 constexpr int kPlanActive = 0;   // [8]
@@ -126,6 +132,8 @@ struct PassSmem {
   uint32_t tmp[WARPS];
   uint64_t mbar[2];
   int64_t tile[2];
+  int64_t bad;  // 1 + the tile whose offsets are unknown (a bounded wait expired)
+  int stop;     // a copy of this CTA never completed: claim no further tile
 };
 
 // Persistent: each CTA claims its next tile once the current one's global
@@ -146,6 +154,8 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
   Smem& S = *reinterpret_cast<Smem*>(smem_raw);
 
   if (!a.flag->unsorted) return;
+  // an earlier pass gave up on a wait: its output is incomplete
+  if (*a.err & DEV_ERR_RADIX_TIMEOUT) return;
   const int pass = a.pass;
   if (!a.plan[kPlanActive + pass]) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -177,6 +187,8 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
   };
 
   if (tid == 0) {
+    S.bad = 0;
+    S.stop = 0;
     mbar_init(&S.mbar[0], 1);
     mbar_init(&S.mbar[1], 1);
     fence_proxy_async_smem();
@@ -194,8 +206,15 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
     const int64_t base = tile * TILE;
     const int tile_n = (int)((a.n - base) < TILE ? (a.n - base) : TILE);
     const bool via_bulk = bulk_ok && tile_n == TILE;
-    if (via_bulk && !mbar_wait(&S.mbar[b], (unsigned)(k >> 1) & 1u) && lane == 0)
-      atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
+    if (via_bulk && !mbar_wait(&S.mbar[b], (unsigned)(k >> 1) & 1u)) {
+      // the tile never arrived: its keys, counts and offsets are unknown.  The
+      // copy gets a second bounded wait; the tile is published as poisoned
+      // and this CTA claims no further tile.
+      if (lane == 0) atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
+      mbar_wait(&S.mbar[b], (unsigned)(k >> 1) & 1u);
+      S.bad = tile + 1;
+      S.stop = 1;
+    }
     uint64_t key[ITEMS];
     uint32_t val[ITEMS];
     uint32_t rank[ITEMS];
@@ -256,7 +275,9 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
       S.whist[w][d] = count;
       count += c;
     }
-    if (tile == 0)
+    if (S.bad == tile + 1)
+      st_relaxed_u32(&stat[tile * R + d], kStatX);
+    else if (tile == 0)
       st_relaxed_u32(&stat[d], kStatP | count);
     else
       st_relaxed_u32(&stat[tile * R + d], kStatA | count);
@@ -293,10 +314,11 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
     // predecessors are read per round, their loads in flight together, and
     // summed in order up to the nearest inclusive one.
     uint32_t excl = 0;
-    if (tile != 0) {
+    if (tile != 0 && S.bad != tile + 1) {
       constexpr int LB = 8;
       int64_t j = tile - 1;
       unsigned spins = 0;
+      bool poisoned = false;
       for (;;) {
         uint32_t sv[LB];
 #pragma unroll
@@ -307,6 +329,10 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
           const uint32_t sw = sv[w];
           if ((sw >> 30) == 0u) {
             blocked = true;
+            break;
+          }
+          if ((sw >> 30) == 3u) {  // a predecessor's offsets are unknown
+            poisoned = done = true;
             break;
           }
           excl += sw & kCountMask;
@@ -320,6 +346,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
           j -= w;  // resume at the tile that has not published yet
           if (++spins > kSpinLimit) {
             atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
+            poisoned = true;
             break;
           }
           __nanosleep(16);
@@ -327,23 +354,35 @@ __global__ void __launch_bounds__(THREADS, 2) k_radix_pass(const PassArgs a) {
         }
         j -= LB;
       }
-      st_relaxed_u32(&stat[tile * R + d], kStatP | (excl + count));
+      if (poisoned) {
+        // unknown offsets: publish the poison onward and write nothing
+        atomicOr(a.err, DEV_ERR_RADIX_TIMEOUT);
+        S.bad = tile + 1;
+        st_relaxed_u32(&stat[tile * R + d], kStatX);
+      } else {
+        st_relaxed_u32(&stat[tile * R + d], kStatP | (excl + count));
+      }
     }
     S.gbase[d] = a.plan[kPlanStarts + pass * R + d] + excl - tex;
     // claim the next tile once this one's offsets are known (claim order
     // then follows processing order) and start its copy into the other buffer
     if (tid == 0) {
-      const int64_t tn = atomicAdd(claim, 1u);
-      S.tile[b ^ 1] = tn;
-      fence_proxy_async_smem();
-      issue(tn, b ^ 1);
+      if (S.stop) {
+        S.tile[b ^ 1] = a.n_tiles;  // ends the loop after this tile
+      } else {
+        const int64_t tn = atomicAdd(claim, 1u);
+        S.tile[b ^ 1] = tn;
+        fence_proxy_async_smem();
+        issue(tn, b ^ 1);
+      }
     }
     __syncthreads();
     for (int i = tid; i < WARPS * R; i += THREADS) (&S.whist[0][0])[i] = 0;
+    const bool skip = S.bad == tile + 1;  // offsets unknown: no write may leave the tile
 #pragma unroll
     for (int jj = 0; jj < ITEMS; ++jj) {
       const int p = jj * THREADS + tid;
-      if (p < tile_n) {
+      if (p < tile_n && !skip) {
         const uint64_t kk = S.keys[b][p];
         const unsigned dd = (unsigned)((kk >> shift) & 255u);
         const int64_t o = (int64_t)S.gbase[dd] + p;
@@ -361,9 +400,10 @@ constexpr int kGatherThreads = 256, kGatherUnroll = 4;
 __global__ void __launch_bounds__(kGatherThreads) k_radix_gather(
     StateTable* table, int64_t n, const uint64_t* keys0, const uint64_t* keys1,
     const uint32_t* pos0, const uint32_t* pos1, const uint32_t* plan, uint32_t* counters,
-    const StepFlags* flag) {
+    const StepFlags* flag, const unsigned* err) {
   constexpr int GU = kGatherUnroll;
-  if (!flag->unsorted) return;
+  // nothing after a pass that gave up on a wait: its slots are incomplete
+  if (!flag->unsorted || (*err & DEV_ERR_RADIX_TIMEOUT)) return;
   const int fb = (int)plan[kPlanFinal];
   const uint64_t* __restrict__ keys = fb ? keys1 : keys0;
   const uint32_t* __restrict__ pos = fb ? pos1 : pos0;
@@ -413,8 +453,9 @@ __global__ void __launch_bounds__(kGatherThreads) k_radix_gather(
 constexpr int64_t kShortRun = 32;
 __global__ void k_radix_ties(StateTable* table, int64_t n, const uint64_t* keys0,
                              const uint64_t* keys1, const uint32_t* plan, uint32_t* counters,
-                             uint32_t* list_start, uint32_t* list_len, const StepFlags* flag) {
-  if (!flag->unsorted || !counters[8]) return;
+                             uint32_t* list_start, uint32_t* list_len, const StepFlags* flag,
+                             const unsigned* err) {
+  if (!flag->unsorted || !counters[8] || (*err & DEV_ERR_RADIX_TIMEOUT)) return;
   const int fb = (int)plan[kPlanFinal];
   const uint64_t* keys = fb ? keys1 : keys0;
   const StateRef oth = table->other;
@@ -462,8 +503,9 @@ __global__ void k_radix_ties(StateTable* table, int64_t n, const uint64_t* keys0
 constexpr int kLongTieThreads = 256;
 __global__ void __launch_bounds__(kLongTieThreads) k_radix_long_ties(
     StateTable* table, int64_t n, uint64_t* bufa, uint64_t* bufb, const uint32_t* counters,
-    const uint32_t* list_start, const uint32_t* list_len, const StepFlags* flag) {
-  if (!flag->unsorted || !counters[9]) return;
+    const uint32_t* list_start, const uint32_t* list_len, const StepFlags* flag,
+    const unsigned* err) {
+  if (!flag->unsorted || !counters[9] || (*err & DEV_ERR_RADIX_TIMEOUT)) return;
   constexpr int T = kLongTieThreads;
   __shared__ uint32_t cnt[16][T + 1];
   __shared__ uint32_t tot[16];
@@ -535,14 +577,48 @@ __global__ void __launch_bounds__(kLongTieThreads) k_radix_long_ties(
   }
 }
 
-__global__ void k_radix_flip(StateTable* table, const StepFlags* flag) {
-  if (!flag->unsorted) return;
+__global__ void k_radix_flip(StateTable* table, const StepFlags* flag, const unsigned* err) {
+  // after an expired wait the current set stays as it was (unsorted, intact)
+  if (!flag->unsorted || (*err & DEV_ERR_RADIX_TIMEOUT)) return;
   const StateRef t = table->cur;
   table->cur = table->other;
   table->other = t;
 }
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Launch configuration of the radix passes on one device: its SM count and
+// the resident pass CTAs per SM, after raising the pass kernel's dynamic
+// shared-memory limit on that device.  Set up once per device (thread-safe).
+struct RadixDevCfg {
+  int sms = 1;
+  int per_sm = 1;
+};
+
+void radix_cfg_init(RadixDevCfg& c, int dev) {
+  constexpr size_t dyn = sizeof(PassSmem<kRadixThreads, kRadixItems>);
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaFuncSetAttribute(k_radix_pass<kRadixThreads, kRadixItems>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, k_radix_pass<kRadixThreads, kRadixItems>, kRadixThreads, dyn);
+  c.sms = sms < 1 ? 1 : sms;
+  c.per_sm = per_sm < 1 ? 1 : per_sm;
+}
+
+RadixDevCfg radix_cfg() {
+  static std::once_flag once[kMaxDevices];
+  static RadixDevCfg cfg[kMaxDevices];
+  const int dev = current_device();
+  if (dev < 0 || dev >= kMaxDevices) {
+    RadixDevCfg c;
+    radix_cfg_init(c, dev < 0 ? 0 : dev);
+    return c;
+  }
+  std::call_once(once[dev], radix_cfg_init, std::ref(cfg[dev]), dev);
+  return cfg[dev];
+}
 
 }  // namespace
 
@@ -573,20 +649,10 @@ void radix_bind(RadixWork* w, void* base, int64_t n) {
 
 void radix_sort_state(StateTable* table, int64_t n, RadixWork* w, const StepFlags* flag,
                       unsigned* err, cudaStream_t s) {
-  static int pass_grid_per_sm = 0, sms = 0;
   constexpr size_t dyn = sizeof(PassSmem<kRadixThreads, kRadixItems>);
   static_assert(kRadixTile == PassSmem<kRadixThreads, kRadixItems>::TILE, "tile size");
-  if (!pass_grid_per_sm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(k_radix_pass<kRadixThreads, kRadixItems>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &pass_grid_per_sm, k_radix_pass<kRadixThreads, kRadixItems>, kRadixThreads, dyn);
-    if (pass_grid_per_sm < 1) pass_grid_per_sm = 1;
-    if (sms < 1) sms = 1;
-  }
+  const RadixDevCfg cfg = radix_cfg();
+  const int pass_grid_per_sm = cfg.per_sm, sms = cfg.sms;
   // the workspace may be bound for more sheets than this sort has: tiles,
   // look-back words and launches follow n
   const int64_t tiles = (n + kRadixTile - 1) / kRadixTile;
@@ -623,17 +689,18 @@ void radix_sort_state(StateTable* table, int64_t n, RadixWork* w, const StepFlag
   if (gg < 1) gg = 1;
   k_radix_gather<<<(unsigned)gg, kGatherThreads, 0, s>>>(table, n, w->keys[0], w->keys[1],
                                                           w->pos[0], w->pos[1], w->plan,
-                                                          w->counters, flag);
+                                                          w->counters, flag, err);
   int g = (int)((n + 255) / 256);
   if (g > 152 * 16) g = 152 * 16;
   if (g < 1) g = 1;
   // pos[] is free once gathered: it holds the list of long runs
   k_radix_ties<<<g, 256, 0, s>>>(table, n, w->keys[0], w->keys[1], w->plan, w->counters,
-                                 w->pos[0], w->pos[1], flag);
+                                 w->pos[0], w->pos[1], flag, err);
   // and, once the runs are listed, the key buffers are scratch for long ones
   k_radix_long_ties<<<sms, kLongTieThreads, 0, s>>>(table, n, w->keys[0], w->keys[1],
-                                                    w->counters, w->pos[0], w->pos[1], flag);
-  k_radix_flip<<<1, 1, 0, s>>>(table, flag);
+                                                    w->counters, w->pos[0], w->pos[1], flag,
+                                                    err);
+  k_radix_flip<<<1, 1, 0, s>>>(table, flag, err);
 }
 
 }  // namespace wg

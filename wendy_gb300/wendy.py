@@ -13,6 +13,17 @@ The sheets stay on the device between outputs.  Each ``next()`` completes
 the output interval enqueued before, copies x and v back into the yielded
 (page-locked) arrays, and enqueues the next interval before yielding, so the
 device computes output k + 1 while the caller works on output k.
+
+One difference a caller can observe: wendy's C step reads the yielded ``v``
+on every call (wendy/wendy.c:318-333; ``x`` is only written, at
+wendy/wendy.c:413-415), so editing ``v`` in place between ``next()`` calls
+changes the trajectory there.  Here the state lives on the device and the
+next output is already being computed, so such edits are ignored unless
+``follow_edits=True``: then every ``next()`` compares ``v`` with the copy
+taken when it was yielded and, if it changed, drops the output computed
+ahead and restarts from the yielded positions and the edited velocities (as
+wendy does, edits of ``x`` still have no effect).  That costs a copy and a
+comparison of ``x`` and ``v`` per output on the host.
 """
 import copy
 import ctypes
@@ -104,11 +115,15 @@ class Simulation:
 
 
 def nbody(x, v, m, dt, t0=0., twopiG=1., omega=None, ext_force=None, approx=False, nleap=None,
-          sort="cuda", maxcoll=100000, warn_maxcoll=False, full_output=False):
+          sort="cuda", maxcoll=100000, warn_maxcoll=False, full_output=False,
+          follow_edits=False):
     """Run a 1D N-body simulation (wendy/wendy.py:112-157 for the approximate path).
 
     Only ``approx=True`` with ``sort='cuda'`` runs here; the exact
     event-driven solver and the CPU sorts are the reference's.
+    ``follow_edits=True`` (not in wendy) honours in-place edits of the
+    yielded ``v`` between outputs, as wendy's C step does; see the module
+    documentation.
     """
     if approx:
         if nleap is None:
@@ -117,13 +132,14 @@ def nbody(x, v, m, dt, t0=0., twopiG=1., omega=None, ext_force=None, approx=Fals
         # yield from: closing this generator closes the inner one (and its
         # simulation) at once
         yield from _nbody_approx(x, v, m, dt, nleap, t0=t0, sort=sort, omega=omega,
-                                 ext_force=ext_force, twopiG=twopiG, full_output=full_output)
+                                 ext_force=ext_force, twopiG=twopiG, full_output=full_output,
+                                 follow_edits=follow_edits)
     raise NotImplementedError("wendy_gb300 implements the approximate integrator (approx=True); "
                               "the exact event-driven solver is the reference wendy's")
 
 
 def _nbody_approx(x, v, m, dt, nleap, t0=0., omega=None, ext_force=None, sort="cuda", twopiG=1.,
-                  full_output=False):
+                  full_output=False, follow_edits=False):
     """Generator mirroring wendy._nbody_approx (wendy/wendy.py:336-437)."""
     if sort != "cuda":
         if sort in CPU_SORTS:
@@ -149,12 +165,25 @@ def _nbody_approx(x, v, m, dt, nleap, t0=0., omega=None, ext_force=None, sort="c
         while True:
             elapsed = sim.step_end()
             # the next output is enqueued first; this one downloads while it runs
+            t_ahead = t.value  # the time that next output starts from
             sim.step_begin(dt_leap, nleap, t)
             sim.download(x, v)
+            if follow_edits:
+                x_seen, v_seen = x.copy(), v.copy()
             if full_output:
                 yield (x, v, elapsed)
             else:
                 yield (x, v)
+            if follow_edits and not numpy.array_equal(v.view(numpy.int64),
+                                                      v_seen.view(numpy.int64)):
+                # v was edited: the output computed ahead is dropped and the
+                # run restarts from the yielded positions and the edited v
+                sim.step_end()
+                sim.close()
+                x[:] = x_seen
+                sim = Simulation(x, v, m, totmass, omega2, ext_force)
+                t.value = t_ahead
+                sim.step_begin(dt_leap, nleap, t)
     finally:
         # also runs when an unclosed generator is collected at interpreter exit
         try:
