@@ -40,6 +40,23 @@ extern "C" {
 #define WG_EXT_NONE 0
 #define WG_EXT_HARMONIC 1    /* F = -p[0] x                                  (1 param)  */
 #define WG_EXT_PULSE_TANH 2  /* F = p[0] exp(-(t-p[1])^2/(2 p[2]^2)) tanh(x/p[3]) (4 params) */
+/* A compiled expression F(x, t): the parameters are a register program
+   (at most WG_EXPR_MAX_OPS ops on WG_EXPR_REGS registers) that
+   wendy_gb300/extforce.py compiles from a restricted Python function or
+   string -- arithmetic, integer and real powers, exp, log, sqrt, sin, cos,
+   tan, tanh, sinh, cosh, arctan, abs of x, t and constants:
+     p[0] = number of ops, p[1] = ops of the time phase (t and constants
+     only, run once per force evaluation), then five numbers per op:
+     code, destination register, operand registers a and b, constant.
+   Codes: 0 x, 1 t, 2 constant, 3 copy a, 4 a+b, 5 a-b, 6 a*b, 7 a/b, 8 -a,
+   9 pow(a, b), 10 exp, 11 log, 12 sqrt, 13 sin, 14 cos, 15 tan, 16 tanh,
+   17 sinh, 18 cosh, 19 atan, 20 abs (of a).  F is the register the last op
+   writes.  Malformed programs (unknown codes, registers out of range or read
+   before written, x in the time phase) return WG_ERR_EXT.  Replaces the
+   numba-compiled callables of wendy/wendy.py:389-404. */
+#define WG_EXT_EXPR 3
+#define WG_EXPR_MAX_OPS 64
+#define WG_EXPR_REGS 16
 
 /* Same layout as wendy's `struct array_w_index` (wendy/wendy.h:12-16). */
 typedef struct wg_sheet {

@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(HERE, "libwendy_oracle.so")
 EXT_SUFFIX = sysconfig.get_config_var("EXT_SUFFIX")
 REF_DIR = os.path.join(HERE, "_ref")
 
-EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH = 0, 1, 2
+EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH, EXT_EXPR = 0, 1, 2, 3
 SORT_IDS = {"quick": 0, "qsort": 3, "parallel": 4}
 
 _F64 = numpy.ctypeslib.ndpointer(dtype=numpy.float64, flags=("C_CONTIGUOUS", "WRITEABLE"))
@@ -74,10 +74,16 @@ def load():
 
 
 def _ext_args(ext):
+    """(kind, params as float64) of ``ext``: None, (kind, params), or an
+    object with ``kind`` and ``params`` (wendy_gb300's registered forces,
+    compiled expressions included)."""
     if ext is None:
         return EXT_NONE, numpy.zeros(8)
-    kind, params = ext
-    p = numpy.zeros(8)
+    if hasattr(ext, "kind") and hasattr(ext, "params"):
+        kind, params = ext.kind, ext.params
+    else:
+        kind, params = ext
+    p = numpy.zeros(max(8, len(params)))
     p[:len(params)] = params
     return int(kind), p
 

@@ -252,12 +252,54 @@ void wo_parallel_sort(wo_sheet *a, size_t n) {
      kind 0: none
      kind 1: harmonic,     F = -p[0] * x                (p[0] = omega^2)
      kind 2: pulsed tanh,  F = p[0]*exp(-(t-p[1])^2/(2 p[2]^2))*tanh(x/p[3])
+     kind 3: a compiled expression (below)
    The expression order matches the numpy expression
    A*numpy.exp(-(t-t0)**2/(2*tau**2))*numpy.tanh(x/h).
    --------------------------------------------------------------------- */
 #define WO_EXT_NONE 0
 #define WO_EXT_HARMONIC 1
 #define WO_EXT_PULSE_TANH 2
+#define WO_EXT_EXPR 3
+
+/* kind 3: a compiled expression F(x, t), the register program of the
+   library's WG_EXT_EXPR (wendy_gb300/extforce.py writes it): p[0] ops,
+   p[1] of them free of x, then (code, dst, a, b, constant) per op; F is the
+   register the last op writes.  Evaluated here op by op in libm double
+   arithmetic, the way the reference evaluates a numba-compiled callable. */
+static double wo_expr_eval(const double *p, double x, double t) {
+  double r[16] = {0};
+  int i, n = (int)p[0];
+  for (i = 0; i < n; i++) {
+    const double *q = p + 2 + 5 * i;
+    int code = (int)q[0], dst = (int)q[1], a = (int)q[2], b = (int)q[3];
+    double va = r[a], vb = r[b], y;
+    switch (code) {
+      case 0: y = x; break;
+      case 1: y = t; break;
+      case 2: y = q[4]; break;
+      case 3: y = va; break;
+      case 4: y = va + vb; break;
+      case 5: y = va - vb; break;
+      case 6: y = va * vb; break;
+      case 7: y = va / vb; break;
+      case 8: y = -va; break;
+      case 9: y = pow(va, vb); break;
+      case 10: y = exp(va); break;
+      case 11: y = log(va); break;
+      case 12: y = sqrt(va); break;
+      case 13: y = sin(va); break;
+      case 14: y = cos(va); break;
+      case 15: y = tan(va); break;
+      case 16: y = tanh(va); break;
+      case 17: y = sinh(va); break;
+      case 18: y = cosh(va); break;
+      case 19: y = atan(va); break;
+      default: y = fabs(va); break;
+    }
+    r[dst] = y;
+  }
+  return r[(int)p[2 + 5 * (n - 1) + 1]];
+}
 
 static double wo_ext_eval(int kind, const double *p, double x, double t) {
   if (kind == WO_EXT_HARMONIC) return -p[0] * x;
@@ -266,6 +308,7 @@ static double wo_ext_eval(int kind, const double *p, double x, double t) {
     double amp = p[0] * exp(-(dt * dt) / (2. * (p[2] * p[2])));
     return amp * tanh(x / p[3]);
   }
+  if (kind == WO_EXT_EXPR) return wo_expr_eval(p, x, t);
   return 0.;
 }
 
@@ -273,12 +316,13 @@ static double wo_ext_eval(int kind, const double *p, double x, double t) {
    reference library built from its own sources can be driven with the same
    registered force (the reference passes `a` in original order for N > 10
    and asks for one scalar when N == 1, wendy/wendy.py:397-403). */
+#define WO_MAX_PARAMS (2 + 5 * 64)
 static int wo_cb_kind = WO_EXT_NONE;
-static double wo_cb_params[8];
+static double wo_cb_params[WO_MAX_PARAMS];
 void wo_set_callback_force(int kind, const double *params, int nparams) {
   int i;
   wo_cb_kind = kind;
-  for (i = 0; i < nparams && i < 8; i++) wo_cb_params[i] = params[i];
+  for (i = 0; i < nparams && i < WO_MAX_PARAMS; i++) wo_cb_params[i] = params[i];
 }
 double wo_callback_force(int n, double *x, double t, double *a) {
   int i;

@@ -20,6 +20,11 @@ Files:
   energy.npz    relative energy error per output of a 1000-output run
                 (N=10,000 sech^2 disk, dt=0.05, nleap=10)
   exact.npz     reference exact solver, N=101 sech^2 disk, 20 outputs
+  extexpr.npz   x, v after outputs 1 and 10 of runs with external forces
+                given as Python functions (tests/golden/forces.py), through
+                the reference's own callable route
+
+    python tests/golden/make_golden.py --only extexpr   # just that file
 """
 import argparse
 import os
@@ -74,16 +79,43 @@ def ref_accel(lib, x, m, omega2, ext, t):
     return a, xi["idx"].copy(), totmass
 
 
+def make_extexpr(wendy):
+    """Runs of the reference's generator with Python-function forces: with
+    numba stubbed out, wendy wraps each function in its ctypes callback
+    (wendy/wendy.py:405-418) and its C step calls it per force evaluation."""
+    import forces
+    out = {}
+    for name, fn, fam, n, seed, dt, nleap, nout, t0 in forces.CASES:
+        x, v, m = ics.FAMILIES[fam](n, seed=seed)
+        g = wendy.nbody(x.copy(), v.copy(), m.copy(), dt, approx=True, nleap=nleap, t0=t0,
+                        sort="quick", ext_force=fn)
+        for k in range(1, nout + 1):
+            tx, tv = next(g)
+            if k in (1, nout):
+                out["%s/x%d" % (name, k)] = tx.copy()
+                out["%s/v%d" % (name, k)] = tv.copy()
+        out[name + "/x0"], out[name + "/v0"], out[name + "/m"] = x, v, m
+    out["names"] = numpy.array([c[0] for c in forces.CASES])
+    numpy.savez_compressed(os.path.join(HERE, "extexpr.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-root", default=None,
                     help="reference checkout (default: $WENDY_REF_ROOT, else the one "
                          "oracle/_ref was built from)")
+    ap.add_argument("--only", default=None, choices=["extexpr"],
+                    help="write just this file")
     args = ap.parse_args()
     lib = O.ref_library()
     wendy = O.import_reference_wendy(args.ref_root)
     if lib is None or wendy is None:
         sys.exit("reference library not built: run `make -C oracle ref` first")
+    sys.path.insert(0, HERE)
+    if args.only == "extexpr":
+        make_extexpr(wendy)
+        print("golden vectors written to", HERE)
+        return
 
     # ---- single force evaluations
     out = {}
@@ -182,6 +214,7 @@ def main():
         ex["x%d" % k] = tx.copy()
         ex["v%d" % k] = tv.copy()
     numpy.savez_compressed(os.path.join(HERE, "exact.npz"), **ex)
+    make_extexpr(wendy)
     print("golden vectors written to", HERE)
 
 

@@ -20,7 +20,7 @@ WG_ERR_EXT, WG_ERR_BUDGET, WG_ERR_NODEV = -5, -6, -7
 STATUS_NAMES = {0: "WG_OK", -1: "WG_ERR_ARG", -2: "WG_ERR_CUDA", -3: "WG_ERR_NOMEM",
                 -4: "WG_ERR_DEVICE", -5: "WG_ERR_EXT", -6: "WG_ERR_BUDGET", -7: "WG_ERR_NODEV"}
 
-EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH = 0, 1, 2
+EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH, EXT_EXPR = 0, 1, 2, 3
 
 # Every symbol include/wendy_gb300.h declares.
 EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", "wg_create",
@@ -145,6 +145,8 @@ def check(status, where):
 
 
 def ext_params(params):
-    p = numpy.zeros(4)
+    """The parameters of an external force as the float64 array the C ABI
+    takes (at least 4 entries, zero-padded)."""
+    p = numpy.zeros(max(4, len(params)))
     p[:len(params)] = params
     return p

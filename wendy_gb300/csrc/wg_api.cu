@@ -11,6 +11,7 @@
 
 #include "../../include/wendy_gb300.h"
 #include "wg_bucket.cuh"
+#include "wg_ext.cuh"
 #include "wg_internal.cuh"
 
 using namespace wg;
@@ -96,30 +97,11 @@ u128 host_mass_to_fixed(double m, int E) {
   return (u128)((mant + (1ull << (r - 1))) >> r);
 }
 
-int check_ext(int kind, const double* p, int np, ExtForce* out) {
-  out->kind = kind;
-  for (int i = 0; i < 4; ++i) out->p[i] = 0.0;
-  const int need = kind == WG_EXT_NONE ? 0 : kind == WG_EXT_HARMONIC ? 1 : kind == WG_EXT_PULSE_TANH ? 4 : -1;
-  if (need < 0) {
-    set_error("unknown external-force id %d", kind);
-    return WG_ERR_EXT;
-  }
-  if (np < need || (need > 0 && !p)) {
-    set_error("external force %d needs %d parameters, got %d", kind, need, np);
-    return WG_ERR_EXT;
-  }
-  for (int i = 0; i < need; ++i) {
-    if (!std::isfinite(p[i])) {
-      set_error("external-force parameter %d is not finite", i);
-      return WG_ERR_EXT;
-    }
-    out->p[i] = p[i];
-  }
-  if (kind == WG_EXT_PULSE_TANH && (p[2] == 0.0 || p[3] == 0.0)) {
-    set_error("pulsed force needs tau != 0 and h != 0");
-    return WG_ERR_EXT;
-  }
-  return WG_OK;
+int check_ext(int kind, const double* p, int np, ExtSpec* out) {
+  char msg[256];
+  const int rc = parse_ext(kind, p, np, out, msg, sizeof(msg));
+  if (rc) set_error("%s", msg);
+  return rc;
 }
 
 }  // namespace
@@ -174,7 +156,7 @@ struct wg_sim {
   bool spec_pending = false;
   int spec_set = 0, spec_nleap = 0;
   double spec_dt = 0, spec_t0_in = 0, spec_t0_out = 0, spec_totmass = 0, spec_omega2 = 0;
-  ExtForce spec_ext{};
+  ExtSpec spec_ext{};
   double* h_t = nullptr;         // pinned host mirrors
   unsigned* h_ep = nullptr;
   StepFlags* h_flags = nullptr;
@@ -240,7 +222,9 @@ struct wg_sim {
   uint64_t T_lo = 0, T_hi = 0;
   int E = 0;
   double totmass = 0, omega2 = -1;
-  ExtForce ext{};
+  ExtForce ext{};        // the force as the kernels see it
+  ExtSpec ext_spec{};    // ... with an expression force's program on the host
+  ExprOp* d_prog = nullptr;  // an expression force's program on the device
   unsigned epoch = 1;
   wg_stats st{};
   // a kernel raised the device error word during a call: the state on the
@@ -249,6 +233,22 @@ struct wg_sim {
 };
 
 namespace {
+
+// The simulation's external force (an expression force's program is
+// copied to the device on the simulation's stream).
+int set_force(wg_sim* s, const ExtSpec& ext) {
+  if (ext.f.kind == EXT_EXPR && s->d_prog && s->ext.kind == EXT_EXPR && same_ext(ext, s->ext_spec))
+    return WG_OK;  // that program is on the device already
+  s->ext_spec = ext;
+  const cudaError_t e = attach_ext_program(&s->ext_spec, &s->d_prog, s->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("upload of the external-force program failed: %s", cudaGetErrorString(e));
+    return WG_ERR_CUDA;
+  }
+  s->ext = s->ext_spec.f;
+  return WG_OK;
+}
 
 // Sheets per bucket of the next bucketize (and with it the bucket count).
 void set_target(wg_sim* s, int target) {
@@ -312,6 +312,7 @@ void free_sim(wg_sim* s) {
   if (s->down_stream) cudaStreamSynchronize(s->down_stream);
   if (s->dl_stream) cudaStreamSynchronize(s->dl_stream);
   if (s->out2) cudaFree(s->out2);
+  if (s->d_prog) cudaFree(s->d_prog);
   if (s->ev_done) cudaEventDestroy(s->ev_done);
   if (s->dl_stream) cudaStreamDestroy(s->dl_stream);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -325,7 +326,7 @@ void free_sim(wg_sim* s) {
 
 // Allocate a simulation for n sheets with the given physics; sheet data is
 // uploaded by the caller.
-int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_sim** out) {
+int make_sim(int64_t n, double totmass, double omega2, const ExtSpec& ext, wg_sim** out) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
     cudaGetLastError();
@@ -337,7 +338,7 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
   s->n_tiles = (n + kForceTile - 1) / kForceTile;
   s->totmass = totmass;
   s->omega2 = omega2;
-  s->ext = ext;
+  s->ext_spec = ext;
   // Fixed-point scale: totmass < 2^eT, so 8 * totmass * 2^E < 2^126.
   if (totmass > 0) {
     int eT = 0;
@@ -463,6 +464,8 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtForce& ext, wg_s
     s->grid_bucket = s->tune.ctas_per_sm * sms;
   }
   rc = alloc_call_arrays(s, 64);
+  if (rc != WG_OK) return fail(rc);
+  rc = set_force(s, ext);
   if (rc != WG_OK) return fail(rc);
   s->st.n = n;
   s->st.device_bytes = (int64_t)(total + bk_b);
@@ -652,6 +655,7 @@ StepLaunch step_launch(wg_sim* s, int i, int nleap, int profile) {
   L.ticket = s->tickets + i;
   L.err = s->err;
   L.profile = profile;
+  L.any_expr = s->ext.kind == EXT_EXPR;
   return L;
 }
 
@@ -768,7 +772,7 @@ int wg_create(int64_t n, const double* x, const double* v, const double* m, doub
     set_error("omega2 must be finite");
     return WG_ERR_ARG;
   }
-  ExtForce ext;
+  ExtSpec ext;
   rc = check_ext(ext_kind, ext_params, n_ext_params, &ext);
   if (rc) return rc;
   wg_sim* s = nullptr;
@@ -1353,23 +1357,28 @@ int wg_ext_force_eval(int64_t n, const double* x, double t, int ext_kind,
     set_error("wg_ext_force_eval needs n >= 1, x, out and a finite t");
     return WG_ERR_ARG;
   }
-  ExtForce ext;
+  ExtSpec ext;
   int rc = check_ext(ext_kind, ext_params, n_ext_params, &ext);
   if (rc) return rc;
   double* d = nullptr;
+  ExprOp* d_prog = nullptr;
   cudaError_t e = cudaMalloc(&d, 16 * (size_t)n);
+  if (e == cudaSuccess) e = attach_ext_program(&ext, &d_prog, 0);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    set_error("cudaMalloc of %zu bytes failed: %s", 16 * (size_t)n, cudaGetErrorString(e));
+    if (d) cudaFree(d);
+    if (d_prog) cudaFree(d_prog);
+    set_error("device buffers of %zu bytes failed: %s", 16 * (size_t)n, cudaGetErrorString(e));
     return WG_ERR_NOMEM;
   }
   e = cudaMemcpy(d, x, 8 * (size_t)n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
-    launch_ext_eval(ext, t, d, d + n, n, 0);
+    launch_ext_eval(ext.f, t, d, d + n, n, 0);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpy(out, d + n, 8 * (size_t)n, cudaMemcpyDeviceToHost);
   cudaFree(d);
+  if (d_prog) cudaFree(d_prog);
   if (e != cudaSuccess) {
     set_error("wg_ext_force_eval failed: %s", cudaGetErrorString(e));
     return WG_ERR_CUDA;
@@ -1383,7 +1392,7 @@ int wg_accel(int64_t n, const double* x, const double* m, double totmass, double
   std::vector<double> zero((size_t)(n > 0 ? n : 1), 0.0);
   int rc = validate_sheets(n, x, zero.data(), m, totmass);
   if (rc) return rc;
-  ExtForce ext;
+  ExtSpec ext;
   rc = check_ext(ext_kind, ext_params, n_ext_params, &ext);
   if (rc) return rc;
   wg_sim* s = nullptr;
@@ -1441,7 +1450,7 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
     set_error("null buffer, n < 1, nleap < 1 or nleap > %d", kMaxLeap);
     return WG_ERR_ARG;
   }
-  ExtForce ext;
+  ExtSpec ext;
   int rc = check_ext(ext_kind, ext_params, n_ext_params, &ext);
   if (rc) return rc;
   std::lock_guard<std::mutex> lock(g_cache_mu);
@@ -1485,9 +1494,7 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   if (spec) {
     const bool same = t0 && bits_eq(dt, s->spec_dt) && nleap == s->spec_nleap &&
                       bits_eq(*t0, s->spec_t0_in) && bits_eq(totmass, s->spec_totmass) &&
-                      bits_eq(omega2, s->spec_omega2) && ext.kind == s->spec_ext.kind &&
-                      bits_eq(ext.p[0], s->spec_ext.p[0]) && bits_eq(ext.p[1], s->spec_ext.p[1]) &&
-                      bits_eq(ext.p[2], s->spec_ext.p[2]) && bits_eq(ext.p[3], s->spec_ext.p[3]);
+                      bits_eq(omega2, s->spec_omega2) && same_ext(ext, s->spec_ext);
     if (!same) {
       drop_spec();
       spec = false;
@@ -1496,7 +1503,8 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   // physics of this call
   s->totmass = totmass;
   s->omega2 = omega2;
-  s->ext = ext;
+  rc = set_force(s, ext);
+  if (rc) return rc;
   if (totmass > 0) {
     int eT = 0;
     std::frexp(totmass, &eT);

@@ -607,7 +607,9 @@ __device__ __forceinline__ void claim_task(const StepLaunch& L, int sub, unsigne
 }
 
 // The fused sub-step.  LAST: the call's last sub-step (half drift, outputs).
-template <bool LAST>
+// EXPR: the launch has simulations with expression forces (the interpreter
+// is compiled only into this instantiation).
+template <bool LAST, bool EXPR>
 __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   StepSmem& S = *reinterpret_cast<StepSmem*>(smem_raw);
@@ -779,6 +781,15 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     const int has_omega = D.has_omega;
     const double omega2 = D.omega2;
     const ExtForce ext = D.ext;
+    // an expression force: its time phase, once per task and thread
+    double xr[EXPR ? kExprRegs : 1];
+    double t_ev = 0.0;
+    if constexpr (EXPR) {
+      if (ext.kind == EXT_EXPR) {
+        t_ev = D.t_seq[sub];
+        expr_time(ext, t_ev, xr);
+      }
+    }
     const uint32_t target = (uint32_t)D.target;
     const int64_t nbk = D.nb;
     // ---- force, kick, drift, routing; new x, v go back to their slots and
@@ -827,7 +838,14 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
         C += M;
         double acc = fixed_to_double(A, E);
         if (has_omega) acc = fma(-omega2, x, acc);
-        if (ext.kind != EXT_NONE) acc = ext_force_at(ext, S.amp, S.inv_h, x) + acc;
+        if constexpr (EXPR) {
+          if (ext.kind == EXT_EXPR)
+            acc = expr_space(ext, xr, x, t_ev) + acc;
+          else if (ext.kind != EXT_NONE)
+            acc = ext_force_at(ext, S.amp, S.inv_h, x) + acc;
+        } else if (ext.kind != EXT_NONE) {
+          acc = ext_force_at(ext, S.amp, S.inv_h, x) + acc;
+        }
         const double vn = fma(dt, acc, v);
         const double xn = fma(dt_drift, vn, x);
         S.x[sidx] = xn;
@@ -1156,9 +1174,13 @@ void set_tuning(const std::vector<std::pair<int64_t, BucketTuning>>& rows) {
 // The sub-step kernel's dynamic shared-memory limit, raised once per device
 // (function attributes belong to the device they were set on).
 void bucket_attr_init() {
-  cudaFuncSetAttribute(k_bucket_step<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_bucket_step<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(StepSmem));
-  cudaFuncSetAttribute(k_bucket_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_bucket_step<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(StepSmem));
+  cudaFuncSetAttribute(k_bucket_step<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(StepSmem));
+  cudaFuncSetAttribute(k_bucket_step<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(StepSmem));
 }
 
@@ -1197,10 +1219,17 @@ void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s) {
   bucket_step_prepare();
   if (grid > a.ntasks) grid = a.ntasks;
   if (grid < 1) grid = 1;
-  if (a.sub == a.nleap - 1)
-    k_bucket_step<true><<<grid, BT, sizeof(StepSmem), s>>>(a);
-  else
-    k_bucket_step<false><<<grid, BT, sizeof(StepSmem), s>>>(a);
+  const bool last = a.sub == a.nleap - 1;
+  if (a.any_expr) {
+    if (last)
+      k_bucket_step<true, true><<<grid, BT, sizeof(StepSmem), s>>>(a);
+    else
+      k_bucket_step<false, true><<<grid, BT, sizeof(StepSmem), s>>>(a);
+  } else if (last) {
+    k_bucket_step<true, false><<<grid, BT, sizeof(StepSmem), s>>>(a);
+  } else {
+    k_bucket_step<false, false><<<grid, BT, sizeof(StepSmem), s>>>(a);
+  }
 }
 
 void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int E,

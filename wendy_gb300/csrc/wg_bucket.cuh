@@ -132,6 +132,7 @@ struct StepLaunch {
   unsigned* ticket;      // zero before the launch
   unsigned* err;
   int profile;           // 1: dt = 0 and no outputs (timing harness)
+  int any_expr;          // some simulation of the launch has an expression force
 };
 
 void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s);

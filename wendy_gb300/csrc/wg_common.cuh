@@ -236,12 +236,80 @@ __device__ __forceinline__ u128 warp_sum_u128(u128 v) {
 // Registered external forces (closed forms replacing wendy's ext_force
 // callables, wendy/wendy.py:389-418).
 // ---------------------------------------------------------------------------
-enum : int { EXT_NONE = 0, EXT_HARMONIC = 1, EXT_PULSE_TANH = 2, EXT_MAX = 2 };
+enum : int { EXT_NONE = 0, EXT_HARMONIC = 1, EXT_PULSE_TANH = 2, EXT_EXPR = 3, EXT_MAX = 3 };
+
+// Compiled expression forces (EXT_EXPR).  wendy accepts any F(x, t) and
+// compiles it with numba (wendy/wendy.py:389-404); here a restricted F is
+// compiled on the host (wendy_gb300/extforce.py) into a short register
+// program that the force kernels interpret.  The program has two phases:
+// ops [0, n_time) use only t and constants and run once per force
+// evaluation and thread; ops [n_time, n_ops) run per sheet with x.  The
+// result is the register the last op writes.
+constexpr int kExprMaxOps = 64;
+constexpr int kExprRegs = 16;
+enum : int {
+  XOP_X = 0, XOP_T, XOP_K, XOP_MOV, XOP_ADD, XOP_SUB, XOP_MUL, XOP_DIV, XOP_NEG, XOP_POW,
+  XOP_EXP, XOP_LOG, XOP_SQRT, XOP_SIN, XOP_COS, XOP_TAN, XOP_TANH, XOP_SINH, XOP_COSH,
+  XOP_ATAN, XOP_ABS, XOP_COUNT
+};
+struct ExprOp {
+  int code;
+  int dst, a, b;  // registers
+  double k;       // the constant of XOP_K
+};
 
 struct ExtForce {
   int kind;
   double p[4];
+  const ExprOp* prog;  // EXT_EXPR: the program, in device memory
+  int n_ops;
+  int n_time;
 };
+
+// Runs ops [lo, hi) of an expression program on the registers r.
+static __device__ __noinline__ void expr_run(const ExprOp* __restrict__ prog, int lo, int hi,
+                                             double* r, double x, double t) {
+  for (int i = lo; i < hi; ++i) {
+    const ExprOp o = prog[i];  // the same op in every thread: a broadcast load
+    const double va = r[o.a], vb = r[o.b];
+    double y;
+    switch (o.code) {
+      case XOP_X: y = x; break;
+      case XOP_T: y = t; break;
+      case XOP_K: y = o.k; break;
+      case XOP_MOV: y = va; break;
+      case XOP_ADD: y = va + vb; break;
+      case XOP_SUB: y = va - vb; break;
+      case XOP_MUL: y = va * vb; break;
+      case XOP_DIV: y = va / vb; break;
+      case XOP_NEG: y = -va; break;
+      case XOP_POW: y = pow(va, vb); break;
+      case XOP_EXP: y = exp(va); break;
+      case XOP_LOG: y = log(va); break;
+      case XOP_SQRT: y = sqrt(va); break;
+      case XOP_SIN: y = sin(va); break;
+      case XOP_COS: y = cos(va); break;
+      case XOP_TAN: y = tan(va); break;
+      case XOP_TANH: y = tanh(va); break;
+      case XOP_SINH: y = sinh(va); break;
+      case XOP_COSH: y = cosh(va); break;
+      case XOP_ATAN: y = atan(va); break;
+      default: y = fabs(va); break;  // XOP_ABS
+    }
+    r[o.dst] = y;
+  }
+}
+
+// The time phase of an expression force at time t (once per force
+// evaluation; the registers then serve every sheet).
+__device__ __forceinline__ void expr_time(const ExtForce& f, double t, double* r) {
+  expr_run(f.prog, 0, f.n_time, r, 0.0, t);
+}
+// F(x) of an expression force after its time phase.
+__device__ __forceinline__ double expr_space(const ExtForce& f, double* r, double x, double t) {
+  expr_run(f.prog, f.n_time, f.n_ops, r, x, t);
+  return r[f.prog[f.n_ops - 1].dst];
+}
 
 // Time factor of the pulsed force, A exp(-(t-t0)^2 / (2 tau^2)); evaluated
 // once per force evaluation, with the numpy expression's operation order.

@@ -85,7 +85,7 @@ __device__ u128 force_lookback(const ForceArgs& a, int64_t tile, u128 total, int
   return prefix;
 }
 
-template <int THREADS, int ITEMS>
+template <int THREADS, int ITEMS, bool EXPR>
 __global__ void __launch_bounds__(THREADS, 2) k_force_kick_drift(const ForceArgs a) {
   constexpr int TILE = THREADS * ITEMS;
   constexpr int WARPS = THREADS / 32;
@@ -168,6 +168,12 @@ __global__ void __launch_bounds__(THREADS, 2) k_force_kick_drift(const ForceArgs
 
   const i128 T = (i128)((((u128)a.T_hi) << 64) | a.T_lo);
   const double amp = s_amp, inv_h = s_inv_h;
+  double xr[EXPR ? kExprRegs : 1];  // an expression force's registers
+  double t_ev = 0.0;
+  if constexpr (EXPR) {
+    t_ev = a.t_seq[a.sub];
+    expr_time(a.ext, t_ev, xr);
+  }
   unsigned long long maxv = 0;
   bool unsorted = false;
   uint64_t first_key = ~0ull, last_key = 0, prev_key = 0;
@@ -180,7 +186,10 @@ __global__ void __launch_bounds__(THREADS, 2) k_force_kick_drift(const ForceArgs
     const i128 A = T - 2 * C - (i128)M;
     double acc = fixed_to_double(A, a.E);
     if (a.has_omega) acc = fma(-a.omega2, x[i], acc);
-    if (a.ext.kind != EXT_NONE) acc = ext_force_at(a.ext, amp, inv_h, x[i]) + acc;
+    if constexpr (EXPR)
+      acc = expr_space(a.ext, xr, x[i], t_ev) + acc;
+    else if (a.ext.kind != EXT_NONE)
+      acc = ext_force_at(a.ext, amp, inv_h, x[i]) + acc;
     const double vn = fma(a.dt_kick, acc, v[i]);
     const double xn = fma(a.dt_drift, vn, x[i]);
     v[i] = vn;
@@ -321,7 +330,12 @@ void launch_force(const ForceArgs& a, int64_t n_tiles, cudaStream_t s) {
   ForceArgs b = a;
   b.spin_limit = g_spin_limit;
   b.withhold_tile = g_withhold_tile;
-  k_force_kick_drift<kForceThreads, kForceItems><<<(unsigned)n_tiles, kForceThreads, 0, s>>>(b);
+  if (b.ext.kind == EXT_EXPR)
+    k_force_kick_drift<kForceThreads, kForceItems, true>
+        <<<(unsigned)n_tiles, kForceThreads, 0, s>>>(b);
+  else
+    k_force_kick_drift<kForceThreads, kForceItems, false>
+        <<<(unsigned)n_tiles, kForceThreads, 0, s>>>(b);
 }
 
 void launch_drift(const StateTable* table, int64_t n, double dt, StepFlags* flag,
@@ -348,9 +362,12 @@ __global__ void k_ext_eval(const ExtForce f, double t, const double* x, double* 
     s_inv_h = f.kind == EXT_PULSE_TANH ? 1.0 / f.p[3] : 0.0;
   }
   __syncthreads();
+  double xr[kExprRegs];
+  if (f.kind == EXT_EXPR) expr_time(f, t, xr);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
-    out[i] = ext_force_at(f, s_amp, s_inv_h, x[i]);
+    out[i] = f.kind == EXT_EXPR ? expr_space(f, xr, x[i], t)
+                                : ext_force_at(f, s_amp, s_inv_h, x[i]);
 }
 
 void launch_ext_eval(const ExtForce& f, double t, const double* x, double* out, int64_t n,

@@ -177,6 +177,9 @@ extern "C" int wg_accel_noalloc(int64_t n, const double* x, const double* m, dou
   for (int i = 0; i < 4; ++i) ext.p[i] = 0.0;
   const int need = ext_kind == WG_EXT_NONE ? 0 : ext_kind == WG_EXT_HARMONIC ? 1
                  : ext_kind == WG_EXT_PULSE_TANH ? 4 : -1;
+  if (ext_kind == WG_EXT_EXPR)
+    return fail(WG_ERR_EXT, "wg_accel_noalloc: an expression force's program needs device "
+                            "memory of its own; use wg_accel");
   if (need < 0 || n_ext_params < need || (need > 0 && !ext_params))
     return fail(WG_ERR_EXT, "wg_accel_noalloc: unknown external force %d or too few parameters",
                 ext_kind);

@@ -22,6 +22,7 @@
 
 #include "../../include/wendy_gb300.h"
 #include "wg_bucket.cuh"
+#include "wg_ext.cuh"
 #include "wg_internal.cuh"
 
 using namespace wg;
@@ -90,6 +91,8 @@ struct PoolSim {
   int E = 0;
   double totmass = 0, omega2 = -1;
   ExtForce ext{};
+  ExtSpec ext_spec{};         // the force with an expression's program on the host
+  ExprOp* d_prog = nullptr;   // an expression force's program on the device
   int mode = 0;  // 0: sheets compact in ox..oi, half drift pending; 1: bucket layout
   int lay = 0, qsel = 0;
   int cslot = 0;  // aggregate slot describing layout `lay`
@@ -212,6 +215,7 @@ struct wg_pool {
   cudaStream_t dl_stream = nullptr;  // downloads while a step runs
   int64_t g_ntasks = -1;
   void* g_small = nullptr;
+  bool g_expr = false;   // the graph launches the expression-force instantiation
   int64_t graph_builds = 0;
 };
 
@@ -391,16 +395,12 @@ int wg_pool_add(wg_pool* p, int64_t n, const double* x, const double* v, const d
   }
   if (mmax > 2 * totmass)
     return pool_fail(WG_ERR_ARG, "a single mass exceeds twice totmass");
-  ExtForce ext;
-  ext.kind = ext_kind;
-  for (int i = 0; i < 4; ++i) ext.p[i] = 0.0;
-  const int need = ext_kind == WG_EXT_NONE ? 0 : ext_kind == WG_EXT_HARMONIC ? 1
-                 : ext_kind == WG_EXT_PULSE_TANH ? 4 : -1;
-  if (need < 0 || n_ext_params < need || (need > 0 && !ext_params))
-    return pool_fail(WG_ERR_EXT, "unknown external force %d or too few parameters", ext_kind);
-  for (int i = 0; i < need; ++i) ext.p[i] = ext_params[i];
-  if (ext_kind == WG_EXT_PULSE_TANH && (ext.p[2] == 0.0 || ext.p[3] == 0.0))
-    return pool_fail(WG_ERR_EXT, "pulsed force needs tau != 0 and h != 0");
+  ExtSpec ext;
+  {
+    char msg[256];
+    if (parse_ext(ext_kind, ext_params, n_ext_params, &ext, msg, sizeof(msg)) != WG_OK)
+      return pool_fail(WG_ERR_EXT, "%s", msg);
+  }
   const size_t bytes = sim_bytes(n);
   if (p->budget && p->used + (int64_t)bytes > p->budget)
     return pool_fail(WG_ERR_BUDGET, "simulation of %lld sheets needs %zu bytes; %lld of %lld in use",
@@ -420,7 +420,16 @@ int wg_pool_add(wg_pool* p, int64_t n, const double* x, const double* v, const d
   carve(s);
   s->totmass = totmass;
   s->omega2 = omega2;
-  s->ext = ext;
+  s->ext_spec = ext;
+  e = attach_ext_program(&s->ext_spec, &s->d_prog, p->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cudaFreeAsync(s->mem, p->stream);
+    delete s;
+    return pool_fail(WG_ERR_NOMEM, "upload of the external-force program failed: %s",
+                     cudaGetErrorString(e));
+  }
+  s->ext = s->ext_spec.f;
   if (totmass > 0) {
     int eT = 0;
     std::frexp(totmass, &eT);
@@ -457,6 +466,10 @@ int wg_pool_remove(wg_pool* p, int sim_id) {
   if (p->pend_active) return pool_fail(WG_ERR_ARG, "a step is in flight: call wg_pool_step_end first");
   PoolSim* s = p->sims[(size_t)sim_id];
   cudaFreeAsync(s->mem, p->stream);
+  if (s->d_prog) {
+    cudaStreamSynchronize(p->stream);
+    cudaFree(s->d_prog);
+  }
   p->used -= (int64_t)s->bytes;
   delete s;
   p->sims[(size_t)sim_id] = nullptr;
@@ -599,8 +612,11 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
   }
   // device sequence of the call, captured in a CUDA graph and replayed while
   // the number of simulations, buckets and sub-steps stays the same
+  bool launch_expr = false;  // the graph's kernels carry the expression interpreter
+  for (PoolSim* a : act) launch_expr |= a->ext.kind == EXT_EXPR;
   const bool rebuild = !p->gexec || p->g_count != count || p->g_nleap != nleap ||
-                       p->g_ntasks != ntasks || p->g_small != p->small;
+                       p->g_ntasks != ntasks || p->g_small != p->small ||
+                       p->g_expr != launch_expr;
   if (rebuild) {
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     p->gexec = nullptr;
@@ -634,6 +650,7 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
       L.ticket = p->tickets + i;
       L.err = p->err;
       L.profile = 0;
+      L.any_expr = launch_expr;
       launch_bucket_step(L, grid, p->stream);
     }
     cudaMemcpyAsync(p->h_oc, p->ocount, 8 * (size_t)count, cudaMemcpyDeviceToHost, p->stream);
@@ -648,6 +665,7 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
     p->g_nleap = nleap;
     p->g_ntasks = ntasks;
     p->g_small = p->small;
+    p->g_expr = launch_expr;
     p->graph_builds++;
   }
   PC(cudaGraphLaunch(p->gexec, p->stream));
@@ -770,6 +788,7 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
         L.ticket = p->tickets + i;
         L.err = p->err;
         L.profile = 0;
+        L.any_expr = s->ext.kind == EXT_EXPR;
         launch_bucket_step(L, s->tune.ctas_per_sm * p->sms, p->stream);
       }
       p->launches += 3 + kRadixLaunches + (nleap - from);
@@ -853,6 +872,10 @@ int wg_pool_destroy(wg_pool* p) {
   for (PoolSim* s : p->sims)
     if (s) {
       cudaFreeAsync(s->mem, p->stream);
+      if (s->d_prog) {
+        cudaStreamSynchronize(p->stream);
+        cudaFree(s->d_prog);
+      }
       delete s;
     }
   cudaStreamSynchronize(p->stream);
