@@ -56,9 +56,14 @@ def test_cpu_sorts_are_rejected_not_emulated():
         next(g)
 
 
-def test_callables_are_rejected():
+def test_callables_compile_or_are_rejected():
+    # a plain function in the supported subset compiles into an expression
+    # force; anything else (here: a comparison) is refused
+    assert resolve(lambda x, t: -x)[0] == _lib.EXT_EXPR
     with pytest.raises(ValueError):
-        resolve(lambda x, t: -x)
+        resolve(lambda x, t: x > t)
+    with pytest.raises(ValueError):
+        resolve(3.0)
     assert resolve(Harmonic(1.1))[0] == _lib.EXT_HARMONIC
     k, p = resolve(PulseTanh(0.3, 5., 1., 0.5))
     assert k == _lib.EXT_PULSE_TANH and p == (0.3, 5., 1., 0.5)
