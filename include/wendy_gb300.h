@@ -35,6 +35,7 @@ extern "C" {
 #define WG_ERR_EXT (-5)      /* unknown external-force id or bad parameter count */
 #define WG_ERR_BUDGET (-6)   /* request exceeds the memory budget it was admitted under */
 #define WG_ERR_NODEV (-7)    /* no CUDA device */
+#define WG_ERR_MAXCOLL (-8)  /* the exact solver reached maxcoll crossings in one output */
 
 /* ---- registered external forces ---------------------------------------- */
 #define WG_EXT_NONE 0
@@ -261,6 +262,32 @@ int wg_pool_download(wg_pool *p, int sim_id, double *x, double *v);
 int wg_pool_info(wg_pool *p, int64_t *used_bytes, int64_t *budget_bytes, int *n_sims,
                  int64_t *launches);
 int wg_pool_destroy(wg_pool *p);
+
+/* ---- the exact event-driven solver (nbody(..., approx=False)) ----------
+   wendy's exact path: every crossing of two neighbouring sheets is found
+   and processed in time order (wendy/wendy.c:53-315, its Python set-up
+   wendy/wendy.py:158-238).  One warp runs the event loop, with the state in
+   shared memory when it fits.  A cross-check for small N, not a fast path:
+   the events are a strict sequence.  The caller sets up the arrays as the
+   reference's _setup_arrays does: x, v, masses m (times twopiG, and divided
+   by omega^2 when omega > 0), accelerations a (mass above minus mass below;
+   with omega, the equilibrium offset of the same formula) and the sort order
+   sindx of x; the pair crossing times are computed on the device.
+   omega <= 0: no harmonic potential.  n in [2, 2^24]. */
+typedef struct wg_exact wg_exact;
+int wg_exact_create(int64_t n, const double *x, const double *v, const double *a,
+                    const double *m, const int32_t *sindx, double omega, wg_exact **out);
+/* One output interval dt: crossings until the next one lies beyond dt, at
+   most maxcoll of them (then WG_ERR_MAXCOLL, with the state advanced as the
+   reference's _wendy_nbody_onestep leaves it); *ncoll receives the number
+   processed, *time_elapsed the device time of the event loop.
+   Reference: _wendy_nbody_onestep and _wendy_nbody_harm_onestep,
+   wendy/wendy.c:53-315. */
+int wg_exact_step(wg_exact *e, double dt, int64_t maxcoll, int64_t *ncoll,
+                  double *time_elapsed);
+/* x, v, a in original order and the position order sindx (any may be NULL). */
+int wg_exact_download(wg_exact *e, double *x, double *v, double *a, int32_t *sindx);
+int wg_exact_destroy(wg_exact *e);
 
 /* Allocation-free force evaluation (no counterpart in the reference).
    For callers that cannot call cudaMalloc themselves or let this library do

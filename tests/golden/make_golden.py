@@ -20,6 +20,9 @@ Files:
   energy.npz    relative energy error per output of a 1000-output run
                 (N=10,000 sech^2 disk, dt=0.05, nleap=10)
   exact.npz     reference exact solver, N=101 sech^2 disk, 20 outputs
+  exact_more.npz  reference exact solver with a harmonic potential (N=101,
+                omega=1.1, 20 outputs) and at N=6000 (3 outputs), with the
+                number of crossings per output
   extexpr.npz   x, v after outputs 1 and 10 of runs with external forces
                 given as Python functions (tests/golden/forces.py), through
                 the reference's own callable route
@@ -79,6 +82,25 @@ def ref_accel(lib, x, m, omega2, ext, t):
     return a, xi["idx"].copy(), totmass
 
 
+def make_exact_more(wendy):
+    """The reference's exact solver with a harmonic potential and at a size
+    beyond what one GPU thread block's shared memory holds."""
+    out = {}
+    for name, n, seed, dt, nout, omega in (("harm", 101, 6, 0.05, 20, 1.1),
+                                           ("large", 6000, 7, 0.02, 3, None)):
+        x, v, m = ics.sech2_disk(n, seed=seed)
+        v = v - numpy.mean(v)
+        g = wendy.nbody(x.copy(), v.copy(), m.copy(), dt, omega=omega, full_output=True)
+        out[name + "/x0"], out[name + "/v0"], out[name + "/m"] = x, v, m
+        out[name + "/par"] = numpy.array([dt, nout, -1.0 if omega is None else omega])
+        for k in range(1, nout + 1):
+            tx, tv, nc, _el = next(g)
+            out["%s/x%d" % (name, k)] = tx.copy()
+            out["%s/v%d" % (name, k)] = tv.copy()
+            out["%s/ncoll%d" % (name, k)] = numpy.array([nc])
+    numpy.savez_compressed(os.path.join(HERE, "exact_more.npz"), **out)
+
+
 def make_extexpr(wendy):
     """Runs of the reference's generator with Python-function forces: with
     numba stubbed out, wendy wraps each function in its ctypes callback
@@ -104,7 +126,7 @@ def main():
     ap.add_argument("--ref-root", default=None,
                     help="reference checkout (default: $WENDY_REF_ROOT, else the one "
                          "oracle/_ref was built from)")
-    ap.add_argument("--only", default=None, choices=["extexpr"],
+    ap.add_argument("--only", default=None, choices=["extexpr", "exact_more"],
                     help="write just this file")
     args = ap.parse_args()
     lib = O.ref_library()
@@ -112,8 +134,8 @@ def main():
     if lib is None or wendy is None:
         sys.exit("reference library not built: run `make -C oracle ref` first")
     sys.path.insert(0, HERE)
-    if args.only == "extexpr":
-        make_extexpr(wendy)
+    if args.only:
+        {"extexpr": make_extexpr, "exact_more": make_exact_more}[args.only](wendy)
         print("golden vectors written to", HERE)
         return
 
@@ -214,6 +236,7 @@ def main():
         ex["x%d" % k] = tx.copy()
         ex["v%d" % k] = tv.copy()
     numpy.savez_compressed(os.path.join(HERE, "exact.npz"), **ex)
+    make_exact_more(wendy)
     make_extexpr(wendy)
     print("golden vectors written to", HERE)
 

@@ -76,10 +76,22 @@ def test_registered_forces_evaluate_like_numpy():
     assert numpy.array_equal(Harmonic(1.1)(x, 0.), -(1.1 ** 2.) * x)
 
 
-def test_exact_solver_is_not_offered():
-    g = wendy_gb300.nbody(numpy.array([-1., 1.]), numpy.zeros(2), numpy.ones(2), 2)
-    with pytest.raises(NotImplementedError):
-        next(g)
+def test_exact_solver_rejects_what_the_reference_rejects():
+    # wendy/wendy.py:159-165, checked before the GPU is touched
+    x, v = numpy.array([-1., 1.]), numpy.zeros(2)
+    cases = [(dict(ext_force=lambda x, t: -x), "External forces (ext_force=) are not supported "
+                                                "for the exact nbody calculation"),
+             (dict(omega=40.), "When omega is set, omega*dt needs to be less than pi/2; please "
+                               "adjust dt")]
+    for kw, msg in cases:
+        with pytest.raises(ValueError) as e:
+            next(wendy_gb300.nbody(x, v, numpy.ones(2), 0.05, **kw))
+        assert str(e.value) == msg
+    for m in (numpy.array([1., 0.]), numpy.array([1., 1e-10])):
+        with pytest.raises(ValueError) as e:
+            next(wendy_gb300.nbody(x, v, m, 2))
+        assert str(e.value) == ("Tiny masses m much smaller than the median mass are not "
+                                "supported, please remove these from the inputs")
 
 
 def test_tuning_table_rows_select_by_size():

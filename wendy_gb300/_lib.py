@@ -16,9 +16,10 @@ LIB_PATH = os.path.join(HERE, "_wendy_gb300.so")
 
 WG_OK = 0
 WG_ERR_ARG, WG_ERR_CUDA, WG_ERR_NOMEM, WG_ERR_DEVICE = -1, -2, -3, -4
-WG_ERR_EXT, WG_ERR_BUDGET, WG_ERR_NODEV = -5, -6, -7
+WG_ERR_EXT, WG_ERR_BUDGET, WG_ERR_NODEV, WG_ERR_MAXCOLL = -5, -6, -7, -8
 STATUS_NAMES = {0: "WG_OK", -1: "WG_ERR_ARG", -2: "WG_ERR_CUDA", -3: "WG_ERR_NOMEM",
-                -4: "WG_ERR_DEVICE", -5: "WG_ERR_EXT", -6: "WG_ERR_BUDGET", -7: "WG_ERR_NODEV"}
+                -4: "WG_ERR_DEVICE", -5: "WG_ERR_EXT", -6: "WG_ERR_BUDGET", -7: "WG_ERR_NODEV",
+                -8: "WG_ERR_MAXCOLL"}
 
 EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH, EXT_EXPR = 0, 1, 2, 3
 
@@ -28,7 +29,8 @@ EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", 
            "wg_nbody_approx_onestep", "wg_nbody_approx_stats", "wg_profile", "wg_host_register", "wg_host_unregister",
            "wg_accel_noalloc", "wg_pool_sim_bytes", "wg_pool_create", "wg_pool_add",
            "wg_pool_remove", "wg_pool_step", "wg_pool_step_begin", "wg_pool_step_end", "wg_pool_download", "wg_pool_info",
-           "wg_pool_destroy", "wg_set_tuning", "wg_get_tuning", "wg_set_debug_wait")
+           "wg_pool_destroy", "wg_set_tuning", "wg_get_tuning", "wg_set_debug_wait",
+           "wg_exact_create", "wg_exact_step", "wg_exact_download", "wg_exact_destroy")
 
 # Largest n wg_accel_noalloc accepts (its fixed device scratch array).
 NOALLOC_MAX_SHEETS = 65536
@@ -113,6 +115,11 @@ def lib():
     L.wg_host_unregister.argtypes = [_P]
     L.wg_accel_noalloc.argtypes = [_I64, _P, _P, _D, _D, _I, _F64, _I, _D, _P, _P, _P]
     L.wg_set_debug_wait.argtypes = [ctypes.c_uint, _I64]
+    _I32 = ndpointer(dtype=numpy.int32, flags=("C_CONTIGUOUS",))
+    L.wg_exact_create.argtypes = [_I64, _F64, _F64, _F64, _F64, _I32, _D, ctypes.POINTER(_P)]
+    L.wg_exact_step.argtypes = [_P, _D, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_D)]
+    L.wg_exact_download.argtypes = [_P, _P, _P, _P, _P]
+    L.wg_exact_destroy.argtypes = [_P]
     L.wg_pool_sim_bytes.argtypes = [_I64]
     L.wg_pool_create.argtypes = [_I64, ctypes.POINTER(_P)]
     L.wg_pool_add.argtypes = [_P, _I64, _F64, _F64, _F64, _D, _D, _I, _F64, _I,

@@ -15,9 +15,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_wendy_gb300.so")
 BUILD_DIR = os.path.join(HERE, "_build")
-SOURCES = ["wg_kernels.cu", "wg_radix.cu", "wg_bucket.cu", "wg_api.cu", "wg_pool.cu", "wg_noalloc.cu"]
+SOURCES = ["wg_kernels.cu", "wg_radix.cu", "wg_bucket.cu", "wg_api.cu", "wg_pool.cu",
+           "wg_exact.cu", "wg_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+# the exact solver follows the reference's operation order without FMA contraction
+FILE_FLAGS = {"wg_exact.cu": ["-fmad=false"]}
 
 
 def nvcc():
@@ -49,7 +52,7 @@ def build(verbose=False, force=False):
         o = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
         objs.append(o)
         if force or not _newer(o, [s] + headers):
-            jobs.append([cc] + ARCH + FLAGS + ["-c", s, "-o", o])
+            jobs.append([cc] + ARCH + FLAGS + FILE_FLAGS.get(src, []) + ["-c", s, "-o", o])
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         results = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs))
     for cmd, r in zip(jobs, results):

@@ -119,8 +119,10 @@ def nbody(x, v, m, dt, t0=0., twopiG=1., omega=None, ext_force=None, approx=Fals
           follow_edits=False):
     """Run a 1D N-body simulation (wendy/wendy.py:112-157 for the approximate path).
 
-    Only ``approx=True`` with ``sort='cuda'`` runs here; the exact
-    event-driven solver and the CPU sorts are the reference's.
+    ``approx=True`` runs the approximate leapfrog integrator (``sort`` must
+    be ``'cuda'``: the CPU sorts are the reference's); ``approx=False`` runs
+    the exact event-driven solver on one GPU warp (a cross-check for small N,
+    wendy/wendy.py:158-206).
     ``follow_edits=True`` (not in wendy) honours in-place edits of the
     yielded ``v`` between outputs, as wendy's C step does; see the module
     documentation.
@@ -134,8 +136,84 @@ def nbody(x, v, m, dt, t0=0., twopiG=1., omega=None, ext_force=None, approx=Fals
         yield from _nbody_approx(x, v, m, dt, nleap, t0=t0, sort=sort, omega=omega,
                                  ext_force=ext_force, twopiG=twopiG, full_output=full_output,
                                  follow_edits=follow_edits)
-    raise NotImplementedError("wendy_gb300 implements the approximate integrator (approx=True); "
-                              "the exact event-driven solver is the reference wendy's")
+        return
+    yield from _nbody_exact(x, v, m, dt, twopiG=twopiG, omega=omega, ext_force=ext_force,
+                            maxcoll=maxcoll, warn_maxcoll=warn_maxcoll, full_output=full_output)
+
+
+def _setup_exact(x, v, m):
+    """Sort order and accelerations of wendy's _setup_arrays
+    (wendy/wendy.py:208-238), with the same numpy operations; the pair
+    crossing times are computed on the device."""
+    sindx = numpy.argsort(x)
+    mass_below = numpy.cumsum(m[sindx])
+    mass_below[-1] = 0.
+    mass_below = numpy.roll(mass_below, 1)
+    mass_above = numpy.cumsum(m[sindx][::-1])[::-1]
+    mass_above[0] = 0.
+    mass_above = numpy.roll(mass_above, -1)
+    a = (mass_above - mass_below)[numpy.argsort(sindx)]
+    return (numpy.require(a, dtype=numpy.float64, requirements=["C", "W"]),
+            numpy.require(sindx, dtype=numpy.int32, requirements=["C"]))
+
+
+def _nbody_exact(x, v, m, dt, twopiG=1., omega=None, ext_force=None, maxcoll=100000,
+                 warn_maxcoll=False, full_output=False):
+    """Generator mirroring wendy's exact path (wendy/wendy.py:158-206) on the
+    GPU event loop (wg_exact_*): one output interval per ``next()``, yielding
+    the same x, v arrays updated in place (and the number of crossings and the
+    event loop's time with ``full_output=True``)."""
+    import warnings
+    if ext_force is not None:
+        raise ValueError("External forces (ext_force=) are not supported for the exact nbody "
+                         "calculation")
+    if omega is not None and omega * dt > numpy.pi / 2.:
+        raise ValueError("When omega is set, omega*dt needs to be less than pi/2; please adjust "
+                         "dt")
+    if numpy.any(m < numpy.median(m) * 10. ** -8.):
+        raise ValueError("Tiny masses m much smaller than the median mass are not supported, "
+                         "please remove these from the inputs")
+    x = numpy.require(copy.copy(x), dtype=numpy.float64, requirements=["C", "W"])
+    v = numpy.require(copy.copy(v), dtype=numpy.float64, requirements=["C", "W"])
+    m = numpy.require(twopiG * copy.copy(m), dtype=numpy.float64, requirements=["C", "W"])
+    if omega is not None:
+        m /= omega ** 2.
+    L = _lib.lib()
+
+    def create():
+        a, sindx = _setup_exact(x, v, m)
+        h = ctypes.c_void_p()
+        _lib.check(L.wg_exact_create(len(x), x, v, a, m, sindx,
+                                     float(omega) if omega is not None else 0., ctypes.byref(h)),
+                   "wg_exact_create")
+        return h
+
+    h = create()
+    ncoll = 0
+    try:
+        while True:
+            nc, el = ctypes.c_int64(0), ctypes.c_double(0.)
+            rc = L.wg_exact_step(h, float(dt), int(maxcoll), ctypes.byref(nc), ctypes.byref(el))
+            ncoll += nc.value
+            _lib.check(L.wg_exact_download(h, x.ctypes.data, v.ctypes.data, None, None),
+                       "wg_exact_download")
+            if rc == _lib.WG_ERR_MAXCOLL:
+                if warn_maxcoll:
+                    warnings.warn("Maximum number of collisions per time step exceeded",
+                                  RuntimeWarning)
+                    # re-compute the accelerations and crossing times
+                    L.wg_exact_destroy(h)
+                    h = create()
+                else:
+                    raise RuntimeError("Maximum number of collisions per time step exceeded")
+            else:
+                _lib.check(rc, "wg_exact_step")
+            if full_output:
+                yield (x, v, ncoll, el.value)
+            else:
+                yield (x, v)
+    finally:
+        L.wg_exact_destroy(h)
 
 
 def _nbody_approx(x, v, m, dt, nleap, t0=0., omega=None, ext_force=None, sort="cuda", twopiG=1.,
