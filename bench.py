@@ -62,7 +62,7 @@ WORKLOADS = {
     # ensemble / serving workloads (see run_ensemble, run_serve)
     "ensemble_4096": dict(sims=4096, nmin=1e3, nmax=1e6, nleap=10),
     "serve_poisson": dict(rate=200.0, nmin=1e3, nmax=4e6, smin=100, smax=10000, nleap=10,
-                          budget=150e9),
+                          budget=150e9, requests=1000),
 }
 
 
@@ -150,24 +150,35 @@ def run_ensemble(args, w):
     for a in pinned:
         LLL.wg_host_unregister(a.ctypes.data)
     pool.close()
+    e2e_value = total * nleap * k_e2e / wall
     # the plain path: a sample of the same simulations, one at a time
+    # the plain path on a random sample of the same simulations, one at a
+    # time: each simulation's step timed on the device (CUDA events, like the
+    # pool's `value`) and end to end (step + download into page-locked
+    # memory, wall clock, like the pool's `e2e`)
     rng = numpy.random.default_rng(1)
-    sample = rng.choice(len(mem), size=min(48, len(mem)), replace=False)
-    solo_ps, solo_t = 0, 0.0
+    sample = rng.choice(len(mem), size=min(args.plain_sample, len(mem)), replace=False)
+    solo_ps, solo_dev, solo_wall = 0, 0.0, 0.0
     for k in sample:
         n, fam, seed, dt, omega = mem[k]
         x, v, m = member_inputs(n, fam, seed)
         sim = wendy_gb300.Simulation(x, v, m, numpy.sum(m), omega ** 2)
         tt = ctypes.c_double(0.0)
-        sim.step(dt / nleap, nleap, tt)
-        t1 = time.perf_counter()
-        sim.step(dt / nleap, nleap, tt)
         xx, vv = numpy.empty(n), numpy.empty(n)
-        sim.download(xx, vv)
-        solo_t += time.perf_counter() - t1
-        solo_ps += n * nleap
+        pin = [a for a in (xx, vv) if LLL.wg_host_register(a.ctypes.data, a.nbytes) == 0]
+        for _ in range(args.warmup):
+            sim.step(dt / nleap, nleap, tt)
+        for _ in range(args.steps):
+            t1 = time.perf_counter()
+            solo_dev += sim.step(dt / nleap, nleap, tt)
+            sim.download(xx, vv)
+            solo_wall += time.perf_counter() - t1
+            solo_ps += n * nleap
+        for a in pin:
+            LLL.wg_host_unregister(a.ctypes.data)
         sim.close()
-    solo = solo_ps / solo_t
+    solo = solo_ps / solo_dev
+    solo_e2e = solo_ps / solo_wall
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -175,13 +186,15 @@ def run_ensemble(args, w):
             "config": {"workload": args.workload, "sims": len(mem), "sheets": total,
                        "nleap": nleap, "n_range": [w["nmin"], w["nmax"]],
                        "l2": "resident state larger than L2; no flush"},
-            "e2e": {"value": total * nleap * k_e2e / wall, "unit": "particle-steps/s",
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s",
                     "h2d_bytes_per_step": 16 * len(ids), "d2h_bytes_per_step": 16 * total,
                     "overlap": "every member's x, v downloaded every step into page-locked "
                                "memory while the next step runs; the last step's after it"},
             "plain_one_at_a_time": {"value": solo, "unit": "particle-steps/s",
-                                    "sample_sims": int(len(sample)),
-                                    "ratio_batched_over_plain": value / solo},
+                                    "e2e": solo_e2e, "sample_sims": int(len(sample)),
+                                    "steps_per_sim": args.steps,
+                                    "ratio_device_to_device": value / solo,
+                                    "ratio_e2e_to_e2e": e2e_value / solo_e2e},
             "clocks": clk.summary(), "gpu_launches": launches}
     print(json.dumps(line))
 
@@ -190,7 +203,7 @@ def run_serve(args, w):
     """Poisson stream of simulation requests: continuous batching vs the plain path."""
     from wendy_gb300.serve import Request, Server, latency_stats, serve_one_at_a_time
     rng = numpy.random.default_rng(0)
-    nreq = max(args.steps, 8)
+    nreq = args.requests or w["requests"]
     fams = ["sech2", "tophat", "gaussian"]
     reqs = []
     t = 0.0
@@ -205,20 +218,24 @@ def run_serve(args, w):
     srv = Server(budget_bytes=int(w["budget"]))
     with Clocks(0) as clk:
         served = srv.run([Request(**r) for r in reqs])
-    rounds = srv.rounds
+    rounds, waits, peak = srv.rounds, srv.budget_waits, srv.peak_bytes
     srv.close()
-    plain = serve_one_at_a_time([Request(**r) for r in reqs])
+    with Clocks(0) as clk_plain:
+        plain = serve_one_at_a_time([Request(**r) for r in reqs])
     a, b = latency_stats(served), latency_stats(plain)
     line = {"metric": "served p50/p99 latency and particle-steps/s", "value": a["p99_s"],
             "unit": "s (p99 latency)", "n_gpus": 1, "steps": nreq, "warmup": 0,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Poisson stream, seeded initial conditions)",
             "config": {"workload": args.workload, "requests": nreq, "rate_per_s": w["rate"],
+                       "arrivals_s": reqs[-1]["arrival"],
                        "n_range": [w["nmin"], w["nmax"]], "steps_range": [w["smin"], w["smax"]],
-                       "budget_bytes": w["budget"], "rounds": rounds},
+                       "budget_bytes": w["budget"], "rounds": rounds,
+                       "rounds_with_a_request_waiting_for_memory": waits,
+                       "peak_admitted_bytes": peak},
             "continuous_batching": a, "plain_one_at_a_time": b,
             "throughput_ratio": a["particle_steps_per_s"] / b["particle_steps_per_s"],
-            "clocks": clk.summary()}
+            "clocks": clk.summary(), "clocks_plain": clk_plain.summary()}
     print(json.dumps(line))
 
 HBM_FALLBACK_GBS = 6800.0
@@ -468,6 +485,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-full-run", action="store_true")
+    ap.add_argument("--plain-sample", type=int, default=48,
+                    help="ensemble_4096: simulations of the plain one-at-a-time comparison")
+    ap.add_argument("--requests", type=int, default=0,
+                    help="serve_poisson: requests in the stream (default 1000)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]

@@ -273,7 +273,8 @@ int wg_pool_destroy(wg_pool *p);
    by omega^2 when omega > 0), accelerations a (mass above minus mass below;
    with omega, the equilibrium offset of the same formula) and the sort order
    sindx of x; the pair crossing times are computed on the device.
-   omega <= 0: no harmonic potential.  n in [2, 2^24]. */
+   omega <= 0: no harmonic potential.  n from 2 to what the pair-time tree's
+   shared memory allows (about 600,000 sheets; WG_ERR_ARG beyond). */
 typedef struct wg_exact wg_exact;
 int wg_exact_create(int64_t n, const double *x, const double *v, const double *a,
                     const double *m, const int32_t *sindx, double omega, wg_exact **out);

@@ -54,7 +54,9 @@ struct ExactArgs {
   double omega;        // > 0: harmonic external potential
   double dt;
   long long maxcoll;
-  double* tree_val[kMaxLevels];  // internal levels of the tournament tree
+  // internal levels of the tournament tree: the order key of the smallest
+  // pair time below each node (see time_key) and that pair's index
+  uint64_t* tree_key[kMaxLevels];
   int32_t* tree_idx[kMaxLevels];
   int levels;
   int level_n[kMaxLevels + 1];   // entries per level (level 0: the n - 1 pair times)
@@ -62,7 +64,8 @@ struct ExactArgs {
   double* next_tcoll;  // in/out: its time
   long long* ncoll;    // out: crossings processed
   int* err;            // out: -2 when maxcoll was reached
-  int use_smem;        // the state is staged in shared memory
+  int use_smem;        // the state is staged in shared memory (after the tree)
+  size_t tree_bytes;   // shared memory of the tree's internal levels (16-byte multiple)
 };
 
 // The reference's root of the crossing quadratic c2 t^2 + c1 t + c0 = 0
@@ -80,45 +83,46 @@ __device__ double solve_coll_harm(double c0, double c1, double c2, double omega)
   return out / omega;
 }
 
-// Ordering of pair times: NaN after everything, ties to the lower index.
-__device__ __forceinline__ bool before(double va, int ia, double vb, int ib) {
-  const bool na = isnan(va), nb = isnan(vb);
-  if (na || nb) return !na && nb ? true : (na && nb ? ia < ib : false);
-  return va < vb || (va == vb && ia < ib);
+// Order key of a pair time: increasing in the time (integer compares, off
+// the FP64 pipe), NaN after everything.
+__device__ __forceinline__ uint64_t time_key(double t) {
+  return isnan(t) ? ~0ull : key_of(t);
 }
 
-__device__ __forceinline__ void warp_min(double& v, int& i) {
+// The smallest (key, index) over the warp; ties to the lower index.
+__device__ __forceinline__ void warp_min(uint64_t& k, int& i) {
 #pragma unroll
   for (int d = 16; d >= 1; d >>= 1) {
-    const double ov = __shfl_xor_sync(0xffffffffu, v, d);
+    const uint64_t ok = __shfl_xor_sync(0xffffffffu, k, d);
     const int oi = __shfl_xor_sync(0xffffffffu, i, d);
-    if (before(ov, oi, v, i)) {
-      v = ov;
+    if (ok < k || (ok == k && oi < i)) {
+      k = ok;
       i = oi;
     }
   }
 }
 
 // Recomputes the tree path above pair time `leaf` (all lanes).
-__device__ void tree_update(const ExactArgs& A, const double* tcoll, int leaf, int lane) {
+__device__ void tree_update(const ExactArgs& A, uint64_t* const* tkey, int32_t* const* tidx,
+                            const double* tcoll, int leaf, int lane) {
   int g = leaf / kTreeFan;  // group at level 0
   for (int lv = 0; lv < A.levels; ++lv) {
     const int j = g * kTreeFan + lane;
-    double v = NAN;
+    uint64_t k = ~0ull;
     int i = 0x7fffffff;
     if (j < A.level_n[lv]) {
       if (lv == 0) {
-        v = tcoll[j];
+        k = time_key(tcoll[j]);
         i = j;
       } else {
-        v = A.tree_val[lv - 1][j];
-        i = A.tree_idx[lv - 1][j];
+        k = tkey[lv - 1][j];
+        i = tidx[lv - 1][j];
       }
     }
-    warp_min(v, i);
+    warp_min(k, i);
     if (lane == 0) {
-      A.tree_val[lv][g] = v;
-      A.tree_idx[lv][g] = i;
+      tkey[lv][g] = k;
+      tidx[lv][g] = i;
     }
     __syncwarp();
     g /= kTreeFan;
@@ -147,23 +151,43 @@ __global__ void __launch_bounds__(32, 1) k_exact_step(const ExactArgs A) {
   const int lane = threadIdx.x;
   const int n = A.n;
   ExactState S = A.g;
-  if (A.use_smem) {
-    // stage the state in shared memory: x v a m t tcoll, then sindx
-    double* d = reinterpret_cast<double*>(smem);
-    S.x = d;
-    S.v = d + n;
-    S.a = d + 2 * n;
-    S.m = d + 3 * n;
-    S.t = d + 4 * n;
-    S.tcoll = d + 5 * n;
-    S.sindx = reinterpret_cast<int32_t*>(d + 6 * n);
-    for (int i = lane; i < n; i += 32) {
-      S.x[i] = A.g.x[i];
-      S.v[i] = A.g.v[i];
-      S.a[i] = A.g.a[i];
-      S.m[i] = A.g.m[i];
-      S.sindx[i] = A.g.sindx[i];
-      if (i < n - 1) S.tcoll[i] = A.g.tcoll[i];
+  // the tree's internal levels: in shared memory always (n / 31 entries)
+  uint64_t* tkey[kMaxLevels];
+  int32_t* tidx[kMaxLevels];
+  {
+    unsigned char* p = smem;
+    for (int lv = 0; lv < A.levels; ++lv) {
+      tkey[lv] = reinterpret_cast<uint64_t*>(p);
+      p += 8 * (size_t)A.level_n[lv + 1];
+    }
+    for (int lv = 0; lv < A.levels; ++lv) {
+      tidx[lv] = reinterpret_cast<int32_t*>(p);
+      p += 4 * (size_t)A.level_n[lv + 1];
+    }
+    for (int lv = 0; lv < A.levels; ++lv)
+      for (int j = lane; j < A.level_n[lv + 1]; j += 32) {
+        tkey[lv][j] = A.tree_key[lv][j];
+        tidx[lv][j] = A.tree_idx[lv][j];
+      }
+    p = smem + A.tree_bytes;
+    if (A.use_smem) {
+      // stage the state in shared memory too: x v a m t tcoll, then sindx
+      double* d = reinterpret_cast<double*>(p);
+      S.x = d;
+      S.v = d + n;
+      S.a = d + 2 * n;
+      S.m = d + 3 * n;
+      S.t = d + 4 * n;
+      S.tcoll = d + 5 * n;
+      S.sindx = reinterpret_cast<int32_t*>(d + 6 * n);
+      for (int i = lane; i < n; i += 32) {
+        S.x[i] = A.g.x[i];
+        S.v[i] = A.g.v[i];
+        S.a[i] = A.g.a[i];
+        S.m[i] = A.g.m[i];
+        S.sindx[i] = A.g.sindx[i];
+        if (i < n - 1) S.tcoll[i] = A.g.tcoll[i];
+      }
     }
   }
   for (int i = lane; i < n; i += 32) S.t[i] = 0.;
@@ -231,15 +255,11 @@ __global__ void __launch_bounds__(32, 1) k_exact_step(const ExactArgs A) {
     // the three pair times that changed, and their paths up the tree
     const int ci = cindx;
     const int lo = ci > 0 ? ci - 1 : ci, hi = ci < n - 2 ? ci + 1 : ci;
-    tree_update(A, S.tcoll, lo, lane);
-    if (hi / kTreeFan != lo / kTreeFan) tree_update(A, S.tcoll, hi, lane);
+    tree_update(A, tkey, tidx, S.tcoll, lo, lane);
+    if (hi / kTreeFan != lo / kTreeFan) tree_update(A, tkey, tidx, S.tcoll, hi, lane);
     // the next crossing: the root
-    double v = A.tree_val[A.levels - 1][0];
-    int i = A.tree_idx[A.levels - 1][0];
-    if (A.levels == 0) {
-      v = S.tcoll[0];
-      i = 0;
-    }
+    const int i = tidx[A.levels - 1][0];
+    const double v = S.tcoll[i];
     cindx = i;
     next = isnan(v) ? INFINITY : v;
   }
@@ -274,20 +294,20 @@ __global__ void k_exact_tree_level(ExactArgs A, int lv) {
   const int ng = (A.level_n[lv] + kTreeFan - 1) / kTreeFan;
   if (g >= ng) return;
   const int j = g * kTreeFan + lane;
-  double v = NAN;
+  uint64_t k = ~0ull;
   int i = 0x7fffffff;
   if (j < A.level_n[lv]) {
     if (lv == 0) {
-      v = A.g.tcoll[j];
+      k = time_key(A.g.tcoll[j]);
       i = j;
     } else {
-      v = A.tree_val[lv - 1][j];
+      k = A.tree_key[lv - 1][j];
       i = A.tree_idx[lv - 1][j];
     }
   }
-  warp_min(v, i);
+  warp_min(k, i);
   if (lane == 0) {
-    A.tree_val[lv][g] = v;
+    A.tree_key[lv][g] = k;
     A.tree_idx[lv][g] = i;
   }
 }
@@ -407,28 +427,32 @@ int wg_exact_create(int64_t n, const double* x, const double* v, const double* a
   A.g.t = reinterpret_cast<double*>(p); p += nd;
   A.g.tcoll = reinterpret_cast<double*>(p); p += nd;
   A.g.sindx = reinterpret_cast<int32_t*>(p); p += ni;
+  A.tree_bytes = 0;
   for (int lv = 0; lv < A.levels; ++lv) {
-    A.tree_val[lv] = reinterpret_cast<double*>(p); p += al(8 * (size_t)A.level_n[lv + 1]);
+    A.tree_key[lv] = reinterpret_cast<uint64_t*>(p); p += al(8 * (size_t)A.level_n[lv + 1]);
     A.tree_idx[lv] = reinterpret_cast<int32_t*>(p); p += al(4 * (size_t)A.level_n[lv + 1]);
+    A.tree_bytes += 12 * (size_t)A.level_n[lv + 1];
   }
+  A.tree_bytes = (A.tree_bytes + 15) & ~(size_t)15;
   A.cindx = reinterpret_cast<int*>(p);
   A.err = A.cindx + 1;
   A.ncoll = reinterpret_cast<long long*>(A.cindx + 2);
   A.next_tcoll = reinterpret_cast<double*>(A.cindx + 4);
-  // stage in shared memory when the state fits (6 doubles and an index per sheet)
-  const size_t smem = 52 * (size_t)n + 64;
+  // the tree's internal levels always live in shared memory; the state too
+  // when it fits (6 doubles and an index per sheet)
+  const size_t smem = A.tree_bytes + 52 * (size_t)n + 64;
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (smem <= (size_t)optin &&
+  A.use_smem = smem <= (size_t)optin;
+  e->smem = A.use_smem ? smem : A.tree_bytes;
+  if (e->smem > (size_t)optin ||
       cudaFuncSetAttribute(k_exact_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) == cudaSuccess) {
-    A.use_smem = 1;
-    e->smem = smem;
-  } else {
+                           (int)e->smem) != cudaSuccess) {
     cudaGetLastError();
-    A.use_smem = 0;
-    e->smem = 0;
+    free_exact(e);
+    return fail(WG_ERR_ARG, "exact solver: %lld sheets need more shared memory for the pair-time "
+                            "tree than a block has", (long long)n);
   }
   cudaStream_t s = e->stream;
   cudaError_t ce = cudaSuccess;

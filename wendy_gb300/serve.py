@@ -82,6 +82,8 @@ class Server:
         self.budget = int(budget_bytes)
         self.on_output = on_output
         self.rounds = 0
+        self.budget_waits = 0   # rounds in which an arrived request waited for memory
+        self.peak_bytes = 0     # most device bytes the admitted simulations held at once
 
     def run(self, requests, clock=time.perf_counter):
         """Serve `requests` (sorted by arrival) in real time; returns them.
@@ -120,12 +122,14 @@ class Server:
                 r = pending[i]
                 need = Pool.sim_bytes(r.n)
                 if used + need > self.budget:
+                    self.budget_waits += 1
                     break
                 sid = self.pool.add(r.x, r.v, r.m, omega=r.omega, ext_force=r.ext_force,
                                     twopiG=1.)
                 r.admitted_at = now
                 active[sid] = [r, r.noutputs, r.t0, _Pinned(r.n), 0]
                 used += need
+                self.peak_bytes = max(self.peak_bytes, used)
                 i += 1
             stepping = [sid for sid, a in active.items() if a[1] > 0]
             if not stepping and not unread:
