@@ -47,13 +47,6 @@ void set_error(const char* fmt, ...) {
 
 size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// Tight mode (see wg_sim): the target it lays buckets out with, the largest
-// bucket count after a restart that it answers (above it the flow is too
-// violent for buckets and the call finishes on the compact path), and the
-// clean calls after which the normal target returns.
-int tight_target(int target) { return target * 2 / 3 > 64 ? target * 2 / 3 : 64; }
-constexpr unsigned kTightLimit = kBucketCap * 3 / 2;
-constexpr int kTightExit = 8;
 // Most calls a violent overflow sends to the compact path before the bucket
 // path is tried again.
 constexpr int kMaxBackoff = 8;
@@ -166,14 +159,16 @@ struct wg_sim {
   bool pend_compact = false;     // ... and it runs on the compact path
   double pend_dt = 0;
   int pend_nleap = 0, pend_lay0 = 0, pend_cs0 = 0;
+  double pend_pre = 0;           // the opening half drift its first sub-step applies
   // bucketed layout (the fast path of wg_step)
   void* bk = nullptr;
-  int64_t nb = 0;        // buckets of the current layout: ceil(n / target_cur)
-  int64_t nb_cap = 0;    // buckets the arrays hold: ceil(n / tight target)
-  int target_cur = 0;    // sheets per bucket after a re-sort, now
-  // Tight mode: a flow that overflows buckets by a little right after a
-  // re-sort (a few per cent above capacity) is laid out with 2/3 of the
-  // target, until kTightExit calls in a row complete without an overflow.
+  int64_t nb = 0;        // buckets: ceil(n / target)
+  // Slots per bucket in the layouts: kBucketCapBig where the memory allows
+  // (a bucket above kBucketCap sheets is then taken in chunks by
+  // k_bucket_big), else kBucketCap (a fuller bucket overflows).
+  int capg = kBucketCap;
+  BigTask* big_list = nullptr;  // [nb]: big buckets of the sub-step in flight
+  unsigned* big_counts = nullptr;  // [2 cap]: per sub-step, listed and taken
   double* bx[2] = {nullptr, nullptr};
   double* bv[2] = {nullptr, nullptr};
   double* bm[2] = {nullptr, nullptr};
@@ -198,7 +193,6 @@ struct wg_sim {
   // penalty; the penalty halves after every call the bucket path completes.
   int compact_calls = 0;
   int backoff = 1;
-  int tight_clean = -1;  // clean calls in tight mode so far; -1: not in tight mode
   double pending_dt = 0; // dt of the half drift the bucket layout was routed for
   bool out_valid = false;  // x_out / v_out hold the last call's output
   // Split steps (wg_step_begin): a second pair of output buffers, so that the
@@ -250,12 +244,6 @@ int set_force(wg_sim* s, const ExtSpec& ext) {
   return WG_OK;
 }
 
-// Sheets per bucket of the next bucketize (and with it the bucket count).
-void set_target(wg_sim* s, int target) {
-  s->target_cur = target;
-  s->nb = (s->n + target - 1) / target;
-}
-
 int alloc_call_arrays(wg_sim* s, int nleap) {
   if (nleap <= s->cap) return WG_OK;
   int cap = 64;
@@ -277,7 +265,8 @@ int alloc_call_arrays(wg_sim* s, int nleap) {
   s->h_ep = nullptr;
   s->h_flags = nullptr;
   const size_t b = al(sizeof(StateTable)) + al(64) + al(sizeof(StepFlags) * (cap + 1)) +
-                   al(4 * (size_t)cap) + al(8 * (size_t)cap) + al(4 * (size_t)cap);
+                   al(4 * (size_t)cap) + al(8 * (size_t)cap) + al(4 * (size_t)cap) +
+                   al(8 * (size_t)cap);
   WG_CUDA(cudaMalloc(&s->small, b));
   char* p = static_cast<char*>(s->small);
   s->table = reinterpret_cast<StateTable*>(p); p += al(sizeof(StateTable));
@@ -286,6 +275,7 @@ int alloc_call_arrays(wg_sim* s, int nleap) {
   s->tickets = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)cap);
   s->t_seq = reinterpret_cast<double*>(p); p += al(8 * (size_t)cap);
   s->epochs = reinterpret_cast<unsigned*>(p); p += al(4 * (size_t)cap);
+  s->big_counts = reinterpret_cast<unsigned*>(p); p += al(8 * (size_t)cap);
   WG_CUDA(cudaMemsetAsync(s->small, 0, b, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->table, &t, sizeof(t), cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMallocHost(&s->h_t, 8 * (size_t)cap));
@@ -326,7 +316,8 @@ void free_sim(wg_sim* s) {
 
 // Allocate a simulation for n sheets with the given physics; sheet data is
 // uploaded by the caller.
-int make_sim(int64_t n, double totmass, double omega2, const ExtSpec& ext, wg_sim** out) {
+int make_sim(int64_t n, double totmass, double omega2, const ExtSpec& ext, wg_sim** out,
+             bool big_buckets = true) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
     cudaGetLastError();
@@ -395,18 +386,30 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtSpec& ext, wg_si
   // bucket layout: two layouts of nb buckets x capacity, counts, splitters,
   // look-back records, the overflow list
   s->tune = tuning_for(n);
-  s->target_cur = s->tune.target;
-  s->nb = (n + s->target_cur - 1) / s->target_cur;
-  s->nb_cap = (n + tight_target(s->tune.target) - 1) / tight_target(s->tune.target);
-  const int64_t nb = s->nb_cap;
-  const size_t slots = (size_t)nb * kBucketCap;
-  const size_t bk_b = 2 * (3 * al(slots * 8) + al(slots * 4)) +
-                      kAggSlots * (al(4 * (size_t)nb) + al(32 * (size_t)nb)) +
-                      2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
-                      al(sizeof(BucketRec) * (size_t)nb) + 3 * nd + ni + al(64) +
-                      al(4 * (size_t)nb) + al(sizeof(SimDev)) + al(sizeof(BucketTask) * (size_t)nb) +
-                      al(8 * 4 * (size_t)(kEnergyBlocks + 1));
+  s->nb = (n + s->tune.target - 1) / s->tune.target;
+  const int64_t nb = s->nb;
+  // layouts with room for big buckets where asked for and where the memory
+  // allows, else kBucketCap slots per bucket
+  size_t slots = 0, bk_b = 0;
+  auto bucket_bytes = [&](int capg) {
+    slots = (size_t)nb * (size_t)capg;
+    bk_b = 2 * (3 * al(slots * 8) + al(slots * 4)) +
+           kAggSlots * (al(4 * (size_t)nb) + al(32 * (size_t)nb)) +
+           2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
+           al(sizeof(BucketRec) * (size_t)nb) + 3 * nd + ni + al(64) + al(4 * (size_t)nb) +
+           al(sizeof(SimDev)) + al(sizeof(BucketTask) * (size_t)nb) +
+           al(8 * 4 * (size_t)(kEnergyBlocks + 1)) +
+           (capg > kBucketCap ? al(sizeof(BigTask) * (size_t)nb) : 0);
+  };
+  s->capg = big_buckets ? kBucketCapBig : kBucketCap;
+  bucket_bytes(s->capg);
   e = cudaMalloc(&s->bk, bk_b);
+  if (e != cudaSuccess && s->capg > kBucketCap) {
+    cudaGetLastError();
+    s->capg = kBucketCap;
+    bucket_bytes(s->capg);
+    e = cudaMalloc(&s->bk, bk_b);
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();
     set_error("cudaMalloc of %zu bytes for the bucket layout failed: %s", bk_b,
@@ -440,6 +443,10 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtSpec& ext, wg_si
   s->d_dev = reinterpret_cast<SimDev*>(p); p += al(sizeof(SimDev));
   s->d_tasks = reinterpret_cast<BucketTask*>(p); p += al(sizeof(BucketTask) * (size_t)nb);
   s->diag = reinterpret_cast<double*>(p); p += al(8 * 4 * (size_t)(kEnergyBlocks + 1));
+  if (s->capg > kBucketCap) {
+    s->big_list = reinterpret_cast<BigTask*>(p);
+    p += al(sizeof(BigTask) * (size_t)nb);
+  }
   {
     std::vector<BucketTask> tasks((size_t)nb);
     for (int64_t b = 0; b < nb; ++b) tasks[(size_t)b] = BucketTask{0, (int)b};
@@ -523,6 +530,15 @@ int finish_call(wg_sim* s, int nleap, bool count_sorts = true) {
   unsigned mc = 0;
   for (int i = 1; i <= nleap; ++i) mc = s->h_flags[i].max_cnt > mc ? s->h_flags[i].max_cnt : mc;
   s->st.last_max_count = mc;
+  if (s->big_list && nleap > 0) {
+    // big buckets listed per sub-step (of the launches that ran last for each)
+    std::vector<unsigned> bc(2 * (size_t)nleap);
+    if (cudaMemcpy(bc.data(), s->big_counts, 8 * (size_t)nleap, cudaMemcpyDeviceToHost) ==
+        cudaSuccess)
+      for (int i = 0; i < nleap; ++i) s->st.big_buckets += bc[2 * (size_t)i];
+    else
+      cudaGetLastError();
+  }
   if (err) {
     set_error("device error word 0x%x (%s); the simulation's state is lost, destroy it", err,
               device_error_names(err).c_str());
@@ -541,7 +557,7 @@ static_assert(kMaxLeap == WG_MAX_LEAP, "sub-step limit of the C header");
 int take_epochs(wg_sim* s, int count) {
   if (s->epoch + (unsigned)count > kEpochLimit) {
     WG_CUDA(cudaMemsetAsync(s->recs, 0, sizeof(TileRec) * (size_t)s->n_tiles, s->stream));
-    WG_CUDA(cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)s->nb_cap, s->stream));
+    WG_CUDA(cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)s->nb, s->stream));
     s->epoch = 1;
   }
   for (int i = 0; i < count; ++i) s->h_ep[i] = s->epoch + (unsigned)i;
@@ -591,7 +607,8 @@ int enqueue_step(wg_sim* s, double dt, int nleap, bool want_accel, double dt_las
 // Bucket layout `lay` with the counts of aggregate slot `cslot` (+ overflow
 // list) -> compact, unsorted sheets in the current sorted-state set.
 void bucket_to_compact(wg_sim* s, int lay, int cslot) {
-  launch_compact(s->table, s->nb, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay], s->bcnt[cslot],
+  launch_compact(s->table, s->nb, s->capg, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay],
+                 s->bcnt[cslot],
                  s->offs, s->ox, s->ov, s->om, s->oi, s->ocount, s->n, s->stream);
   s->st.launches += 2;
 }
@@ -628,7 +645,8 @@ void fill_dev(wg_sim* s, double dt, double pre) {
   d.t_seq = s->t_seq;
   d.n = s->n;
   d.nb = s->nb;
-  d.target = s->target_cur;
+  d.target = s->tune.target;
+  d.capg = s->capg;
   d.window = s->tune.window;
   d.sort_bits = s->tune.sort_bits;
   d.T_lo = s->T_lo;
@@ -656,7 +674,19 @@ StepLaunch step_launch(wg_sim* s, int i, int nleap, int profile) {
   L.err = s->err;
   L.profile = profile;
   L.any_expr = s->ext.kind == EXT_EXPR;
+  L.big_list = s->big_list;
+  L.big_count = s->big_counts + 2 * i;
+  L.big_ticket = s->big_counts + 2 * i + 1;
+  L.big_cap = s->big_list ? (unsigned)s->nb : 0u;
   return L;
+}
+
+// One sub-step on the bucket path: the fused kernel, then (simulations whose
+// buckets can outgrow shared memory) the big buckets it listed.
+void launch_substep(wg_sim* s, int i, int nleap, int profile) {
+  const StepLaunch L = step_launch(s, i, nleap, profile);
+  launch_bucket_step(L, s->grid_bucket, s->stream);
+  if (s->big_list) launch_bucket_big(L, s->grid_bucket, s->stream);
 }
 
 void fill_times(wg_sim* s, double dt, int nleap, double* t0) {
@@ -848,12 +878,13 @@ static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool reco
     // path (full re-sort + fused force kernel per sub-step)
     if (record_start) WG_CUDA(cudaEventRecord(s->ev0, s->stream));
     if (s->mode == 1) {
-      WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));
+      WG_CUDA(cudaMemsetAsync(s->ocount, 0, 16, s->stream));
       bucket_to_compact(s, s->lay, s->cslot);
       s->mode = 0;
     }
     rc = enqueue_step(s, dt, nleap, s->call_a != nullptr, dt / 2.);
     if (rc) return rc;
+    WG_CUDA(cudaMemsetAsync(s->big_counts, 0, 8 * (size_t)nleap, s->stream));
     s->st.substeps_compact += nleap;
     if (s->call_a) launch_scatter_accel(s->table, s->n, s->a_sorted, s->call_a, s->stream);
     if (s->call_xi)
@@ -872,16 +903,13 @@ static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool reco
   WG_CUDA(cudaMemcpyAsync(s->epochs, s->h_ep, 4 * (size_t)nleap, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemsetAsync(s->flags, 0, sizeof(StepFlags) * (nleap + 1), s->stream));
   WG_CUDA(cudaMemsetAsync(s->tickets, 0, 4 * (size_t)nleap, s->stream));
-  WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));  // overflow count and abort word
-  if (s->mode == 1 && (dt != s->pending_dt || s->tight_clean >= kTightExit)) {
-    // routed for another dt, or tight buckets no longer needed: back to
-    // compact state, the half drift still pending
+  WG_CUDA(cudaMemsetAsync(s->big_counts, 0, 8 * (size_t)nleap, s->stream));
+  // overflow count, abort word and redo word
+  WG_CUDA(cudaMemsetAsync(s->ocount, 0, 16, s->stream));
+  if (s->mode == 1 && dt != s->pending_dt) {
+    // routed for another dt: back to compact state, the half drift still pending
     bucket_to_compact(s, s->lay, s->cslot);
     s->mode = 0;
-  }
-  if (s->tight_clean >= kTightExit) {
-    s->tight_clean = -1;
-    set_target(s, s->tune.target);
   }
   double pre = 0.0;
   if (s->mode == 0) {
@@ -890,7 +918,8 @@ static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool reco
     s->lay = 0;
     s->qsel = 0;
     s->cslot = 0;
-    launch_bucketize(s->table, s->n, s->target_cur, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
+    launch_bucketize(s->table, s->n, s->tune.target, s->nb, s->capg, s->E, s->bx[0], s->bv[0],
+                     s->bm[0],
                      s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], s->stream);
     s->st.launches += 2 + kRadixLaunches;
     s->st.sorts_full += 1;
@@ -898,16 +927,17 @@ static int run_call_begin(wg_sim* s, double dt, int nleap, double* t0, bool reco
     pre = dt / 2.;
   }
   const int lay0 = s->lay, cs0 = s->cslot;
+  s->pend_pre = pre;
   fill_dev(s, dt, pre);
   WG_CUDA(cudaMemcpyAsync(s->d_dev, &s->dev, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream));
-  for (int i = 0; i < nleap; ++i) launch_bucket_step(step_launch(s, i, nleap, 0), s->grid_bucket, s->stream);
+  for (int i = 0; i < nleap; ++i) launch_substep(s, i, nleap, 0);
   launch_split_out(s->dev.rec_out, s->n, s->x_out, s->v_out, s->call_a, s->stream);
   s->lay = (lay0 + nleap) & 1;
   s->qsel = (s->qsel + nleap) & 1;
   s->cslot = (cs0 + nleap) % kAggSlots;
   s->st.launches += nleap + 1;
   WG_CUDA(cudaGetLastError());
-  WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
+  WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 16, cudaMemcpyDeviceToHost, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(StepFlags) * (nleap + 1),
                           cudaMemcpyDeviceToHost, s->stream));
   s->pend_active = true;
@@ -953,49 +983,63 @@ static int run_call_end(wg_sim* s, double* time_elapsed) {
   int from = 0;  // first sub-step of the current run of bucket launches
   bool clean = true;
   for (;;) {
-    const unsigned ab = s->h_ab[1];
-    if (ab == 0) {
+    const unsigned ab = s->h_ab[1], redo = s->h_ab[2];
+    if (ab == 0 && redo == 0) {
       window_steps += nleap - from;
       break;
     }
     clean = false;
-    // sub-step k overflowed a bucket: its sheets are complete in the layout
-    // it wrote plus the overflow list.  Re-sort them once, lay out fresh
-    // buckets (exact quantiles) and restart the remaining sub-steps on the
-    // bucket path; a last sub-step has already written every output.
-    const int k = (int)ab - 1;
-    window_steps += k + 1 - from;
-    s->st.sorts_full += 1;
-    const int lay_k = (lay0 + k + 1) & 1;
-    bucket_to_compact(s, lay_k, (cs0 + k + 1) % kAggSlots);
-    if (k == nleap - 1) {
-      s->mode = 0;  // the next call re-sorts
-      break;
-    }
-    if (from > 0 && k < from + 2) {
-      // overflowed again right after a re-sort.  A little above capacity:
-      // restart once more with tight buckets (2/3 of the target).  Otherwise
-      // the buckets cannot follow this flow for now: finish the call on the
-      // compact path and keep the next calls there (back-off doubling up to
-      // kMaxBackoff calls).
-      const unsigned worst = s->h_flags[k + 1].max_cnt;
-      const int tight = tight_target(s->tune.target);
-      if (worst <= kTightLimit && s->target_cur != tight) {
-        set_target(s, tight);
-        s->tight_clean = 0;
-      } else {
-        compact_continue(s, dt, nleap, k + 1);
-        s->mode = 0;
-        s->out_valid = false;
-        s->compact_calls = s->backoff;
-        s->backoff = s->backoff < kMaxBackoff ? 2 * s->backoff : kMaxBackoff;
+    int k, resume;
+    if (redo) {
+      // sub-step k met a big bucket it could not cut into chunks: the layout
+      // it read is intact, its own output is dropped.  Re-sort that layout
+      // and run the sub-steps from k again.
+      k = (int)redo - 1;
+      window_steps += k - from;
+      s->st.sorts_full += 1;
+      WG_CUDA(cudaMemsetAsync(s->ocount, 0, 16, s->stream));
+      bucket_to_compact(s, (lay0 + k) & 1, (cs0 + k) % kAggSlots);
+      // a call's first sub-step applies the opening half drift while loading
+      if (k == 0 && s->pend_pre != 0.0)
+        launch_drift(s->table, s->n, s->pend_pre, nullptr, s->stream);
+      resume = k;
+    } else {
+      // sub-step k overflowed a bucket: its sheets are complete in the layout
+      // it wrote plus the overflow list.  Re-sort them once, lay out fresh
+      // buckets (exact quantiles) and restart the remaining sub-steps on the
+      // bucket path; a last sub-step has already written every output.
+      k = (int)ab - 1;
+      window_steps += k + 1 - from;
+      s->st.sorts_full += 1;
+      bucket_to_compact(s, (lay0 + k + 1) & 1, (cs0 + k + 1) % kAggSlots);
+      if (k == nleap - 1) {
+        s->mode = 0;  // the next call re-sorts
         break;
       }
+      resume = k + 1;
     }
-    from = k + 1;
+    if (from > 0 && k < from + 2) {
+      // failed again right after a re-sort: the buckets cannot follow this
+      // flow for now.  Finish the call on the compact path and keep the next
+      // calls there (back-off doubling up to kMaxBackoff calls).
+      compact_continue(s, dt, nleap, resume);
+      s->mode = 0;
+      s->out_valid = false;
+      s->compact_calls = s->backoff;
+      s->backoff = s->backoff < kMaxBackoff ? 2 * s->backoff : kMaxBackoff;
+      break;
+    }
+    from = resume;
+    // fresh look-back epochs for the sub-steps that run again (a redone
+    // sub-step published records under its old epoch)
+    rc = take_epochs(s, nleap - from);
+    if (rc) return rc;
+    WG_CUDA(cudaMemcpyAsync(s->epochs + from, s->h_ep, 4 * (size_t)(nleap - from),
+                            cudaMemcpyHostToDevice, s->stream));
     WG_CUDA(cudaMemsetAsync(&s->flags[from].unsorted, 1, sizeof(unsigned), s->stream));
     radix_sort_state(s->table, s->n, &s->radix, &s->flags[from], s->err, s->stream);
-    launch_bucketize(s->table, s->n, s->target_cur, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
+    launch_bucketize(s->table, s->n, s->tune.target, s->nb, s->capg, s->E, s->bx[0], s->bv[0],
+                     s->bm[0],
                      s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], s->stream);
     // sub-step `from` reads layout 0, aggregate slot 0 and routes by splitter set 0
     lay0 = from & 1;
@@ -1007,25 +1051,25 @@ static int run_call_end(wg_sim* s, double* time_elapsed) {
     fill_dev(s, dt, 0.0);
     WG_CUDA(cudaMemcpyAsync(s->d_dev, &s->dev, sizeof(SimDev), cudaMemcpyHostToDevice,
                             s->stream));
-    WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));
+    WG_CUDA(cudaMemsetAsync(s->ocount, 0, 16, s->stream));
     // the skipped launches of these sub-steps consumed their tickets
     WG_CUDA(cudaMemsetAsync(s->tickets + from, 0, 4 * (size_t)(nleap - from), s->stream));
-    for (int i = from; i < nleap; ++i)
-      launch_bucket_step(step_launch(s, i, nleap, 0), s->grid_bucket, s->stream);
+    WG_CUDA(cudaMemsetAsync(s->big_counts + 2 * from, 0, 8 * (size_t)(nleap - from),
+                            s->stream));
+    for (int i = from; i < nleap; ++i) launch_substep(s, i, nleap, 0);
     launch_split_out(s->dev.rec_out, s->n, s->x_out, s->v_out, s->call_a, s->stream);
     s->lay = (lay0 + nleap) & 1;
     s->qsel = (qs0 + nleap) & 1;
     s->cslot = (cs0 + nleap) % kAggSlots;
     s->st.launches += 4 + kRadixLaunches + (nleap - from);
     WG_CUDA(cudaGetLastError());
-    WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 8, cudaMemcpyDeviceToHost, s->stream));
+    WG_CUDA(cudaMemcpyAsync(s->h_ab, s->ocount, 16, cudaMemcpyDeviceToHost, s->stream));
     WG_CUDA(cudaMemcpyAsync(s->h_flags, s->flags, sizeof(StepFlags) * (nleap + 1),
                             cudaMemcpyDeviceToHost, s->stream));
     WG_CUDA(cudaStreamSynchronize(s->stream));
   }
   s->st.sorts_window += window_steps;
   if (clean && s->backoff > 1) s->backoff /= 2;
-  if (s->tight_clean >= 0) s->tight_clean = clean ? s->tight_clean + 1 : 0;
   WG_CUDA(cudaEventRecord(s->ev1, s->stream));
   rc = finish_call(s, nleap, false);
   float ms = 0;
@@ -1184,6 +1228,7 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   WG_CUDA(cudaMemcpyAsync(s->t_seq, s->h_t, 8 * (size_t)reps, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemcpyAsync(s->epochs, s->h_ep, 4 * (size_t)reps, cudaMemcpyHostToDevice, s->stream));
   WG_CUDA(cudaMemsetAsync(s->tickets, 0, 4 * (size_t)reps, s->stream));
+  WG_CUDA(cudaMemsetAsync(s->big_counts, 0, 8 * (size_t)reps, s->stream));
   // flags[i].unsorted = 1 forces every sort to run in full
   for (int i = 0; i < reps; ++i) s->h_flags[i] = StepFlags{1u, 0u, 0ull};
   WG_CUDA(cudaMemcpyAsync(s->flags, s->h_flags, sizeof(StepFlags) * (size_t)reps,
@@ -1205,7 +1250,7 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   a.dt_kick = 0.0;
   a.dt_drift = 0.0;
   a.flag_out = &s->flags[s->cap];  // scratch slot
-  WG_CUDA(cudaMemsetAsync(s->ocount, 0, 8, s->stream));
+  WG_CUDA(cudaMemsetAsync(s->ocount, 0, 16, s->stream));
   WG_CUDA(cudaStreamSynchronize(s->stream));
   const int lay_start = s->lay, cs_start = s->cslot;
   if (what == WG_PROF_BUCKET) {
@@ -1216,7 +1261,7 @@ int wg_profile(wg_sim* s, int what, int reps, double* avg_seconds) {
   WG_CUDA(cudaEventRecord(s->ev0, s->stream));
   for (int i = 0; i < reps; ++i) {
     if (what == WG_PROF_BUCKET) {
-      launch_bucket_step(step_launch(s, i, reps, 1), s->grid_bucket, s->stream);
+      launch_substep(s, i, reps, 1);
     } else if (what == WG_PROF_FORCE) {
       a.sub = i;
       a.ticket = s->tickets + i;
@@ -1396,7 +1441,7 @@ int wg_accel(int64_t n, const double* x, const double* m, double totmass, double
   rc = check_ext(ext_kind, ext_params, n_ext_params, &ext);
   if (rc) return rc;
   wg_sim* s = nullptr;
-  rc = make_sim(n, totmass, omega2, ext, &s);
+  rc = make_sim(n, totmass, omega2, ext, &s, false);
   if (rc) return rc;
   const StateRef c = s->set[0];
   cudaMemcpyAsync(c.x, x, 8 * n, cudaMemcpyHostToDevice, s->stream);

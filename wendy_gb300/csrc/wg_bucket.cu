@@ -53,6 +53,13 @@ constexpr int WARPS = BT / 32;
 constexpr int RWIN = kSplitterWindow;
 constexpr int NBIN = 1 << kSortBitsMax;  // bins the shared memory is sized for
 constexpr int MAXBIN = 48;          // a fuller bin sends the bucket to the radix sort
+// Big buckets are cut into chunks of at most CAP sheets along 4096 key bins:
+// a chunk starts at every bin whose exclusive count passes a multiple of
+// CHUNK, so a chunk holds at most CHUNK + (its last bin) <= CAP sheets as long
+// as no bin holds more than CAP - CHUNK.
+constexpr int BIGBINS = 4096;
+constexpr int CHUNK = CAP / 2;
+constexpr int kMaxChunks = kBucketCapBig / CHUNK + 1;
 // Two 16-bit bin counters (later offsets) per 32-bit word: bin b lives in the
 // half (b & 1) of word b / 2.  Words are padded with one per 32 so that a
 // thread scanning 16 consecutive words and its 31 neighbours hit 32
@@ -136,6 +143,11 @@ struct StepSmem {
   unsigned long long maxv;
   unsigned maxc;  // largest destination count this task saw after its reservations
   uint64_t mbar;  // completion of the bucket's bulk copies
+  // a big bucket (k_bucket_big): its chunks as ranges of key bins
+  int chunk_lo[kMaxChunks + 1];
+  int nchunks;
+  unsigned load_cnt;  // sheets of the current chunk gathered so far
+  unsigned splittable;
 };
 
 // Two CTAs per SM: 228 KiB of shared memory per SM, 1 KiB reserved per CTA.
@@ -520,12 +532,13 @@ __device__ __forceinline__ void prepare_task(const StepLaunch& L, int sub, unsig
     if (lane == 0) out.n = -1;
     return;
   }
-  const int n = own_c < (unsigned)CAP ? (int)own_c : CAP;
+  const int capg = D.capg;
+  const int n = own_c < (unsigned)capg ? (int)own_c : capg;
   const int lay = (D.lay0 + sub) & 1;
   if (lane == 0 && n > 0) {
     // the bucket is loaded after the current one: bring it into L2 now
-    const uint32_t n4 = (uint32_t)((n + 3) & ~3);
-    const int64_t base = b * CAP;
+    const uint32_t n4 = (uint32_t)((min(n, CAP) + 3) & ~3);
+    const int64_t base = b * capg;
     bulk_prefetch_l2(D.bx[lay] + base, n4 * 8u);
     bulk_prefetch_l2(D.bv[lay] + base, n4 * 8u);
     bulk_prefetch_l2(D.bm[lay] + base, n4 * 8u);
@@ -606,6 +619,346 @@ __device__ __forceinline__ void claim_task(const StepLaunch& L, int sub, unsigne
   prepare_task(L, sub, ep, lane, t, tk, S, wbuf);
 }
 
+// Sort, scan, force, kick, drift, route and write out the n <= CAP sheets of
+// a bucket (or of one chunk of a big bucket) that sit in shared memory, with
+// their key range [kmin, kmax]; S.prefix_mass / S.prefix_cnt hold the
+// exclusive (mass, count) prefix of the first of them and the splitter window
+// of the next layout is in S.wkey[S.cur_wbuf].  PREP: warp 0 prepares the
+// next task (S.next_ticket, ntk) during the grouping, as the main kernel's
+// pipeline does; otherwise (chunks of a big bucket) the prefix base is
+// advanced past these sheets at the end.
+template <bool LAST, bool EXPR, bool PREP>
+__device__ __forceinline__ void process_bucket(const StepLaunch& L, StepSmem& S, const SimDev& D,
+                                               const int64_t b, const int lay, const int n,
+                                               const int sub, const unsigned ep, uint64_t kmin,
+                                               uint64_t kmax, const BucketTask ntk) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ipt = (n + BT - 1) / BT;
+  const int E = D.E;
+  const uint64_t* const wk = S.wkey[S.cur_wbuf];
+  const int32_t* const wi = S.widx[S.cur_wbuf];
+  // ---- sort the bucket
+  if (n > 1) {
+    bucket_sort(S, n, ipt, kmin, kmax, D.sort_bits);
+  } else {
+    if (tid == 0) S.perm[0] = 0;
+    __syncthreads();
+  }
+
+  // ---- exact prefix of the masses in sorted order: thread tid holds the
+  // sorted positions [tid * ipt, tid * ipt + ipt)
+  if (PREP && tid == 0) S.next_tk = ntk;
+  const int j0 = tid * ipt;
+  const int nmine = (j0 < n) ? ((n - j0) < ipt ? (n - j0) : ipt) : 0;
+  u128 tot = 0;
+  for (int i = 0; i < nmine; ++i) {
+    const u128 M = mass_to_fixed(S.m[S.perm[j0 + i]], E);
+    S.u.pos.mfix[j0 + i] = M;
+    tot += M;
+  }
+  const u128 incl = warp_inclusive_scan_u128(tot, lane);
+  uint32_t cin = (uint32_t)nmine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, cin, o);
+    if (lane >= o) cin += y;
+  }
+  if (lane == 31) {
+    S.warp_mass[warp] = incl;
+    S.warp_cnt[warp] = cin;
+  }
+  __syncthreads();
+  u128 C = S.prefix_mass;
+  uint32_t rank0 = S.prefix_cnt;
+#pragma unroll
+  for (int w = 0; w < WARPS; ++w) {
+    if (w < warp) {
+      C += S.warp_mass[w];
+      rank0 += S.warp_cnt[w];
+    }
+  }
+  C += incl - tot;
+  rank0 += cin - (uint32_t)nmine;
+
+  // ---- splitters of the layout after next: keys at global ranks j*T
+  uint64_t* qnk = D.qk[1 - ((D.qsel0 + sub) & 1)];
+  int32_t* qni = D.qi[1 - ((D.qsel0 + sub) & 1)];
+  if (b == 0 && tid == 0) {
+    qnk[0] = 0ull;
+    qni[0] = (int32_t)0x80000000;
+    qnk[D.nb] = ~0ull;
+    qni[D.nb] = 0x7fffffff;
+  }
+  // descriptor fields used per sheet, held in registers (the descriptor is
+  // in global memory and the compiler cannot prove the stores below leave it alone)
+  const int has_omega = D.has_omega;
+  const double omega2 = D.omega2;
+  const ExtForce ext = D.ext;
+  // an expression force: its time phase, once per task and thread
+  double xr[EXPR ? kExprRegs : 1];
+  double t_ev = 0.0;
+  if constexpr (EXPR) {
+    if (ext.kind == EXT_EXPR) {
+      t_ev = D.t_seq[sub];
+      expr_time(ext, t_ev, xr);
+    }
+  }
+  const uint32_t target = (uint32_t)D.target;
+  const int64_t nbk = D.nb;
+  // ---- force, kick, drift, routing; new x, v go back to their slots and
+  // the destination of every sorted position to the (now free) sort area
+  const double dt = L.profile ? 0.0 : D.dt;
+  const double dt_drift = LAST ? dt / 2. : dt;
+  const double dest_dt = (LAST && !L.profile) ? dt / 2. : 0.0;
+  const i128 T = (i128)((((u128)D.T_hi) << 64) | D.T_lo);
+  unsigned long long maxv = 0;
+  // the first rank >= rank0 that is a positive multiple of the target
+  // starts the next splitter (one per thread at most: ipt <= 8 < target)
+  uint32_t qnext = (rank0 + target - 1) / target;
+  qnext = qnext ? qnext : 1u;
+  const uint32_t rnext = qnext * target;
+  // two sheets at a time, interleaved, so that their shared-memory and
+  // FP64 latencies overlap; the window searches run in lock-step
+  const int wlen = S.win_hi - S.win_lo;
+  int top = 1;
+  while ((top << 1) < wlen) top <<= 1;
+  for (int i0 = 0; i0 < nmine; i0 += 2) {
+    const bool ok1 = i0 + 1 < nmine;
+    int sl[2];
+    uint64_t kd[2];
+    int32_t idv[2];
+    bool live[2] = {true, ok1};
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      sl[u] = S.perm[j0 + (live[u] ? i0 + u : i0)];
+      idv[u] = S.idx[sl[u]];
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (!live[u]) {
+        kd[u] = 0;
+        continue;
+      }
+      const int sidx = sl[u];
+      const uint32_t r = rank0 + (uint32_t)(i0 + u);
+      const double x = S.x[sidx], v = S.v[sidx];
+      if (r == rnext) {
+        qnk[qnext] = key_of(x);
+        qni[qnext] = idv[u];
+      }
+      const u128 M = S.u.pos.mfix[j0 + i0 + u];
+      const i128 A = T - 2 * (i128)C - (i128)M;
+      C += M;
+      double acc = fixed_to_double(A, E);
+      if (has_omega) acc = fma(-omega2, x, acc);
+      if constexpr (EXPR) {
+        if (ext.kind == EXT_EXPR)
+          acc = expr_space(ext, xr, x, t_ev) + acc;
+        else if (ext.kind != EXT_NONE)
+          acc = ext_force_at(ext, S.amp, S.inv_h, x) + acc;
+      } else if (ext.kind != EXT_NONE) {
+        acc = ext_force_at(ext, S.amp, S.inv_h, x) + acc;
+      }
+      const double vn = fma(dt, acc, v);
+      const double xn = fma(dt_drift, vn, x);
+      S.x[sidx] = xn;
+      S.v[sidx] = vn;
+      const unsigned long long av =
+          (unsigned long long)__double_as_longlong(vn) & 0x7FFFFFFFFFFFFFFFull;
+      maxv = av > maxv ? av : maxv;
+      if (LAST && !L.profile) {
+        OutRec* const ro = D.rec_out;
+        if (ro) {
+          double2* const r2 = reinterpret_cast<double2*>(ro + idv[u]);
+          r2[0] = make_double2(xn, vn);
+          r2[1] = make_double2(acc, 0.0);
+        } else {
+          D.x_out[idv[u]] = xn;
+          D.v_out[idv[u]] = vn;
+          double* const a_out = D.a_out;
+          if (a_out) a_out[idv[u]] = acc;
+        }
+        SheetRec* const xi_out = D.xi_out;
+        if (xi_out) {
+          SheetRec rec;
+          rec.idx = idv[u];
+          rec.pad = 0;
+          rec.val = xn;
+          xi_out[r] = rec;
+        }
+      }
+      kd[u] = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, vn, xn) : xn);
+    }
+    // routing: binary lifting over the window, both sheets in lock-step
+    int l[2] = {0, 0};
+    bool inw[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      inw[u] = live[u] && win_ge(wk, wi, 0, kd[u], idv[u]) && !win_ge(wk, wi, wlen, kd[u], idv[u]);
+    // the largest l with key Q_l <= key, on keys alone; then splitters with
+    // an equal key and a larger index step back (pair order)
+    for (int step = top; step >= 1; step >>= 1) {
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+        if (l[u] + step < wlen && wk[l[u] + step] <= kd[u]) l[u] += step;
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      while (l[u] > 0 && wk[l[u]] == kd[u] && wi[l[u]] > idv[u]) --l[u];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (!live[u]) continue;
+      // destination: window entry l, or wlen for a bucket outside the
+      // window (found again, by a global search, where it is needed)
+      const int w = inw[u] ? l[u] : wlen;
+      const int pq = j0 + i0 + u;
+      S.u.pos.dw[pq] = (uint8_t)w;
+      S.u.pos.drk[pq] = (uint16_t)atomicAdd(&S.dcount[w], 1u);
+    }
+  }
+  __syncthreads();
+  // ---- the sheets grouped by destination bucket of the next layout.  Warp 0
+  // prepares the next task meanwhile; the other warps synchronise among
+  // themselves (named barrier 1) until the block-wide barrier below.
+  const int cw = (D.cs0 + sub + 1) % kAggSlots;
+  unsigned* const cnt_out = D.bcnt[cw];
+  unsigned long long* const mass_out = D.bmass[cw];
+  const uint64_t* const qfar = D.qk[(D.qsel0 + sub) & 1];
+  const int32_t* const ifar = D.qi[(D.qsel0 + sub) & 1];
+  uint32_t db = 0;
+  if (warp == 0) {
+    if constexpr (PREP) prepare_task(L, sub, ep, lane, S.next_ticket, S.next_tk, S, S.cur_wbuf ^ 1);
+  } else {
+    const int wt = tid - 32;  // 0 .. BT - 33
+    // slots: one atomic per window bucket, its round trip overlapping the
+    // grouping and the mass sums
+    if (wt < wlen) {
+      const uint32_t c = S.dcount[wt];
+      if (c) {
+        db = atomicAdd(&cnt_out[S.win_lo + wt], c);
+        atomicMax(&S.maxc, db + c);
+      }
+    }
+    if (warp == 1) {
+      // segments: exclusive prefix of the counts of the wlen + 1 entries
+      constexpr int E5 = (2 * RWIN + 2 + 31) / 32;
+      uint32_t cv[E5];
+      uint32_t sum = 0;
+#pragma unroll
+      for (int k = 0; k < E5; ++k) {
+        const int j = lane * E5 + k;
+        cv[k] = j <= wlen ? S.dcount[j] : 0u;
+        sum += cv[k];
+      }
+      uint32_t incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      uint32_t ex = incl - sum;
+#pragma unroll
+      for (int k = 0; k < E5; ++k) {
+        const int j = lane * E5 + k;
+        if (j <= wlen) S.dstart[j] = ex;
+        ex += cv[k];
+      }
+      if (lane == 31) S.dstart[wlen + 1] = incl;
+    }
+    bar_sync_workers();
+    for (int pq = wt; pq < n; pq += BT - 32)
+      S.u.pos.order[S.dstart[S.u.pos.dw[pq]] + S.u.pos.drk[pq]] = (uint16_t)pq;
+    bar_sync_workers();
+    // ---- masses of the next layout: a warp sums the fixed-point masses of
+    // a window bucket's segment and adds them to that bucket's accumulators
+    for (int w = warp - 1; w < wlen; w += WARPS - 1) {
+      const int q0 = (int)S.dstart[w], q1 = (int)S.dstart[w + 1];
+      if (q0 == q1) continue;
+      u128 P = 0;
+      for (int q = q0 + lane; q < q1; q += 32) P += S.u.pos.mfix[S.u.pos.order[q]];
+      P = warp_sum_u128(P);
+      if (lane < 4) {
+        const unsigned long long limb = (unsigned long long)(uint32_t)(P >> (32 * lane));
+        if (limb) atomicAdd(&mass_out[4 * (int64_t)(S.win_lo + w) + lane], limb);
+      }
+    }
+    // sheets bound outside the window: one by one
+    for (int q = (int)S.dstart[wlen] + wt; q < n; q += BT - 32) {
+      const int pq = S.u.pos.order[q];
+      const int sl = S.perm[pq];
+      const double xn = S.x[sl];
+      const uint64_t kf = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, S.v[sl], xn) : xn);
+      const int d = dest_bucket(wk, wi, S.win_lo, wlen, qfar, ifar, nbk, kf, S.idx[sl]);
+      const u128 M = S.u.pos.mfix[pq];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const unsigned long long limb = (unsigned long long)(uint32_t)(M >> (32 * k));
+        if (limb) atomicAdd(&mass_out[4 * (int64_t)d + k], limb);
+      }
+    }
+    if (wt < wlen) S.dbase[wt] = db;
+  }
+  __syncthreads();
+  bool overflow = false;
+  {
+    // write-out grouped by destination: consecutive positions of a segment
+    // take consecutive slots, so a warp's stores coalesce
+    double* const xout = D.bx[1 - lay];
+    double* const vout = D.bv[1 - lay];
+    double* const mout = D.bm[1 - lay];
+    int32_t* const iout = D.bi[1 - lay];
+    for (int q = tid; q < n; q += BT) {
+      const int pq = S.u.pos.order[q];
+      const int w = S.u.pos.dw[pq];
+      const int sl = S.perm[pq];
+      int d;
+      uint32_t slot;
+      if (w < wlen) {
+        d = S.win_lo + w;
+        slot = S.dbase[w] + (uint32_t)q - S.dstart[w];
+      } else {
+        const double xn = S.x[sl];
+        const uint64_t kf = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, S.v[sl], xn) : xn);
+        d = dest_bucket(wk, wi, S.win_lo, wlen, qfar, ifar, nbk, kf, S.idx[sl]);
+        slot = atomicAdd(&cnt_out[d], 1u);
+        atomicMax(&S.maxc, slot + 1u);
+      }
+      if (slot < (uint32_t)D.capg) {
+        const int64_t o = (int64_t)d * D.capg + slot;
+        xout[o] = S.x[sl];
+        vout[o] = S.v[sl];
+        mout[o] = S.m[sl];
+        iout[o] = S.idx[sl];
+      } else {
+        const uint32_t o = atomicAdd(D.ocount, 1u);
+        D.ox[o] = S.x[sl];
+        D.ov[o] = S.v[sl];
+        D.om[o] = S.m[sl];
+        D.oi[o] = S.idx[sl];
+        overflow = true;
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) {
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, maxv, d);
+    maxv = o > maxv ? o : maxv;
+  }
+  if (lane == 0 && maxv) atomicMax(&S.maxv, maxv);
+  if (overflow) atomicCAS(D.ocount + 1, 0u, (unsigned)(sub + 1));
+  __syncthreads();
+  if (tid == 0 && S.maxv) atomicMax(&D.flags[sub + 1].max_v, S.maxv);
+  if (tid == 0 && S.maxc) atomicMax(&D.flags[sub + 1].max_cnt, S.maxc);
+  if (!PREP && tid == 0) {
+    // the next chunk of a big bucket starts where this one ended
+    u128 tot_all = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) tot_all += S.warp_mass[w];
+    S.prefix_mass += tot_all;
+    S.prefix_cnt += (uint32_t)n;
+  }
+}
+
 // The fused sub-step.  LAST: the call's last sub-step (half drift, outputs).
 // EXPR: the launch has simulations with expression forces (the interpreter
 // is compiled only into this instantiation).
@@ -631,11 +984,39 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       if (warp == 0) claim_task(L, sub, ep, lane, S, tm.wbuf);
       continue;
     }
+    if (tm.n > CAP) {
+      // more sheets than shared memory holds (a simulation whose layout has
+      // room for them): listed for k_bucket_big, which runs next on the
+      // stream and takes the bucket in chunks.  Its prefix is known already.
+      if (tid == 0) {
+        const unsigned slot = atomicAdd(L.big_count, 1u);
+        if (slot < L.big_cap) {
+          BigTask bt;
+          bt.sim = tm.sim;
+          bt.bucket = (int)tm.bucket;
+          bt.n = tm.n;
+          bt.lay = tm.lay;
+          bt.wlo = tm.wlo;
+          bt.whi = tm.whi;
+          bt.pcnt = tm.pcnt;
+          bt.pm_lo = tm.pm_lo;
+          bt.pm_hi = tm.pm_hi;
+          bt.amp = tm.amp;
+          bt.inv_h = tm.inv_h;
+          L.big_list[slot] = bt;
+        } else {
+          atomicOr(L.err, DEV_ERR_BAD_STATE);
+        }
+      }
+      __syncthreads();  // every thread has read S.next
+      if (warp == 0) claim_task(L, sub, ep, lane, S, tm.wbuf);
+      continue;
+    }
     const SimDev& D = L.sims[tm.sim];
     const int64_t b = tm.bucket;
     const int lay = tm.lay;
     const int n = tm.n;
-    const int64_t base = b * CAP;
+    const int64_t base = b * D.capg;
     // ---- load: the bucket's four arrays arrive by bulk copy (sizes rounded
     // up to 4 sheets, which stays inside the bucket's capacity), then its
     // keys and key range are formed from shared memory
@@ -652,13 +1033,9 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     // and the task is prepared by warp 0 during the write-out
     unsigned nt = 0;
     if (tid == 0) nt = atomicAdd(L.ticket, 1u);
-    const int ipt = (n + BT - 1) / BT;
     const double pre = sub == 0 ? D.pre_dt : 0.0;
-    const int E = D.E;
     // the splitter window of the next layout around this bucket arrived with
     // the task; the per-destination counters are cleared here
-    const uint64_t* const wk = S.wkey[tm.wbuf];
-    const int32_t* const wi = S.widx[tm.wbuf];
     for (int j = tid; j <= tm.whi - tm.wlo; j += BT) S.dcount[j] = 0;  // wlen + 1 entries
     if (tid == 0) {
       S.win_lo = tm.wlo;
@@ -724,325 +1101,206 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       kmin = S.red_min[w] < kmin ? S.red_min[w] : kmin;
       kmax = S.red_max[w] > kmax ? S.red_max[w] : kmax;
     }
-    // ---- sort the bucket
-    if (n > 1) {
-      bucket_sort(S, n, ipt, kmin, kmax, D.sort_bits);
-    } else {
-      if (tid == 0) S.perm[0] = 0;
-      __syncthreads();
-    }
+    process_bucket<LAST, EXPR, true>(L, S, D, b, lay, n, sub, ep, kmin, kmax, ntk);
+  }
+}
 
-    // ---- exact prefix of the masses in sorted order: thread tid holds the
-    // sorted positions [tid * ipt, tid * ipt + ipt)
-    if (tid == 0) S.next_tk = ntk;
-    const int j0 = tid * ipt;
-    const int nmine = (j0 < n) ? ((n - j0) < ipt ? (n - j0) : ipt) : 0;
-    u128 tot = 0;
-    for (int i = 0; i < nmine; ++i) {
-      const u128 M = mass_to_fixed(S.m[S.perm[j0 + i]], E);
-      S.u.pos.mfix[j0 + i] = M;
-      tot += M;
-    }
-    const u128 incl = warp_inclusive_scan_u128(tot, lane);
-    uint32_t cin = (uint32_t)nmine;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, cin, o);
-      if (lane >= o) cin += y;
-    }
-    if (lane == 31) {
-      S.warp_mass[warp] = incl;
-      S.warp_cnt[warp] = cin;
-    }
-    __syncthreads();
-    u128 C = S.prefix_mass;
-    uint32_t rank0 = S.prefix_cnt;
-#pragma unroll
-    for (int w = 0; w < WARPS; ++w) {
-      if (w < warp) {
-        C += S.warp_mass[w];
-        rank0 += S.warp_cnt[w];
-      }
-    }
-    C += incl - tot;
-    rank0 += cin - (uint32_t)nmine;
+// Bin of a key in [kmin, kmin + span] among BIGBINS (non-decreasing in the
+// key; the same multiplicative map as the in-bucket counting sort).
+__device__ __forceinline__ int big_bin(uint64_t k, uint64_t kmin, uint64_t span, uint64_t scale) {
+  const uint64_t dk = k - kmin;
+  return span < (uint64_t)BIGBINS ? (int)dk : (int)__umul64hi(dk, scale);
+}
 
-    // ---- splitters of the layout after next: keys at global ranks j*T
-    uint64_t* qnk = D.qk[1 - ((D.qsel0 + sub) & 1)];
-    int32_t* qni = D.qi[1 - ((D.qsel0 + sub) & 1)];
-    if (b == 0 && tid == 0) {
-      qnk[0] = 0ull;
-      qni[0] = (int32_t)0x80000000;
-      qnk[D.nb] = ~0ull;
-      qni[D.nb] = 0x7fffffff;
-    }
-    // descriptor fields used per sheet, held in registers (the descriptor is
-    // in global memory and the compiler cannot prove the stores below leave it alone)
-    const int has_omega = D.has_omega;
-    const double omega2 = D.omega2;
-    const ExtForce ext = D.ext;
-    // an expression force: its time phase, once per task and thread
-    double xr[EXPR ? kExprRegs : 1];
-    double t_ev = 0.0;
-    if constexpr (EXPR) {
-      if (ext.kind == EXT_EXPR) {
-        t_ev = D.t_seq[sub];
-        expr_time(ext, t_ev, xr);
-      }
-    }
-    const uint32_t target = (uint32_t)D.target;
-    const int64_t nbk = D.nb;
-    // ---- force, kick, drift, routing; new x, v go back to their slots and
-    // the destination of every sorted position to the (now free) sort area
-    const double dt = L.profile ? 0.0 : D.dt;
-    const double dt_drift = LAST ? dt / 2. : dt;
-    const double dest_dt = (LAST && !L.profile) ? dt / 2. : 0.0;
-    const i128 T = (i128)((((u128)D.T_hi) << 64) | D.T_lo);
-    unsigned long long maxv = 0;
-    // the first rank >= rank0 that is a positive multiple of the target
-    // starts the next splitter (one per thread at most: ipt <= 8 < target)
-    uint32_t qnext = (rank0 + target - 1) / target;
-    qnext = qnext ? qnext : 1u;
-    const uint32_t rnext = qnext * target;
-    // two sheets at a time, interleaved, so that their shared-memory and
-    // FP64 latencies overlap; the window searches run in lock-step
-    const int wlen = S.win_hi - S.win_lo;
-    int top = 1;
-    while ((top << 1) < wlen) top <<= 1;
-    for (int i0 = 0; i0 < nmine; i0 += 2) {
-      const bool ok1 = i0 + 1 < nmine;
-      int sl[2];
-      uint64_t kd[2];
-      int32_t idv[2];
-      bool live[2] = {true, ok1};
+// Position (with the opening half drift of a call applied) of slot j.
+__device__ __forceinline__ double big_pos(const double* gx, const double* gv, int j, double pre) {
+  const double x = gx[j];
+  return pre != 0.0 ? fma(pre, gv[j], x) : x;
+}
+
+// Block-wide minimum and maximum of per-thread key ranges (all threads).
+__device__ __forceinline__ void block_range(StepSmem& S, uint64_t& kmin, uint64_t& kmax) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        sl[u] = S.perm[j0 + (live[u] ? i0 + u : i0)];
-        idv[u] = S.idx[sl[u]];
-      }
+  for (int d = 16; d >= 1; d >>= 1) {
+    const uint64_t o1 = __shfl_xor_sync(0xffffffffu, kmin, d);
+    const uint64_t o2 = __shfl_xor_sync(0xffffffffu, kmax, d);
+    kmin = o1 < kmin ? o1 : kmin;
+    kmax = o2 > kmax ? o2 : kmax;
+  }
+  if (lane == 0) {
+    S.red_min[warp] = kmin;
+    S.red_max[warp] = kmax;
+  }
+  __syncthreads();
+  kmin = ~0ull;
+  kmax = 0;
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        if (!live[u]) {
-          kd[u] = 0;
-          continue;
-        }
-        const int sidx = sl[u];
-        const uint32_t r = rank0 + (uint32_t)(i0 + u);
-        const double x = S.x[sidx], v = S.v[sidx];
-        if (r == rnext) {
-          qnk[qnext] = key_of(x);
-          qni[qnext] = idv[u];
-        }
-        const u128 M = S.u.pos.mfix[j0 + i0 + u];
-        const i128 A = T - 2 * (i128)C - (i128)M;
-        C += M;
-        double acc = fixed_to_double(A, E);
-        if (has_omega) acc = fma(-omega2, x, acc);
-        if constexpr (EXPR) {
-          if (ext.kind == EXT_EXPR)
-            acc = expr_space(ext, xr, x, t_ev) + acc;
-          else if (ext.kind != EXT_NONE)
-            acc = ext_force_at(ext, S.amp, S.inv_h, x) + acc;
-        } else if (ext.kind != EXT_NONE) {
-          acc = ext_force_at(ext, S.amp, S.inv_h, x) + acc;
-        }
-        const double vn = fma(dt, acc, v);
-        const double xn = fma(dt_drift, vn, x);
-        S.x[sidx] = xn;
-        S.v[sidx] = vn;
-        const unsigned long long av =
-            (unsigned long long)__double_as_longlong(vn) & 0x7FFFFFFFFFFFFFFFull;
-        maxv = av > maxv ? av : maxv;
-        if (LAST && !L.profile) {
-          OutRec* const ro = D.rec_out;
-          if (ro) {
-            double2* const r2 = reinterpret_cast<double2*>(ro + idv[u]);
-            r2[0] = make_double2(xn, vn);
-            r2[1] = make_double2(acc, 0.0);
-          } else {
-            D.x_out[idv[u]] = xn;
-            D.v_out[idv[u]] = vn;
-            double* const a_out = D.a_out;
-            if (a_out) a_out[idv[u]] = acc;
-          }
-          SheetRec* const xi_out = D.xi_out;
-          if (xi_out) {
-            SheetRec rec;
-            rec.idx = idv[u];
-            rec.pad = 0;
-            rec.val = xn;
-            xi_out[r] = rec;
-          }
-        }
-        kd[u] = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, vn, xn) : xn);
-      }
-      // routing: binary lifting over the window, both sheets in lock-step
-      int l[2] = {0, 0};
-      bool inw[2];
-#pragma unroll
-      for (int u = 0; u < 2; ++u)
-        inw[u] = live[u] && win_ge(wk, wi, 0, kd[u], idv[u]) && !win_ge(wk, wi, wlen, kd[u], idv[u]);
-      // the largest l with key Q_l <= key, on keys alone; then splitters with
-      // an equal key and a larger index step back (pair order)
-      for (int step = top; step >= 1; step >>= 1) {
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-          if (l[u] + step < wlen && wk[l[u] + step] <= kd[u]) l[u] += step;
-      }
-#pragma unroll
-      for (int u = 0; u < 2; ++u)
-        while (l[u] > 0 && wk[l[u]] == kd[u] && wi[l[u]] > idv[u]) --l[u];
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        if (!live[u]) continue;
-        // destination: window entry l, or wlen for a bucket outside the
-        // window (found again, by a global search, where it is needed)
-        const int w = inw[u] ? l[u] : wlen;
-        const int pq = j0 + i0 + u;
-        S.u.pos.dw[pq] = (uint8_t)w;
-        S.u.pos.drk[pq] = (uint16_t)atomicAdd(&S.dcount[w], 1u);
-      }
-    }
+  for (int w = 0; w < WARPS; ++w) {
+    kmin = S.red_min[w] < kmin ? S.red_min[w] : kmin;
+    kmax = S.red_max[w] > kmax ? S.red_max[w] : kmax;
+  }
+  __syncthreads();  // red_min / red_max are free again
+}
+
+// The big buckets k_bucket_step listed in this sub-step (kBucketCap < n <=
+// capg sheets): each is cut by key into chunks that fit in shared memory --
+// a histogram of its keys over BIGBINS bins, chunks along the bins -- and
+// every chunk is gathered from the layout and processed like a bucket, the
+// chunks in key order with the mass and rank prefix carried from one to the
+// next.  A bucket whose keys crowd into one bin beyond CAP - CHUNK cannot be
+// cut this way: the simulation is flagged (ocount[2]) and its host side
+// re-sorts the layout this sub-step read, which the sub-step leaves intact.
+template <bool LAST, bool EXPR>
+__global__ void __launch_bounds__(BT, 2) k_bucket_big(const StepLaunch L) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  StepSmem& S = *reinterpret_cast<StepSmem*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int sub = L.sub;
+  const unsigned ep = L.epochs[sub];
+  const unsigned total = *L.big_count;  // final: k_bucket_step ran before
+  const unsigned ntask = total < L.big_cap ? total : L.big_cap;
+  for (;;) {
     __syncthreads();
-    // ---- the sheets grouped by destination bucket of the next layout.  Warp 0
-    // prepares the next task meanwhile; the other warps synchronise among
-    // themselves (named barrier 1) until the block-wide barrier below.
-    const int cw = (D.cs0 + sub + 1) % kAggSlots;
-    unsigned* const cnt_out = D.bcnt[cw];
-    unsigned long long* const mass_out = D.bmass[cw];
-    const uint64_t* const qfar = D.qk[(D.qsel0 + sub) & 1];
-    const int32_t* const ifar = D.qi[(D.qsel0 + sub) & 1];
-    uint32_t db = 0;
-    if (warp == 0) {
-      prepare_task(L, sub, ep, lane, S.next_ticket, S.next_tk, S, S.cur_wbuf ^ 1);
-    } else {
-      const int wt = tid - 32;  // 0 .. BT - 33
-      // slots: one atomic per window bucket, its round trip overlapping the
-      // grouping and the mass sums
-      if (wt < wlen) {
-        const uint32_t c = S.dcount[wt];
-        if (c) {
-          db = atomicAdd(&cnt_out[S.win_lo + wt], c);
-          atomicMax(&S.maxc, db + c);
-        }
-      }
-      if (warp == 1) {
-        // segments: exclusive prefix of the counts of the wlen + 1 entries
-        constexpr int E5 = (2 * RWIN + 2 + 31) / 32;
-        uint32_t cv[E5];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int k = 0; k < E5; ++k) {
-          const int j = lane * E5 + k;
-          cv[k] = j <= wlen ? S.dcount[j] : 0u;
-          sum += cv[k];
-        }
-        uint32_t incl = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        uint32_t ex = incl - sum;
-#pragma unroll
-        for (int k = 0; k < E5; ++k) {
-          const int j = lane * E5 + k;
-          if (j <= wlen) S.dstart[j] = ex;
-          ex += cv[k];
-        }
-        if (lane == 31) S.dstart[wlen + 1] = incl;
-      }
-      bar_sync_workers();
-      for (int pq = wt; pq < n; pq += BT - 32)
-        S.u.pos.order[S.dstart[S.u.pos.dw[pq]] + S.u.pos.drk[pq]] = (uint16_t)pq;
-      bar_sync_workers();
-      // ---- masses of the next layout: a warp sums the fixed-point masses of
-      // a window bucket's segment and adds them to that bucket's accumulators
-      for (int w = warp - 1; w < wlen; w += WARPS - 1) {
-        const int q0 = (int)S.dstart[w], q1 = (int)S.dstart[w + 1];
-        if (q0 == q1) continue;
-        u128 P = 0;
-        for (int q = q0 + lane; q < q1; q += 32) P += S.u.pos.mfix[S.u.pos.order[q]];
-        P = warp_sum_u128(P);
-        if (lane < 4) {
-          const unsigned long long limb = (unsigned long long)(uint32_t)(P >> (32 * lane));
-          if (limb) atomicAdd(&mass_out[4 * (int64_t)(S.win_lo + w) + lane], limb);
-        }
-      }
-      // sheets bound outside the window: one by one
-      for (int q = (int)S.dstart[wlen] + wt; q < n; q += BT - 32) {
-        const int pq = S.u.pos.order[q];
-        const int sl = S.perm[pq];
-        const double xn = S.x[sl];
-        const uint64_t kf = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, S.v[sl], xn) : xn);
-        const int d = dest_bucket(wk, wi, S.win_lo, wlen, qfar, ifar, nbk, kf, S.idx[sl]);
-        const u128 M = S.u.pos.mfix[pq];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const unsigned long long limb = (unsigned long long)(uint32_t)(M >> (32 * k));
-          if (limb) atomicAdd(&mass_out[4 * (int64_t)d + k], limb);
-        }
-      }
-      if (wt < wlen) S.dbase[wt] = db;
-    }
+    if (tid == 0) S.next_ticket = atomicAdd(L.big_ticket, 1u);
     __syncthreads();
-    bool overflow = false;
+    const unsigned t = S.next_ticket;
+    if (t >= ntask) break;
+    const BigTask bt = L.big_list[t];
+    const SimDev& D = L.sims[bt.sim];
+    const int n = bt.n;
+    const int64_t base = (int64_t)bt.bucket * D.capg;
+    const double* gx = D.bx[bt.lay] + base;
+    const double* gv = D.bv[bt.lay] + base;
+    const double* gm = D.bm[bt.lay] + base;
+    const int32_t* gi = D.bi[bt.lay] + base;
+    const double pre = sub == 0 ? D.pre_dt : 0.0;
+    // the splitter window of the next layout around the bucket
     {
-      // write-out grouped by destination: consecutive positions of a segment
-      // take consecutive slots, so a warp's stores coalesce
-      double* const xout = D.bx[1 - lay];
-      double* const vout = D.bv[1 - lay];
-      double* const mout = D.bm[1 - lay];
-      int32_t* const iout = D.bi[1 - lay];
-      for (int q = tid; q < n; q += BT) {
-        const int pq = S.u.pos.order[q];
-        const int w = S.u.pos.dw[pq];
-        const int sl = S.perm[pq];
-        int d;
-        uint32_t slot;
-        if (w < wlen) {
-          d = S.win_lo + w;
-          slot = S.dbase[w] + (uint32_t)q - S.dstart[w];
-        } else {
-          const double xn = S.x[sl];
-          const uint64_t kf = key_of(LAST && dest_dt != 0.0 ? fma(dest_dt, S.v[sl], xn) : xn);
-          d = dest_bucket(wk, wi, S.win_lo, wlen, qfar, ifar, nbk, kf, S.idx[sl]);
-          slot = atomicAdd(&cnt_out[d], 1u);
-          atomicMax(&S.maxc, slot + 1u);
-        }
-        if (slot < (uint32_t)CAP) {
-          const int64_t o = (int64_t)d * CAP + slot;
-          xout[o] = S.x[sl];
-          vout[o] = S.v[sl];
-          mout[o] = S.m[sl];
-          iout[o] = S.idx[sl];
-        } else {
-          const uint32_t o = atomicAdd(D.ocount, 1u);
-          D.ox[o] = S.x[sl];
-          D.ov[o] = S.v[sl];
-          D.om[o] = S.m[sl];
-          D.oi[o] = S.idx[sl];
-          overflow = true;
-        }
+      const int qs = (D.qsel0 + sub) & 1;
+      for (int j = tid; j <= bt.whi - bt.wlo; j += BT) {
+        S.wkey[0][j] = D.qk[qs][bt.wlo + j];
+        S.widx[0][j] = D.qi[qs][bt.wlo + j];
       }
     }
-#pragma unroll
-    for (int d = 16; d >= 1; d >>= 1) {
-      const unsigned long long o = __shfl_xor_sync(0xffffffffu, maxv, d);
-      maxv = o > maxv ? o : maxv;
+    if (tid == 0) {
+      S.win_lo = bt.wlo;
+      S.win_hi = bt.whi;
+      S.cur_wbuf = 0;
+      S.maxv = 0;
+      S.maxc = 0;
+      S.prefix_mass = (((u128)bt.pm_hi) << 64) | bt.pm_lo;
+      S.prefix_cnt = bt.pcnt;
+      S.amp = bt.amp;
+      S.inv_h = bt.inv_h;
+      S.nchunks = 0;
+      S.splittable = 1u;
+      for (int c = 0; c <= kMaxChunks; ++c) S.chunk_lo[c] = BIGBINS;
     }
-    if (lane == 0 && maxv) atomicMax(&S.maxv, maxv);
-    if (overflow) atomicCAS(D.ocount + 1, 0u, (unsigned)(sub + 1));
+    // ---- the bucket's key range and the histogram of its keys
+    uint64_t kmin = ~0ull, kmax = 0;
+    for (int j = tid; j < n; j += BT) {
+      const uint64_t k = key_of(big_pos(gx, gv, j, pre));
+      kmin = k < kmin ? k : kmin;
+      kmax = k > kmax ? k : kmax;
+    }
+    uint32_t* hist = S.u.srt.bins;  // BIGBINS 32-bit counters
+    for (int j = tid; j < BIGBINS; j += BT) hist[j] = 0u;
+    block_range(S, kmin, kmax);
+    const uint64_t span = kmax - kmin;
+    uint64_t scale = 0;
+    if (span >= (uint64_t)BIGBINS)
+      scale = (uint64_t)((float)BIGBINS / ((float)span + 1.0f) * 18446744073709551616.0f *
+                         (1.0f - 9.5367431640625e-07f));
+    for (int j = tid; j < n; j += BT) {
+      const int bin = big_bin(key_of(big_pos(gx, gv, j, pre)), kmin, span, scale);
+      atomicAdd(&hist[bin], 1u);
+    }
     __syncthreads();
-    if (tid == 0 && S.maxv) atomicMax(&D.flags[sub + 1].max_v, S.maxv);
-    if (tid == 0 && S.maxc) atomicMax(&D.flags[sub + 1].max_cnt, S.maxc);
+    // ---- chunks: thread tid owns bins [16 tid, 16 tid + 16)
+    {
+      constexpr int BPT = BIGBINS / BT;
+      uint32_t c[BPT], sum = 0, mx = 0;
+#pragma unroll
+      for (int k = 0; k < BPT; ++k) {
+        c[k] = hist[tid * BPT + k];
+        sum += c[k];
+        mx = c[k] > mx ? c[k] : mx;
+      }
+      uint32_t tot;
+      uint32_t ex = block_excl_scan(S, sum, tot);
+      if (mx > (uint32_t)(CAP - CHUNK)) atomicAnd(&S.splittable, 0u);
+      // non-empty bin i belongs to chunk floor(ex_i / CHUNK), ex_i the
+      // sheets in earlier bins; a chunk starts at its first bin.  With no
+      // bin above CHUNK, consecutive non-empty bins differ by at most one
+      // chunk, and a chunk holds fewer than 2 CHUNK = CAP sheets.
+#pragma unroll
+      for (int k = 0; k < BPT; ++k) {
+        if (c[k]) {
+          const uint32_t chunk = ex / CHUNK;
+          if (chunk < (uint32_t)kMaxChunks) atomicMin(&S.chunk_lo[chunk], tid * BPT + k);
+          atomicMax(&S.nchunks, (int)chunk + 1);
+        }
+        ex += c[k];
+      }
+    }
+    __syncthreads();
+    const int nchunks = S.nchunks;
+    if (!S.splittable || nchunks > kMaxChunks) {
+      // keys crowded into one bin: the host re-sorts the layout read here
+      if (tid == 0) {
+        atomicCAS(D.ocount + 2, 0u, (unsigned)(sub + 1));
+        atomicCAS(D.ocount + 1, 0u, (unsigned)(sub + 1));
+      }
+      continue;
+    }
+    if (tid == 0) {
+      S.chunk_lo[0] = 0;  // bins below the first non-empty one are empty
+      S.chunk_lo[nchunks] = BIGBINS;
+    }
+    __syncthreads();
+    // ---- the chunks in key order
+    for (int ch = 0; ch < nchunks; ++ch) {
+      const int blo = S.chunk_lo[ch], bhi = S.chunk_lo[ch + 1];
+      for (int j = tid; j < NBIN_PAD; j += BT) S.u.srt.bins[j] = 0u;
+      for (int j = tid; j <= S.win_hi - S.win_lo; j += BT) S.dcount[j] = 0;
+      if (tid == 0) S.load_cnt = 0;
+      __syncthreads();
+      uint64_t cmin = ~0ull, cmax = 0;
+      for (int j = tid; j < n; j += BT) {
+        const double x = big_pos(gx, gv, j, pre);
+        const uint64_t k = key_of(x);
+        const int bin = big_bin(k, kmin, span, scale);
+        if (bin >= blo && bin < bhi) {
+          const unsigned slot = atomicAdd(&S.load_cnt, 1u);
+          if (slot < (unsigned)CAP) {
+            S.x[slot] = x;
+            S.v[slot] = gv[j];
+            S.m[slot] = gm[j];
+            S.idx[slot] = gi[j];
+            cmin = k < cmin ? k : cmin;
+            cmax = k > cmax ? k : cmax;
+          }
+        }
+      }
+      block_range(S, cmin, cmax);
+      const int nc = (int)S.load_cnt;
+      if (nc > CAP) {  // cannot happen with the chunk rule; never write past the arrays
+        if (tid == 0) atomicOr(L.err, DEV_ERR_BAD_STATE);
+        break;
+      }
+      if (nc == 0) continue;
+      process_bucket<LAST, EXPR, false>(L, S, D, bt.bucket, bt.lay, nc, sub, ep, cmin, cmax,
+                                        BucketTask{0, 0});
+    }
   }
 }
 
 // Compact sorted state -> bucket layout with exactly T sheets per bucket,
 // the splitters Q_b = (key, idx) of the sheet at rank b*T, and the buckets'
 // aggregates in slot 0 (slots 1 and 2 cleared).  One block per bucket.
-__global__ void k_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int E,
+__global__ void k_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int capg,
+                            int E,
                             double* x, double* v, double* m, int32_t* idx, unsigned* cnt0,
                             unsigned* cnt1, unsigned* cnt2, unsigned long long* mass0,
                             unsigned long long* mass1, unsigned long long* mass2, uint64_t* qk,
@@ -1055,7 +1313,7 @@ __global__ void k_bucketize(const StateTable* table, int64_t n, int target, int6
     const int c = (int)((n - r0) < target ? (n - r0) : target);
     u128 msum = 0;
     for (int j = threadIdx.x; j < c; j += blockDim.x) {
-      const int64_t o = b * CAP + j;
+      const int64_t o = b * capg + j;
       const double mj = st.m[r0 + j];
       x[o] = st.x[r0 + j];
       v[o] = st.v[r0 + j];
@@ -1094,17 +1352,17 @@ __global__ void k_bucketize(const StateTable* table, int64_t n, int target, int6
 }
 
 // Bucket layout (+ overflow list) -> compact arrays in table->cur, unsorted.
-__global__ void k_compact(StateTable* table, int64_t nb, const double* x, const double* v,
+__global__ void k_compact(StateTable* table, int64_t nb, int capg, const double* x, const double* v,
                           const double* m, const int32_t* idx, const unsigned* cnt,
                           const unsigned* offs, const double* ox, const double* ov,
                           const double* om, const int32_t* oi, const unsigned* ocount,
                           int64_t n) {
   const StateRef st = table->cur;
   for (int64_t b = blockIdx.x; b < nb; b += gridDim.x) {
-    const unsigned c = cnt[b] < (unsigned)CAP ? cnt[b] : (unsigned)CAP;
+    const unsigned c = cnt[b] < (unsigned)capg ? cnt[b] : (unsigned)capg;
     const int64_t o = offs[b];
     for (unsigned j = threadIdx.x; j < c && o + j < n; j += blockDim.x) {
-      const int64_t s = b * CAP + j;
+      const int64_t s = b * capg + j;
       st.x[o + j] = x[s];
       st.v[o + j] = v[s];
       st.m[o + j] = m[s];
@@ -1123,7 +1381,7 @@ __global__ void k_compact(StateTable* table, int64_t nb, const double* x, const 
 }
 
 // Exclusive scan of the clamped bucket counts (single block, any nb).
-__global__ void k_count_offsets(const unsigned* cnt, int64_t nb, unsigned* offs) {
+__global__ void k_count_offsets(const unsigned* cnt, int64_t nb, int capg, unsigned* offs) {
   __shared__ unsigned s_carry;
   __shared__ unsigned s_w[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1131,7 +1389,7 @@ __global__ void k_count_offsets(const unsigned* cnt, int64_t nb, unsigned* offs)
   __syncthreads();
   for (int64_t base = 0; base < nb; base += blockDim.x) {
     const int64_t b = base + tid;
-    const unsigned c = b < nb ? (cnt[b] < (unsigned)CAP ? cnt[b] : (unsigned)CAP) : 0u;
+    const unsigned c = b < nb ? (cnt[b] < (unsigned)capg ? cnt[b] : (unsigned)capg) : 0u;
     unsigned incl = c;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -1181,6 +1439,14 @@ void bucket_attr_init() {
   cudaFuncSetAttribute(k_bucket_step<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(StepSmem));
   cudaFuncSetAttribute(k_bucket_step<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(StepSmem));
+  cudaFuncSetAttribute(k_bucket_big<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(StepSmem));
+  cudaFuncSetAttribute(k_bucket_big<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(StepSmem));
+  cudaFuncSetAttribute(k_bucket_big<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(StepSmem));
+  cudaFuncSetAttribute(k_bucket_big<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(StepSmem));
 }
 
@@ -1232,25 +1498,41 @@ void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s) {
   }
 }
 
-void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int E,
+void launch_bucket_big(const StepLaunch& a, int grid, cudaStream_t s) {
+  bucket_step_prepare();
+  if (grid < 1) grid = 1;
+  const bool last = a.sub == a.nleap - 1;
+  if (a.any_expr) {
+    if (last)
+      k_bucket_big<true, true><<<grid, BT, sizeof(StepSmem), s>>>(a);
+    else
+      k_bucket_big<false, true><<<grid, BT, sizeof(StepSmem), s>>>(a);
+  } else if (last) {
+    k_bucket_big<true, false><<<grid, BT, sizeof(StepSmem), s>>>(a);
+  } else {
+    k_bucket_big<false, false><<<grid, BT, sizeof(StepSmem), s>>>(a);
+  }
+}
+
+void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int capg, int E,
                       double* x, double* v, double* m, int32_t* idx,
                       unsigned* const cnt[kAggSlots], unsigned long long* const mass[kAggSlots],
                       uint64_t* qk, int32_t* qi, cudaStream_t s) {
   int64_t g = nb < 152 * 8 ? nb : 152 * 8;
   if (g < 1) g = 1;
-  k_bucketize<<<(unsigned)g, 256, 0, s>>>(table, n, target, nb, E, x, v, m, idx, cnt[0], cnt[1],
-                                           cnt[2], mass[0], mass[1], mass[2], qk, qi);
+  k_bucketize<<<(unsigned)g, 256, 0, s>>>(table, n, target, nb, capg, E, x, v, m, idx, cnt[0],
+                                           cnt[1], cnt[2], mass[0], mass[1], mass[2], qk, qi);
 }
 
-void launch_compact(StateTable* table, int64_t nb, const double* x, const double* v,
+void launch_compact(StateTable* table, int64_t nb, int capg, const double* x, const double* v,
                     const double* m, const int32_t* idx, const unsigned* cnt, unsigned* offs,
                     const double* ox, const double* ov, const double* om, const int32_t* oi,
                     const unsigned* ocount, int64_t n, cudaStream_t s) {
-  k_count_offsets<<<1, 1024, 0, s>>>(cnt, nb, offs);
+  k_count_offsets<<<1, 1024, 0, s>>>(cnt, nb, capg, offs);
   int64_t g = nb < 152 * 8 ? nb : 152 * 8;
   if (g < 1) g = 1;
-  k_compact<<<(unsigned)g, 256, 0, s>>>(table, nb, x, v, m, idx, cnt, offs, ox, ov, om, oi,
-                                         ocount, n);
+  k_compact<<<(unsigned)g, 256, 0, s>>>(table, nb, capg, x, v, m, idx, cnt, offs, ox, ov, om,
+                                         oi, ocount, n);
 }
 
 }  // namespace wg

@@ -13,7 +13,9 @@
 namespace wg {
 
 constexpr int kBucketThreads = 256;
-constexpr int kBucketCap = 2048;      // sheets a bucket can hold
+constexpr int kBucketCap = 2048;      // sheets a bucket's shared-memory pass can hold
+constexpr int kBucketCapBig = 4 * kBucketCap;  // sheets a bucket of a single simulation
+                                               // can hold (taken in chunks above kBucketCap)
 constexpr int kSplitterWindow = 64;   // largest splitter window (buckets on each side)
 constexpr int kSortBitsMin = 9;       // smallest counting-sort offset (bits)
 constexpr int kSortBitsMax = 13;      // largest counting-sort offset (bits)
@@ -89,7 +91,9 @@ struct SimDev {
   double* ov;
   double* om;
   int32_t* oi;
-  unsigned* ocount;      // [0] sheets in the overflow list, [1] 1 + sub-step that overflowed
+  unsigned* ocount;      // [0] sheets in the overflow list, [1] 1 + sub-step that overflowed,
+                         // [2] 1 + sub-step that could not take a big bucket (its input
+                         // layout is intact and is re-sorted by the host)
   double* x_out;         // output of the call's last sub-step, original order
   double* v_out;
   SheetRec* xi_out;      // optional: (idx, x) in the last sub-step's sorted order
@@ -103,7 +107,7 @@ struct SimDev {
   int target;            // sheets per bucket at a re-sort (splitters at ranks j * target)
   int window;            // splitter window half-width (<= kSplitterWindow)
   int sort_bits;         // counting-sort offset bits (9..13)
-  int pad0;
+  int capg;              // slots per bucket in the layouts (kBucketCap .. kBucketCapBig)
   uint64_t T_lo, T_hi;   // totmass in fixed point
   int E;
   int has_omega;
@@ -122,6 +126,22 @@ struct BucketTask {
   int bucket;
 };
 
+// A bucket with more sheets than shared memory holds (kBucketCap < n <=
+// capg), listed by k_bucket_step for k_bucket_big with what its preparation
+// found: its exclusive (mass, count) prefix, splitter window and force
+// factors.
+struct BigTask {
+  int sim;
+  int bucket;
+  int n;
+  int lay;
+  int wlo, whi;
+  uint32_t pcnt;
+  uint32_t pad;
+  uint64_t pm_lo, pm_hi;
+  double amp, inv_h;
+};
+
 struct StepLaunch {
   const SimDev* sims;
   const BucketTask* tasks;
@@ -133,9 +153,17 @@ struct StepLaunch {
   unsigned* err;
   int profile;           // 1: dt = 0 and no outputs (timing harness)
   int any_expr;          // some simulation of the launch has an expression force
+  // big buckets of this sub-step (simulations with capg > kBucketCap only):
+  // the list k_bucket_step fills and k_bucket_big takes in ticket order
+  BigTask* big_list;
+  unsigned* big_count;   // zero before the launch
+  unsigned* big_ticket;  // zero before the launch
+  unsigned big_cap;      // entries of big_list
 };
 
 void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s);
+// The big buckets k_bucket_step listed (launch right after it, same arguments).
+void launch_bucket_big(const StepLaunch& a, int grid, cudaStream_t s);
 // x_out, v_out (and a_out when not null) from the records of rec_out.
 void launch_split_out(const OutRec* rec, int64_t n, double* x_out, double* v_out, double* a_out,
                       cudaStream_t s);
@@ -144,11 +172,11 @@ void bucket_step_prepare();
 int bucket_step_grid(int sm_count);
 // Compact sorted state -> layout 0 with `target` sheets per bucket; fills
 // aggregate slot 0 and clears the other two.
-void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int E,
+void launch_bucketize(const StateTable* table, int64_t n, int target, int64_t nb, int capg, int E,
                       double* x, double* v, double* m, int32_t* idx,
                       unsigned* const cnt[kAggSlots], unsigned long long* const mass[kAggSlots],
                       uint64_t* qk, int32_t* qi, cudaStream_t s);
-void launch_compact(StateTable* table, int64_t nb, const double* x, const double* v,
+void launch_compact(StateTable* table, int64_t nb, int capg, const double* x, const double* v,
                     const double* m, const int32_t* idx, const unsigned* cnt, unsigned* offs,
                     const double* ox, const double* ov, const double* om, const int32_t* oi,
                     const unsigned* ocount, int64_t n, cudaStream_t s);

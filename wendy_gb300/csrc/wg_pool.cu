@@ -316,7 +316,8 @@ int to_buckets(wg_pool* p, PoolSim* s, double dt) {
   k_set_table<<<1, 1, 0, p->stream>>>(p->table, own, p->set[1]);
   launch_drift(p->table, s->n, dt / 2., &p->wflags[0], p->stream);  // also marks "unsorted"
   radix_sort_state(p->table, s->n, &p->radix, &p->wflags[0], p->err, p->stream);
-  launch_bucketize(p->table, s->n, s->tune.target, s->nb, s->E, s->bx[0], s->bv[0], s->bm[0],
+  launch_bucketize(p->table, s->n, s->tune.target, s->nb, kBucketCap, s->E, s->bx[0], s->bv[0],
+                   s->bm[0],
                    s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], p->stream);
   p->launches += 3 + kRadixLaunches;
   s->lay = 0;
@@ -331,7 +332,8 @@ int to_buckets(wg_pool* p, PoolSim* s, double dt) {
 // overflow entries counted in oc) -> the workspace's first set, unsorted.
 void buckets_to_workspace(wg_pool* p, PoolSim* s, int lay, int cslot, const unsigned* oc) {
   k_set_table<<<1, 1, 0, p->stream>>>(p->table, p->set[0], p->set[1]);
-  launch_compact(p->table, s->nb, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay], s->bcnt[cslot],
+  launch_compact(p->table, s->nb, kBucketCap, s->bx[lay], s->bv[lay], s->bm[lay], s->bi[lay],
+                 s->bcnt[cslot],
                  p->offs, s->ox, s->ov, s->om, s->oi, oc, s->n, p->stream);
   p->launches += 3;
 }
@@ -597,6 +599,7 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
     d.target = s->tune.target;
     d.window = s->tune.window;
     d.sort_bits = s->tune.sort_bits;
+    d.capg = kBucketCap;  // members have no big buckets
     d.T_lo = s->T_lo;
     d.T_hi = s->T_hi;
     d.E = s->E;
@@ -651,6 +654,10 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
       L.err = p->err;
       L.profile = 0;
       L.any_expr = launch_expr;
+      L.big_list = nullptr;
+      L.big_count = nullptr;
+      L.big_ticket = nullptr;
+      L.big_cap = 0;
       launch_bucket_step(L, grid, p->stream);
     }
     cudaMemcpyAsync(p->h_oc, p->ocount, 8 * (size_t)count, cudaMemcpyDeviceToHost, p->stream);
@@ -762,7 +769,7 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
       restarted_at = from;
       PC(cudaMemsetAsync(&p->wflags[from].unsorted, 1, sizeof(unsigned), p->stream));
       radix_sort_state(p->table, s->n, &p->radix, &p->wflags[from], p->err, p->stream);
-      launch_bucketize(p->table, s->n, s->tune.target, s->nb, s->E, s->bx[0], s->bv[0],
+      launch_bucketize(p->table, s->n, s->tune.target, s->nb, kBucketCap, s->E, s->bx[0], s->bv[0],
                        s->bm[0], s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], p->stream);
       // sub-step `from` reads layout 0, aggregate slot 0 and routes by splitter set 0
       l0 = from & 1;
@@ -789,6 +796,10 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
         L.err = p->err;
         L.profile = 0;
         L.any_expr = s->ext.kind == EXT_EXPR;
+        L.big_list = nullptr;
+        L.big_count = nullptr;
+        L.big_ticket = nullptr;
+        L.big_cap = 0;
         launch_bucket_step(L, s->tune.ctas_per_sm * p->sms, p->stream);
       }
       p->launches += 3 + kRadixLaunches + (nleap - from);
