@@ -14,7 +14,7 @@ namespace wg {
 
 constexpr int kBucketThreads = 256;
 constexpr int kBucketCap = 2048;      // sheets a bucket's shared-memory pass can hold
-constexpr int kBucketCapBig = 4 * kBucketCap;  // sheets a bucket of a single simulation
+constexpr int kBucketCapBig = 3 * kBucketCap;  // sheets a bucket of a single simulation
                                                // can hold (taken in chunks above kBucketCap)
 constexpr int kSplitterWindow = 64;   // largest splitter window (buckets on each side)
 constexpr int kSortBitsMin = 9;       // smallest counting-sort offset (bits)
