@@ -215,7 +215,8 @@ def run_serve(args, w):
         x, v, m = member_inputs(n, fams[k % 3], int(rng.integers(1 << 30)))
         reqs.append(dict(x=x, v=v, m=m, dt=float(rng.uniform(0.005, 0.05)), nleap=w["nleap"],
                          noutputs=nout, omega=[None, 0.5, 1.1][int(rng.integers(3))], arrival=t))
-    srv = Server(budget_bytes=int(w["budget"]))
+    budget = args.budget_gb * 1e9 if args.budget_gb else w["budget"]
+    srv = Server(budget_bytes=int(budget))
     with Clocks(0) as clk:
         served = srv.run([Request(**r) for r in reqs])
     rounds, waits, peak = srv.rounds, srv.budget_waits, srv.peak_bytes
@@ -230,7 +231,7 @@ def run_serve(args, w):
             "config": {"workload": args.workload, "requests": nreq, "rate_per_s": w["rate"],
                        "arrivals_s": reqs[-1]["arrival"],
                        "n_range": [w["nmin"], w["nmax"]], "steps_range": [w["smin"], w["smax"]],
-                       "budget_bytes": w["budget"], "rounds": rounds,
+                       "budget_bytes": budget, "rounds": rounds,
                        "rounds_with_a_request_waiting_for_memory": waits,
                        "peak_admitted_bytes": peak},
             "continuous_batching": a, "plain_one_at_a_time": b,
@@ -489,6 +490,8 @@ def main():
                     help="ensemble_4096: simulations of the plain one-at-a-time comparison")
     ap.add_argument("--requests", type=int, default=0,
                     help="serve_poisson: requests in the stream (default 1000)")
+    ap.add_argument("--budget-gb", type=float, default=0.0,
+                    help="serve_poisson: HBM budget in GB (default: the configuration's 150)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -596,16 +599,11 @@ def main():
             "stats": {k: st1[k] - st0[k] for k in ("sorts_full", "sorts_window", "substeps",
                                                    "substeps_compact")}}
 
-    # the same simulation on through all of the configuration's outputs: the
-    # whole run from t = 0, collapse and relaxation included
-    full = None
-    if not args.no_full_run and w.get("outputs"):
-        while len(per_output) < w["outputs"]:
-            one_output()
-        full = full_run_summary(w, per_output, world)
-    sim.close()
-
-    # end to end through the reference-shaped call, page-locked host buffers
+    # end to end through the reference-shaped call, page-locked host buffers.
+    # Timed before the long full run below: on the measured GB300 hosts the
+    # host-to-device copy rate falls from about 200 GB/s to under 20 GB/s
+    # after tens of seconds of sustained device-memory load (a plain torch
+    # device-to-device copy loop shows the same), and recovers only slowly.
     e2e = None
     if not args.no_e2e:
         from wendy_gb300 import _lib as LL
@@ -641,6 +639,16 @@ def main():
                           "wall clock); as in wendy's generator each call is handed the previous "
                           "call's outputs, which it verifies bit for bit on the device, so its "
                           "sub-steps, enqueued by the previous call, run under these transfers"}
+
+    # the same simulation on through all of the configuration's outputs: the
+    # whole run from t = 0, collapse and relaxation included
+    full = None
+    if not args.no_full_run and w.get("outputs"):
+        while len(per_output) < w["outputs"]:
+            one_output()
+        full = full_run_summary(w, per_output, world)
+
+    sim.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
