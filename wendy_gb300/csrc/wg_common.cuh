@@ -264,6 +264,7 @@ struct ExtForce {
   const ExprOp* prog;  // EXT_EXPR: the program, in device memory
   int n_ops;
   int n_time;
+  const long long* ttab;  // EXT_PULSE_TANH: the device's tanh table (wg_tanh.cuh)
 };
 
 // Runs ops [lo, hi) of an expression program on the registers r.
@@ -320,11 +321,11 @@ __device__ __forceinline__ double pulse_amplitude(const ExtForce& f, double t) {
 
 // F(x, t) given the per-evaluation amplitude `amp` and inv_h = 1 / h (pulse)
 // -- harmonic: -p0 x; pulse: amp * tanh(x / h), as amp * tanh(x * inv_h) with
-// the integer-pipe tanh (wg_tanh.cuh).
+// the table-driven integer-pipe tanh (wg_tanh.cuh).
 __device__ __forceinline__ double ext_force_at(const ExtForce& f, double amp, double inv_h,
                                                double x) {
   if (f.kind == EXT_HARMONIC) return -f.p[0] * x;
-  if (f.kind == EXT_PULSE_TANH) return amp * tanh_fixed(x * inv_h);
+  if (f.kind == EXT_PULSE_TANH) return amp * tanh_tab(f.ttab, x * inv_h);
   return 0.0;
 }
 

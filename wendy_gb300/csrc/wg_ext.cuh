@@ -64,6 +64,10 @@ inline int parse_ext(int kind, const double* p, int np, ExtSpec* spec, char* err
       std::snprintf(err, errlen, "pulsed force needs tau != 0 and h != 0");
       return WG_ERR_EXT;
     }
+    if (kind == WG_EXT_PULSE_TANH && !(f.ttab = tanh_table())) {
+      std::snprintf(err, errlen, "the pulsed force's tanh table could not be set up on the device");
+      return WG_ERR_CUDA;
+    }
     return WG_OK;
   }
   if (kind != WG_EXT_EXPR) {

@@ -90,6 +90,13 @@ inline int current_device() {
   return d;
 }
 
+// The tanh table of the pulsed force (wg_tanh.cuh) on the current device,
+// computed there by its first call (a kernel on the legacy stream, waited
+// for; no allocation: the table is a __device__ array of the library), or
+// nullptr when the device cannot be reached.  Call it before any stream
+// capture, as every entry point does when it parses a force.
+const long long* tanh_table();
+
 constexpr int kForceThreads = 256;
 constexpr int kForceItems = 8;
 constexpr int kForceTile = kForceThreads * kForceItems;

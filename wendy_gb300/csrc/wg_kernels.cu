@@ -13,6 +13,7 @@
 // what decides how the next sub-step re-sorts.
 #include <atomic>
 #include <cstdint>
+#include <mutex>
 
 #include "wg_internal.cuh"
 
@@ -373,6 +374,42 @@ __global__ void k_ext_eval(const ExtForce f, double t, const double* x, double* 
 void launch_ext_eval(const ExtForce& f, double t, const double* x, double* out, int64_t n,
                      cudaStream_t s) {
   k_ext_eval<<<grid_for(n, 256), 256, 0, s>>>(f, t, x, out, n);
+}
+
+// ---- the pulsed force's tanh table (wg_tanh.cuh): one per device, in a
+// __device__ array of the library, computed by its first use on the device
+namespace {
+__device__ __align__(256) long long g_tanh_tab[kTanhCells * kTanhRow];
+
+__global__ void k_tanh_table(long long* tab) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kTanhCells) tanh_table_row(i, tab + (size_t)kTanhRow * i);
+}
+
+std::once_flag g_tanh_once[kMaxDevices];
+const long long* g_tanh_ptr[kMaxDevices];
+
+const long long* tanh_table_setup() {
+  long long* p = nullptr;
+  if (cudaGetSymbolAddress((void**)&p, g_tanh_tab) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  k_tanh_table<<<(kTanhCells + 255) / 256, 256, 0, 0>>>(p);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(0) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+}  // namespace
+
+const long long* tanh_table() {
+  const int dev = current_device();
+  if (dev < 0) return nullptr;
+  if (dev >= kMaxDevices) return tanh_table_setup();
+  std::call_once(g_tanh_once[dev], [dev] { g_tanh_ptr[dev] = tanh_table_setup(); });
+  return g_tanh_ptr[dev];
 }
 
 // Sums of the energy and momentum diagnostics over the sorted state, with

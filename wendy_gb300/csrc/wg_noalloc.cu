@@ -172,7 +172,7 @@ extern "C" int wg_accel_noalloc(int64_t n, const double* x, const double* m, dou
   if (!x || !m || (!a && !perm)) return fail(WG_ERR_ARG, "wg_accel_noalloc: null buffer");
   if (!std::isfinite(totmass) || totmass < 0 || !std::isfinite(omega2))
     return fail(WG_ERR_ARG, "wg_accel_noalloc: totmass must be finite and >= 0");
-  ExtForce ext;
+  ExtForce ext{};
   ext.kind = ext_kind;
   for (int i = 0; i < 4; ++i) ext.p[i] = 0.0;
   const int need = ext_kind == WG_EXT_NONE ? 0 : ext_kind == WG_EXT_HARMONIC ? 1
@@ -186,6 +186,10 @@ extern "C" int wg_accel_noalloc(int64_t n, const double* x, const double* m, dou
   for (int i = 0; i < need; ++i) ext.p[i] = ext_params[i];
   if (ext_kind == WG_EXT_PULSE_TANH && (ext.p[2] == 0.0 || ext.p[3] == 0.0))
     return fail(WG_ERR_EXT, "wg_accel_noalloc: pulsed force needs tau != 0 and h != 0");
+  // the pulsed force's tanh table is a __device__ array of the library, set
+  // up on the device's first use (no allocation)
+  if (ext_kind == WG_EXT_PULSE_TANH && !(ext.ttab = tanh_table()))
+    return fail(WG_ERR_CUDA, "wg_accel_noalloc: the tanh table could not be set up");
 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {

@@ -23,6 +23,10 @@
 // The constants are round(2^62 2^(-j/256)), round(2^62 / n!), round(2^64 ln 2)
 // and round(2^61 2 log2(e)), computed with 60-digit decimal arithmetic; the
 // CPU tests recompute them the same way and compare.
+//
+// The force kernels do not call this per sheet: tanh_q62 fills, once per
+// device, a table of degree-5 Taylor polynomials on cells of width 2^-10
+// (tanh_tab, at the end of this file), which costs a fraction of it.
 #pragma once
 #include <cstdint>
 
@@ -115,16 +119,10 @@ __device__ __forceinline__ uint64_t mul62(uint64_t a, uint64_t b) {
 
 }  // namespace tanh_fx
 
-__device__ __forceinline__ double tanh_fixed(double y) {
+// tanh(|y|) 2^62 for 2^-27 <= |y| < 20, |y| given by its bits; the absolute
+// error is below 2^-57 (the bound stated above).
+__device__ __forceinline__ uint64_t tanh_q62(uint64_t abits) {
   using namespace tanh_fx;
-  const uint64_t bits = (uint64_t)__double_as_longlong(y);
-  const uint64_t sign = bits & 0x8000000000000000ull;
-  const uint64_t abits = bits ^ sign;
-  if (abits < 0x3e40000000000000ull) return y;  // |y| < 2^-27, +-0, subnormals
-  if (abits >= 0x4034000000000000ull) {          // |y| >= 20, +-inf, NaN
-    if (abits > 0x7ff0000000000000ull) return y;
-    return __longlong_as_double((long long)(sign | 0x3ff0000000000000ull));
-  }
   // |y| = m 2^(e - 52); t = 2 |y| log2(e) with 58 fractional bits (t < 58),
   // from the full 117-bit product m L and one truncation:
   // t 2^58 = m L 2^(e - 52 - 61 + 58) = (m L) >> (55 - e)
@@ -150,8 +148,11 @@ __device__ __forceinline__ double tanh_fixed(double y) {
   uint64_t R = __float2ull_rn(rf * 4.611686018427388e18f);                 // 2^62 / D
   R = mul62(R, (1ull << 63) - mul62(D, R));
   R = mul62(R, (1ull << 63) - mul62(D, R));
-  const uint64_t Tq = mul62(N, R);  // tanh(a) 2^62, in (2^35, 2^62)
-  // to double, rounding to nearest
+  return mul62(N, R);  // tanh(a) 2^62, in (2^35, 2^62)
+}
+
+// Tq 2^-62 (0 < Tq < 2^62) to double, rounded to nearest, with the sign bit given.
+__device__ __forceinline__ double q62_to_double(uint64_t Tq, uint64_t sign) {
   const int p = 63 - __clzll((long long)Tq);  // leading bit
   uint64_t mant;
   int be = p + 961;                            // biased exponent of 2^(p - 62)
@@ -167,6 +168,95 @@ __device__ __forceinline__ double tanh_fixed(double y) {
   }
   return __longlong_as_double(
       (long long)(sign | ((uint64_t)be << 52) | (mant & 0x000fffffffffffffull)));
+}
+
+__device__ __forceinline__ double tanh_fixed(double y) {
+  const uint64_t bits = (uint64_t)__double_as_longlong(y);
+  const uint64_t sign = bits & 0x8000000000000000ull;
+  const uint64_t abits = bits ^ sign;
+  if (abits < 0x3e40000000000000ull) return y;  // |y| < 2^-27, +-0, subnormals
+  if (abits >= 0x4034000000000000ull) {          // |y| >= 20, +-inf, NaN
+    if (abits > 0x7ff0000000000000ull) return y;
+    return __longlong_as_double((long long)(sign | 0x3ff0000000000000ull));
+  }
+  return q62_to_double(tanh_q62(abits), sign);
+}
+
+// ---------------------------------------------------------------------------
+// tanh from a table of Taylor polynomials.  The argument range [0, 20) is cut
+// into cells of width 2^-10; cell i holds, in 2^62 fixed point, t = tanh(a_i)
+// at a_i = i 2^-10 (from tanh_q62) and the Taylor coefficients about a_i,
+//
+//   tanh(a_i + D) = t + s D - t s D^2 + s (3t^2 - 1)/3 D^3
+//                   + t s (2 - 3t^2)/3 D^4 + s (2 - 15t^2 + 15t^4)/15 D^5 + O(D^6),
+//
+// s = 1 - t^2 (the derivatives follow from t' = s, s' = -2ts).  With
+// 0 <= D < 2^-10 the remainder is below 2^-64 (the Taylor coefficients of
+// tanh are below 1), s is formed in fixed point and the higher coefficients
+// in double (their rounding enters multiplied by D^2 <= 2^-20), and each
+// Horner step is one signed high product with D 2^64, so the absolute error
+// stays within that of tanh_q62 plus 2^-61.  The cell and D come from the
+// argument's bits (D is exact up to one truncation of 2^-64).  Per argument
+// this is some 35 integer instructions and three 16-byte loads, which hit
+// in L1 for the sorted positions of a bucket or tile, against about 150
+// instructions and two conversions on the FP64 pipe for tanh_fixed.  The
+// table (20480 cells, 960 KB) is computed once per device by
+// k_tanh_table; the result is a function of the argument alone, so every
+// kernel that evaluates the force gives the same bits.
+// ---------------------------------------------------------------------------
+constexpr int kTanhCellBits = 10;
+constexpr int kTanhCells = 20 << kTanhCellBits;
+constexpr int kTanhRow = 6;  // t, then the coefficients of D .. D^5
+
+// Row of cell i.
+__device__ __forceinline__ void tanh_table_row(int i, long long* row) {
+  const double a = (double)i * 0x1p-10;
+  const uint64_t tq = i == 0 ? 0ull : tanh_q62((uint64_t)__double_as_longlong(a));
+  const uint64_t s = (1ull << 62) - tanh_fx::mul62(tq, tq);
+  const double td = (double)tq * 0x1p-62, sd = (double)s * 0x1p-62;
+  const double t2 = td * td;
+  row[0] = (long long)tq;
+  row[1] = (long long)s;
+  row[2] = __double2ll_rn(-td * sd * 0x1p62);
+  row[3] = __double2ll_rn(sd * (3.0 * t2 - 1.0) / 3.0 * 0x1p62);
+  row[4] = __double2ll_rn(td * sd * (2.0 - 3.0 * t2) / 3.0 * 0x1p62);
+  row[5] = __double2ll_rn(sd * (2.0 - 15.0 * t2 + 15.0 * t2 * t2) / 15.0 * 0x1p62);
+}
+
+// tanh(y) with the table (16-byte aligned, kTanhCells rows).
+__device__ __forceinline__ double tanh_tab(const long long* __restrict__ tab, double y) {
+  const uint64_t bits = (uint64_t)__double_as_longlong(y);
+  const uint64_t sign = bits & 0x8000000000000000ull;
+  const uint64_t abits = bits ^ sign;
+  if (abits < 0x3e40000000000000ull) return y;  // |y| < 2^-27, +-0, subnormals
+  if (abits >= 0x4034000000000000ull) {          // |y| >= 20, +-inf, NaN
+    if (abits > 0x7ff0000000000000ull) return y;
+    return __longlong_as_double((long long)(sign | 0x3ff0000000000000ull));
+  }
+  const int e = (int)(abits >> 52) - 1023;  // -27 .. 4
+  const uint64_t m = (abits & 0x000fffffffffffffull) | 0x0010000000000000ull;
+  // |y| = m 2^(e - 52) = cell 2^-10 + D 2^-64
+  int cell;
+  uint64_t D;
+  if (e >= -10) {
+    const int sh = 42 - e;  // 38 .. 52
+    cell = (int)(m >> sh);
+    D = (m & ((1ull << sh) - 1)) << (e + 12);
+  } else {
+    cell = 0;
+    D = e >= -12 ? m << (e + 12) : m >> (-12 - e);
+  }
+  const longlong2* r = reinterpret_cast<const longlong2*>(tab + kTanhRow * cell);
+  const longlong2 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2);
+  const long long d = (long long)D;  // < 2^54
+  long long p = r2.y;
+  p = r2.x + __mul64hi(p, d);
+  p = r1.y + __mul64hi(p, d);
+  p = r1.x + __mul64hi(p, d);
+  p = r0.y + __mul64hi(p, d);
+  const long long T = r0.x + __mul64hi(p, d);  // tanh(|y|) 2^62, in (2^35, 2^62)
+  const uint64_t Tq = T >= (1ll << 62) ? (1ull << 62) - 1 : (uint64_t)T;
+  return q62_to_double(Tq, sign);
 }
 
 }  // namespace wg
