@@ -245,6 +245,9 @@ HBM_FALLBACK_GBS = 6800.0
 TRAFFIC_PER_SHEET = {
     "sech2": ((237.496576e6 + 185.93152e6) / (1 << 23),
               "ncu capture of one sub-step of the sech2 disk at N = 2^23"),
+    "tophat": ((237.603328e6 + 187.855872e6) / (1 << 23),
+               "ncu capture of one sub-step of the cold top-hat with the pulsed force at "
+               "N = 2^23"),
 }
 
 

@@ -959,6 +959,32 @@ __device__ __forceinline__ void process_bucket(const StepLaunch& L, StepSmem& S,
   }
 }
 
+// Appends a big bucket's task to the list k_bucket_big works through (one
+// thread).  Kept out of line: inlined, its fields stayed live across the
+// bucket loop and pushed the kernel into register spills.
+static __device__ __noinline__ void list_big(const TaskMeta* tm, unsigned* big_count,
+                                             unsigned big_cap, BigTask* big_list,
+                                             unsigned* err) {
+  const unsigned slot = atomicAdd(big_count, 1u);
+  if (slot >= big_cap) {
+    atomicOr(err, DEV_ERR_BAD_STATE);
+    return;
+  }
+  BigTask bt;
+  bt.sim = tm->sim;
+  bt.bucket = (int)tm->bucket;
+  bt.n = tm->n;
+  bt.lay = tm->lay;
+  bt.wlo = tm->wlo;
+  bt.whi = tm->whi;
+  bt.pcnt = tm->pcnt;
+  bt.pm_lo = tm->pm_lo;
+  bt.pm_hi = tm->pm_hi;
+  bt.amp = tm->amp;
+  bt.inv_h = tm->inv_h;
+  big_list[slot] = bt;
+}
+
 // The fused sub-step.  LAST: the call's last sub-step (half drift, outputs).
 // EXPR: the launch has simulations with expression forces (the interpreter
 // is compiled only into this instantiation).
@@ -979,35 +1005,12 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
     __syncthreads();
     const TaskMeta tm = S.next;  // claimed during the previous task
     if (tm.task >= (unsigned)L.ntasks) break;
-    if (tm.n < 0) {
-      __syncthreads();  // every thread has read S.next
-      if (warp == 0) claim_task(L, sub, ep, lane, S, tm.wbuf);
-      continue;
-    }
-    if (tm.n > CAP) {
-      // more sheets than shared memory holds (a simulation whose layout has
-      // room for them): listed for k_bucket_big, which runs next on the
-      // stream and takes the bucket in chunks.  Its prefix is known already.
-      if (tid == 0) {
-        const unsigned slot = atomicAdd(L.big_count, 1u);
-        if (slot < L.big_cap) {
-          BigTask bt;
-          bt.sim = tm.sim;
-          bt.bucket = (int)tm.bucket;
-          bt.n = tm.n;
-          bt.lay = tm.lay;
-          bt.wlo = tm.wlo;
-          bt.whi = tm.whi;
-          bt.pcnt = tm.pcnt;
-          bt.pm_lo = tm.pm_lo;
-          bt.pm_hi = tm.pm_hi;
-          bt.amp = tm.amp;
-          bt.inv_h = tm.inv_h;
-          L.big_list[slot] = bt;
-        } else {
-          atomicOr(L.err, DEV_ERR_BAD_STATE);
-        }
-      }
+    if (tm.n < 0 || tm.n > CAP) {
+      // n < 0: the simulation has aborted this call.  n > CAP: more sheets
+      // than shared memory holds (a simulation whose layout has room for
+      // them): listed for k_bucket_big, which runs next on the stream and
+      // takes the bucket in chunks; its prefix is known already.
+      if (tm.n > CAP && tid == 0) list_big(&S.next, L.big_count, L.big_cap, L.big_list, L.err);
       __syncthreads();  // every thread has read S.next
       if (warp == 0) claim_task(L, sub, ep, lane, S, tm.wbuf);
       continue;
@@ -1052,30 +1055,23 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       // counting-sort bins, cleared while the copies are in flight
       for (int j = tid; j < NBIN_PAD; j += BT) S.u.srt.bins[j] = 0u;
     }
-    if (n4 > 0) {
-      const bool arrived = mbar_wait(&S.mbar, parity);
-      if (__syncthreads_or(!arrived)) {
-        // the bucket's copies did not complete within the bounded wait: its
-        // contents are unknown, so this CTA writes nothing more.  It gives the
-        // copies a second bounded wait and stops; the host sees the error word
-        // (the call fails and the simulation is given up).
-        if (tid == 0) atomicOr(L.err, DEV_ERR_COPY_TIMEOUT);
-        mbar_wait(&S.mbar, parity);
-        break;
-      }
-      parity ^= 1u;
-    }
+    // the copies' completion: a thread that did not see it within the bounded
+    // wait leaves the data alone, and the barrier after the key range below
+    // (which every thread reaches) decides for the whole CTA
+    const bool arrived = n4 > 0 ? mbar_wait(&S.mbar, parity) : true;
     uint64_t kmin = ~0ull, kmax = 0;
+    if (arrived) {
 #pragma unroll 4
-    for (int j = tid; j < n; j += BT) {
-      double x = S.x[j];
-      if (pre != 0.0) {
-        x = fma(pre, S.v[j], x);
-        S.x[j] = x;
+      for (int j = tid; j < n; j += BT) {
+        double x = S.x[j];
+        if (pre != 0.0) {
+          x = fma(pre, S.v[j], x);
+          S.x[j] = x;
+        }
+        const uint64_t k = key_of(x);
+        kmin = k < kmin ? k : kmin;
+        kmax = k > kmax ? k : kmax;
       }
-      const uint64_t k = key_of(x);
-      kmin = k < kmin ? k : kmin;
-      kmax = k > kmax ? k : kmax;
     }
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) {
@@ -1088,7 +1084,16 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       S.red_min[warp] = kmin;
       S.red_max[warp] = kmax;
     }
-    __syncthreads();
+    if (__syncthreads_or(!arrived)) {
+      // the bucket's copies did not complete within the bounded wait: its
+      // contents are unknown, so this CTA writes nothing more.  It gives the
+      // copies a second bounded wait and stops; the host sees the error word
+      // (the call fails and the simulation is given up).
+      if (tid == 0) atomicOr(L.err, DEV_ERR_COPY_TIMEOUT);
+      mbar_wait(&S.mbar, parity);
+      break;
+    }
+    if (n4 > 0) parity ^= 1u;
     BucketTask ntk{0, 0};
     if (tid == 0) {
       S.next_ticket = nt;
