@@ -446,7 +446,7 @@ def full_run_summary(w, per_output, world):
     nout = len(per_output)
     last = per_output[-1][2]
     phases = []
-    prev = {"substeps_compact": 0, "sorts_full": 0}
+    prev = {"substeps_compact": 0, "sorts_full": 0, "substeps_predicted": 0}
     for lo in range(0, nout, 100):
         rows = per_output[lo:lo + 100]
         st = rows[-1][2]
@@ -456,6 +456,7 @@ def full_run_summary(w, per_output, world):
                        "ms_per_substep": d / (len(rows) * nleap) * 1e3,
                        "particle_steps_per_s": n * nleap * len(rows) / d,
                        "substeps_compact": st["substeps_compact"] - prev["substeps_compact"],
+                       "substeps_predicted": st["substeps_predicted"] - prev["substeps_predicted"],
                        "resorts": st["sorts_full"] - prev["sorts_full"],
                        "largest_bucket_count": max(r[2]["last_max_count"] for r in rows)})
         prev = st
@@ -464,6 +465,7 @@ def full_run_summary(w, per_output, world):
            "device_s": dev, "wall_s": wall, "wall_value": world * n * nleap * nout / wall,
            "substeps_bucket": nout * nleap - last["substeps_compact"],
            "substeps_compact": last["substeps_compact"], "sorts_full": last["sorts_full"],
+           "substeps_predicted": last["substeps_predicted"],
            "phases": phases}
     if w["family"] == "tophat":
         # inside the uniform slab a = -x (total mass 1): it collapses at t = pi/2

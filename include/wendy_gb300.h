@@ -79,6 +79,7 @@ typedef struct wg_stats {
   int64_t last_max_count;    /* most sheets any bucket received during the last call */
   int64_t substeps_compact;  /* sub-steps run on the compact path (full re-sort + force) */
   int64_t big_buckets;       /* buckets taken in chunks (more sheets than one pass holds) */
+  int64_t substeps_predicted; /* bucket sub-steps whose splitters were predicted from velocities */
 } wg_stats;
 
 /* Library and device information. */

@@ -61,20 +61,24 @@ def test_full_run_summary_counts_paths_and_phases():
     import bench
     w = dict(bench.WORKLOADS["tophat_2p27"], n=1000)
     rows = []
-    compact = sorts = 0
+    compact = sorts = pred = 0
     for k in range(500):
-        # the compact path from the collapse (output 158) to output 300
+        # the compact path from the collapse (output 158) to output 300,
+        # predicted splitters on the bucket path from output 300 to 316
         step_c = 10 if 158 <= k < 300 else 0
         compact += step_c
         sorts += step_c + (1 if k == 0 else 0)
+        pred += 10 if 300 <= k < 316 else 0
         rows.append((0.02 if step_c else 0.01, 0.011,
                      {"substeps_compact": compact, "sorts_full": sorts,
+                      "substeps_predicted": pred,
                       "last_max_count": 0 if step_c else 1800}))
     s = bench.full_run_summary(w, rows, 1)
     assert s["outputs"] == 500 and s["substeps"] == 5000
     assert s["substeps_compact"] == 1420 and s["substeps_bucket"] == 3580
     assert len(s["phases"]) == 5 and s["phases"][0]["substeps_compact"] == 0
     assert s["phases"][1]["substeps_compact"] == 420
+    assert s["phases"][3]["substeps_predicted"] == 160 and s["substeps_predicted"] == 160
     assert abs(s["value"] - 1000 * 5000 / (0.01 * 358 + 0.02 * 142)) < 1e-6 * s["value"]
     pc = s["post_collapse"]
     assert pc["from_output"] == 158 and pc["substeps_compact"] == 1420

@@ -44,7 +44,7 @@ def test_a_block_moving_into_a_region_doubles_its_buckets():
     x = rng.uniform(-1, 1, n)
     v = numpy.where((x > 0.5) & (x < 0.6), -50.0, 0.0)
     m = numpy.full(n, 1.0 / n)
-    st = _compare(x, v, m, 0.001, 4, 2)
+    st = _compare(x, v, m, 0.001, 4, 1)
     assert st["big_buckets"] > 0
     assert st["sorts_full"] == 1  # the first sort only: no bucket overflowed
 
@@ -62,3 +62,18 @@ def test_a_dense_cluster_is_sent_back_and_recovered():
     m = numpy.full(n, 1.0 / n)
     st = _compare(x, v, m, 0.001, 4, 2)
     assert st["sorts_full"] > 1
+
+
+def test_predicted_splitters_follow_the_block():
+    # the first output meets buckets above one shared-memory pass, so the
+    # next outputs take their splitters from the sheets' positions moved on
+    # by two drifts at their bucket's mean velocity (sorted after every
+    # sub-step); any sorted splitters give the same trajectory
+    n = 1 << 20
+    rng = numpy.random.default_rng(5)
+    x = rng.uniform(-1, 1, n)
+    v = numpy.where((x > 0.5) & (x < 0.6), -50.0, 0.0)
+    m = rng.lognormal(0.0, 0.5, n)
+    m /= m.sum()
+    st = _compare(x, v, m, 0.001, 4, 4)
+    assert st["substeps_predicted"] > 0

@@ -52,7 +52,7 @@ class WgStats(ctypes.Structure):
                 ("sorts_window", ctypes.c_int64), ("last_max_disp", ctypes.c_double),
                 ("device_bytes", ctypes.c_int64), ("launches", ctypes.c_int64),
                 ("last_max_count", ctypes.c_int64), ("substeps_compact", ctypes.c_int64),
-                ("big_buckets", ctypes.c_int64)]
+                ("big_buckets", ctypes.c_int64), ("substeps_predicted", ctypes.c_int64)]
 
 
 class WgTuning(ctypes.Structure):

@@ -50,6 +50,7 @@ size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 // Most calls a violent overflow sends to the compact path before the bucket
 // path is tried again.
 constexpr int kMaxBackoff = 8;
+constexpr int kPredCalls = 16;
 
 // The bits of a device error word, by name.
 std::string device_error_names(unsigned err) {
@@ -193,6 +194,20 @@ struct wg_sim {
   // penalty; the penalty halves after every call the bucket path completes.
   int compact_calls = 0;
   int backoff = 1;
+  // Predicted splitters (single simulations with at least 3 buckets): a
+  // sample per bucket, its position moved on by two drifts at its bucket's
+  // mean velocity, sorted after every sub-step (a radix sort of nb - 1
+  // entries) and taken as the splitters of the layout after next.  Turned on
+  // for kPredCalls calls whenever a call sees a bucket receive more sheets
+  // than one shared-memory pass sorts (flows that outrun the exact quantiles
+  // of two sub-steps back: a collapsing cold slab); off otherwise, where the
+  // exact quantiles already balance the buckets and the sort would be pure
+  // cost.
+  int pred_calls = 0;
+  void* pmem = nullptr;
+  StateTable* ptab = nullptr;   // device table of the two sample sets
+  StepFlags* pflag = nullptr;   // device flags with `unsorted` set: the sort always runs
+  RadixWork pradix{};
   double pending_dt = 0; // dt of the half drift the bucket layout was routed for
   bool out_valid = false;  // x_out / v_out hold the last call's output
   // Split steps (wg_step_begin): a second pair of output buffers, so that the
@@ -292,6 +307,7 @@ void free_sim(wg_sim* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->big) cudaFree(s->big);
   if (s->bk) cudaFree(s->bk);
+  if (s->pmem) cudaFree(s->pmem);
   if (s->small) cudaFree(s->small);
   if (s->stage) cudaFree(s->stage);
   if (s->h_t) cudaFreeHost(s->h_t);
@@ -456,6 +472,44 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtSpec& ext, wg_si
       return fail(WG_ERR_CUDA);
     }
   }
+  if (big_buckets && nb >= 3) {
+    // predicted splitters: two sample sets of nb - 1 entries (SoA as the
+    // radix sort wants them), their table, the sort's workspace and flags
+    const int64_t m = nb - 1;
+    const size_t nd = al(8 * (size_t)m), ni = al(4 * (size_t)m);
+    const size_t pb = 2 * (3 * nd + ni) + al(sizeof(StateTable)) + al(sizeof(StepFlags)) +
+                      radix_bytes(m);
+    if (cudaMalloc(&s->pmem, pb) == cudaSuccess) {
+      char* q = static_cast<char*>(s->pmem);
+      StateRef set[2];
+      for (int k = 0; k < 2; ++k) {
+        set[k].x = reinterpret_cast<double*>(q); q += nd;
+        set[k].v = reinterpret_cast<double*>(q); q += nd;
+        set[k].m = reinterpret_cast<double*>(q); q += nd;
+        set[k].idx = reinterpret_cast<int32_t*>(q); q += ni;
+      }
+      s->ptab = reinterpret_cast<StateTable*>(q); q += al(sizeof(StateTable));
+      s->pflag = reinterpret_cast<StepFlags*>(q); q += al(sizeof(StepFlags));
+      radix_bind(&s->pradix, q, m);
+      StateTable t;
+      t.cur = set[0];
+      t.other = set[1];
+      StepFlags f{};
+      f.unsorted = 1u;
+      if (cudaMemsetAsync(s->pmem, 0, 2 * (3 * nd + ni), s->stream) != cudaSuccess ||
+          cudaMemcpyAsync(s->ptab, &t, sizeof(t), cudaMemcpyHostToDevice, s->stream) !=
+              cudaSuccess ||
+          cudaMemcpyAsync(s->pflag, &f, sizeof(f), cudaMemcpyHostToDevice, s->stream) !=
+              cudaSuccess) {
+        set_error("set-up of the predicted splitters failed");
+        return fail(WG_ERR_CUDA);
+      }
+      s->st.device_bytes += (int64_t)pb;
+    } else {
+      cudaGetLastError();  // no room: the exact quantiles only
+      s->pmem = nullptr;
+    }
+  }
   if (cudaMemsetAsync(s->brecs, 0, sizeof(BucketRec) * (size_t)nb, s->stream) != cudaSuccess ||
       cudaMemsetAsync(s->bcnt[0], 0,
                       static_cast<char*>(static_cast<void*>(s->bmass[kAggSlots - 1])) +
@@ -475,7 +529,7 @@ int make_sim(int64_t n, double totmass, double omega2, const ExtSpec& ext, wg_si
   rc = set_force(s, ext);
   if (rc != WG_OK) return fail(rc);
   s->st.n = n;
-  s->st.device_bytes = (int64_t)(total + bk_b);
+  s->st.device_bytes += (int64_t)(total + bk_b);
   *out = s;
   return WG_OK;
 }
@@ -530,6 +584,13 @@ int finish_call(wg_sim* s, int nleap, bool count_sorts = true) {
   unsigned mc = 0;
   for (int i = 1; i <= nleap; ++i) mc = s->h_flags[i].max_cnt > mc ? s->h_flags[i].max_cnt : mc;
   s->st.last_max_count = mc;
+  // predicted splitters for the next kPredCalls calls after a bucket outgrew
+  // one shared-memory pass; counted down by the bucket-path calls that stay
+  // within it (calls on the compact path see no buckets and count nothing)
+  if (s->ptab && mc > (unsigned)kBucketCap)
+    s->pred_calls = kPredCalls;
+  else if (s->pred_calls > 0 && mc > 0)
+    --s->pred_calls;
   if (s->big_list && nleap > 0) {
     // big buckets listed per sub-step (of the launches that ran last for each)
     std::vector<unsigned> bc(2 * (size_t)nleap);
@@ -660,6 +721,7 @@ void fill_dev(wg_sim* s, double dt, double pre) {
   d.lay0 = s->lay;
   d.qsel0 = s->qsel;
   d.cs0 = s->cslot;
+  d.ptab = s->pred_calls > 0 ? s->ptab : nullptr;
 }
 
 StepLaunch step_launch(wg_sim* s, int i, int nleap, int profile) {
@@ -687,6 +749,15 @@ void launch_substep(wg_sim* s, int i, int nleap, int profile) {
   const StepLaunch L = step_launch(s, i, nleap, profile);
   launch_bucket_step(L, s->grid_bucket, s->stream);
   if (s->big_list) launch_bucket_big(L, s->grid_bucket, s->stream);
+  if (s->dev.ptab) {
+    // the samples this sub-step wrote, sorted, become the splitters it
+    // would have published (those of the layout after next)
+    const int q = 1 - ((s->dev.qsel0 + i) & 1);
+    radix_sort_state(s->ptab, s->nb - 1, &s->pradix, s->pflag, s->err, s->stream);
+    launch_samples_to_splitters(s->ptab, s->nb - 1, s->qk[q], s->qi[q], s->stream);
+    s->st.launches += kRadixLaunches + 1;
+    if (!profile) s->st.substeps_predicted += 1;
+  }
 }
 
 void fill_times(wg_sim* s, double dt, int nleap, double* t0) {

@@ -142,6 +142,11 @@ struct StepSmem {
   double amp, inv_h;
   unsigned long long maxv;
   unsigned maxc;  // largest destination count this task saw after its reservations
+  float vsum[WARPS];      // per warp: sum of the new velocities (predicted splitters)
+  unsigned nsamp;         // splitter samples of this task (at most 3: n <= CAP < 3 target)
+  double samp_x[4];
+  int32_t samp_idx[4];
+  uint32_t samp_q[4];
   uint64_t mbar;  // completion of the bucket's bulk copies
   // a big bucket (k_bucket_big): its chunks as ranges of key bins
   int chunk_lo[kMaxChunks + 1];
@@ -712,6 +717,8 @@ __device__ __forceinline__ void process_bucket(const StepLaunch& L, StepSmem& S,
   const double dest_dt = (LAST && !L.profile) ? dt / 2. : 0.0;
   const i128 T = (i128)((((u128)D.T_hi) << 64) | D.T_lo);
   unsigned long long maxv = 0;
+  StateTable* const ptab = D.ptab;  // predicted splitters this sub-step
+
   // the first rank >= rank0 that is a positive multiple of the target
   // starts the next splitter (one per thread at most: ipt <= 8 < target)
   uint32_t qnext = (rank0 + target - 1) / target;
@@ -745,6 +752,14 @@ __device__ __forceinline__ void process_bucket(const StepLaunch& L, StepSmem& S,
       if (r == rnext) {
         qnk[qnext] = key_of(x);
         qni[qnext] = idv[u];
+        if (ptab) {
+          const unsigned k = atomicAdd(&S.nsamp, 1u);
+          if (k < 4u) {
+            S.samp_x[k] = x;
+            S.samp_idx[k] = idv[u];
+            S.samp_q[k] = qnext;
+          }
+        }
       }
       const u128 M = S.u.pos.mfix[j0 + i0 + u];
       const i128 A = T - 2 * (i128)C - (i128)M;
@@ -763,6 +778,7 @@ __device__ __forceinline__ void process_bucket(const StepLaunch& L, StepSmem& S,
       const double xn = fma(dt_drift, vn, x);
       S.x[sidx] = xn;
       S.v[sidx] = vn;
+
       const unsigned long long av =
           (unsigned long long)__double_as_longlong(vn) & 0x7FFFFFFFFFFFFFFFull;
       maxv = av > maxv ? av : maxv;
@@ -816,7 +832,31 @@ __device__ __forceinline__ void process_bucket(const StepLaunch& L, StepSmem& S,
       S.u.pos.drk[pq] = (uint16_t)atomicAdd(&S.dcount[w], 1u);
     }
   }
+  if (ptab) {
+    // the new velocities of this thread's sheets (back from shared memory:
+    // a register held across the force loop would spill)
+    float vsum = 0.f;
+    for (int i = 0; i < nmine; ++i) vsum += (float)S.v[S.perm[j0 + i]];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) vsum += __shfl_xor_sync(0xffffffffu, vsum, o);
+    if (lane == 0) S.vsum[warp] = vsum;
+  }
   __syncthreads();
+  if (ptab && tid < (int)min(S.nsamp, 4u)) {
+    // the sample's position moved on by two drifts at the bucket's mean
+    // velocity: where the bucket is heading.  The mean, not the sample's
+    // own velocity: in a warm region single velocities would scatter the
+    // splitters by more than a bucket, while the mean follows the bulk flow
+    // of a collapsing or breathing slab (single precision is plenty for a
+    // splitter, which only has to be near the quantile)
+    float vs = 0.f;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) vs += S.vsum[w];
+    const StateRef c = ptab->cur;
+    const uint32_t q = S.samp_q[tid];
+    c.x[q - 1] = fma(2.0 * dt, (double)(vs / (float)n), S.samp_x[tid]);
+    c.idx[q - 1] = S.samp_idx[tid];
+  }
   // ---- the sheets grouped by destination bucket of the next layout.  Warp 0
   // prepares the next task meanwhile; the other warps synchronise among
   // themselves (named barrier 1) until the block-wide barrier below.
@@ -1046,6 +1086,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_step(const StepLaunch L) {
       S.cur_wbuf = tm.wbuf;
       S.maxv = 0;
       S.maxc = 0;
+      S.nsamp = 0;
       S.prefix_mass = (((u128)tm.pm_hi) << 64) | tm.pm_lo;
       S.prefix_cnt = tm.pcnt;
       S.amp = tm.amp;
@@ -1194,6 +1235,7 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_big(const StepLaunch L) {
       S.cur_wbuf = 0;
       S.maxv = 0;
       S.maxc = 0;
+      S.nsamp = 0;
       S.prefix_mass = (((u128)bt.pm_hi) << 64) | bt.pm_lo;
       S.prefix_cnt = bt.pcnt;
       S.amp = bt.amp;
@@ -1269,7 +1311,10 @@ __global__ void __launch_bounds__(BT, 2) k_bucket_big(const StepLaunch L) {
       const int blo = S.chunk_lo[ch], bhi = S.chunk_lo[ch + 1];
       for (int j = tid; j < NBIN_PAD; j += BT) S.u.srt.bins[j] = 0u;
       for (int j = tid; j <= S.win_hi - S.win_lo; j += BT) S.dcount[j] = 0;
-      if (tid == 0) S.load_cnt = 0;
+      if (tid == 0) {
+        S.load_cnt = 0;
+        S.nsamp = 0;  // splitter samples of this chunk
+      }
       __syncthreads();
       uint64_t cmin = ~0ull, cmax = 0;
       for (int j = tid; j < n; j += BT) {
@@ -1501,6 +1546,23 @@ void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s) {
   } else {
     k_bucket_step<false, false><<<grid, BT, sizeof(StepSmem), s>>>(a);
   }
+}
+
+__global__ void k_samples_to_splitters(const StateTable* table, int64_t m, uint64_t* qk,
+                                       int32_t* qi) {
+  const StateRef c = table->cur;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += stride) {
+    qk[j + 1] = key_of(c.x[j]);
+    qi[j + 1] = c.idx[j];
+  }
+}
+
+void launch_samples_to_splitters(const StateTable* table, int64_t m, uint64_t* qk, int32_t* qi,
+                                 cudaStream_t s) {
+  int64_t g = (m + 255) / 256;
+  if (g > 1216) g = 1216;
+  k_samples_to_splitters<<<(unsigned)(g < 1 ? 1 : g), 256, 0, s>>>(table, m, qk, qi);
 }
 
 void launch_bucket_big(const StepLaunch& a, int grid, cudaStream_t s) {

@@ -119,6 +119,11 @@ struct SimDev {
   int qsel0;             // splitter array defining the layout the first sub-step writes
   int cs0;               // aggregate slot read by the call's first sub-step
   int pad1;
+  // predicted splitters (or null): the sheet at global rank j * target writes
+  // its position moved on by two drifts at its bucket's mean velocity into
+  // entry j - 1 of this table's current set; the host sorts the set after the
+  // sub-step and takes it as the splitters of the layout after next
+  StateTable* ptab;
 };
 
 struct BucketTask {
@@ -164,6 +169,10 @@ struct StepLaunch {
 void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s);
 // The big buckets k_bucket_step listed (launch right after it, same arguments).
 void launch_bucket_big(const StepLaunch& a, int grid, cudaStream_t s);
+// Splitters 1 .. m of a layout from the m sorted samples in table->cur
+// (predicted splitters): keys of their positions, and their indices.
+void launch_samples_to_splitters(const StateTable* table, int64_t m, uint64_t* qk, int32_t* qi,
+                                 cudaStream_t s);
 // x_out, v_out (and a_out when not null) from the records of rec_out.
 void launch_split_out(const OutRec* rec, int64_t n, double* x_out, double* v_out, double* a_out,
                       cudaStream_t s);

@@ -600,6 +600,7 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
     d.window = s->tune.window;
     d.sort_bits = s->tune.sort_bits;
     d.capg = kBucketCap;  // members have no big buckets
+    d.ptab = nullptr;     // nor predicted splitters
     d.T_lo = s->T_lo;
     d.T_hi = s->T_hi;
     d.E = s->E;
