@@ -1101,6 +1101,9 @@ static int run_call_end(wg_sim* s, double* time_elapsed) {
       break;
     }
     from = resume;
+    // a bucket outgrew its layout: the restarted sub-steps predict their
+    // splitters already (not only the calls after this one)
+    if (s->ptab) s->pred_calls = kPredCalls;
     // fresh look-back epochs for the sub-steps that run again (a redone
     // sub-step published records under its old epoch)
     rc = take_epochs(s, nleap - from);
