@@ -158,3 +158,35 @@ def test_download_during_a_step_returns_the_previous_output():
         assert numpy.array_equal(x, qx) and numpy.array_equal(v, qv)
     p.close()
     q.close()
+
+
+def test_collapsing_members_match_their_solo_runs():
+    # cold top-hats run through their collapse (t = pi/2) in one pool: their
+    # buckets overflow, the pool recovers them and switches them to predicted
+    # splitters; every output must still be the solo run's, bit for bit
+    members = [(20000, 11), (60000, 12), (150000, 13)]
+    dt, nleap, nout = 0.002, 10, 100  # t = 0 .. 2
+    with Pool() as pool:
+        ids = []
+        for n, seed in members:
+            x, v, m = ics.top_hat(n, seed=seed)
+            ids.append(pool.add(x, v, m))
+        t0 = numpy.zeros(len(ids))
+        got = [[] for _ in members]
+        for k in range(nout):
+            pool.step(ids, numpy.full(len(ids), dt), nleap, t0)
+            if k % 10 == 9:
+                for j, sid in enumerate(ids):
+                    got[j].append(pool.download(sid))
+    for j, (n, seed) in enumerate(members):
+        x, v, m = ics.top_hat(n, seed=seed)
+        sim = wendy_gb300.Simulation(x, v, m, numpy.sum(m), -1.)
+        t = ctypes.c_double(0.)
+        for k in range(nout):
+            sim.step(dt, nleap, t)
+            if k % 10 == 9:
+                sx, sv = numpy.empty(n), numpy.empty(n)
+                sim.download(sx, sv)
+                gx, gv = got[j][k // 10]
+                assert numpy.array_equal(gx, sx) and numpy.array_equal(gv, sv), (n, k)
+        sim.close()

@@ -1548,6 +1548,59 @@ void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s) {
   }
 }
 
+__global__ void __launch_bounds__(256) k_member_splitters(const SimDev* devs, const int* list,
+                                                          int sub) {
+  __shared__ uint64_t sk[kMemberSampleCap];
+  __shared__ int32_t si[kMemberSampleCap];
+  const SimDev& d = devs[list ? list[blockIdx.x] : (int)blockIdx.x];
+  StateTable* const pt = d.ptab;
+  if (!pt) return;
+  const int64_t m64 = d.nb - 1;
+  if (m64 < 1 || m64 > kMemberSampleCap) return;
+  const int m = (int)m64;
+  int P = 1;
+  while (P < m) P <<= 1;
+  const StateRef c = pt->cur;
+  for (int j = threadIdx.x; j < P; j += blockDim.x) {
+    sk[j] = j < m ? key_of(c.x[j]) : ~0ull;
+    si[j] = j < m ? c.idx[j] : 0x7fffffff;
+  }
+  __syncthreads();
+  // bitonic sort of (key, idx) pairs, ascending
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const int l = i ^ j;
+        if (l > i) {
+          const bool up = (i & k) == 0;
+          const bool gt = sk[i] > sk[l] || (sk[i] == sk[l] && si[i] > si[l]);
+          if (gt == up) {
+            const uint64_t tk = sk[i];
+            sk[i] = sk[l];
+            sk[l] = tk;
+            const int32_t ti = si[i];
+            si[i] = si[l];
+            si[l] = ti;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const int q = 1 - ((d.qsel0 + sub) & 1);
+  uint64_t* const qk = d.qk[q];
+  int32_t* const qi = d.qi[q];
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    qk[j + 1] = sk[j];
+    qi[j + 1] = si[j];
+  }
+}
+
+void launch_member_splitters(const SimDev* devs, const int* list, int count, int sub,
+                             cudaStream_t s) {
+  if (count > 0) k_member_splitters<<<(unsigned)count, 256, 0, s>>>(devs, list, sub);
+}
+
 __global__ void k_samples_to_splitters(const StateTable* table, int64_t m, uint64_t* qk,
                                        int32_t* qi) {
   const StateRef c = table->cur;
@@ -1556,6 +1609,142 @@ __global__ void k_samples_to_splitters(const StateTable* table, int64_t m, uint6
     qk[j + 1] = key_of(c.x[j]);
     qi[j + 1] = c.idx[j];
   }
+}
+
+// Exclusive scan of each batch member's clamped bucket counts (one block per
+// member): offs[toff + b] = sheets of the member's buckets before b.
+__global__ void k_batch_offsets(const SimDev* devs, const BatchSeg* segs, unsigned* offs) {
+  __shared__ unsigned s_carry;
+  __shared__ unsigned s_w[32];
+  const BatchSeg g = segs[blockIdx.x];
+  const SimDev& d = devs[g.k];
+  const unsigned* cnt = d.bcnt[g.cslot];
+  const int64_t nb = d.nb;
+  const unsigned capg = (unsigned)d.capg;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < nb; base += blockDim.x) {
+    const int64_t b = base + tid;
+    const unsigned c = b < nb ? (cnt[b] < capg ? cnt[b] : capg) : 0u;
+    unsigned incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_w[warp] = incl;
+    __syncthreads();
+    unsigned wpre = 0;
+    for (int w = 0; w < warp; ++w) wpre += s_w[w];
+    if (b < nb) offs[g.toff + b] = s_carry + wpre + incl - c;
+    __syncthreads();
+    if (tid == (int)blockDim.x - 1) s_carry += wpre + incl;
+    __syncthreads();
+  }
+}
+
+// One block per task: bucket b of batch member j into dst, or (b == nb) the
+// member's overflow list after its buckets' sheets.
+__global__ void k_batch_compact(const SimDev* devs, const BatchSeg* segs, const BucketTask* tasks,
+                                StateRef dst, const unsigned* offs, int64_t total) {
+  const BucketTask t = tasks[blockIdx.x];
+  const BatchSeg g = segs[t.sim];
+  const SimDev& d = devs[g.k];
+  const int64_t b = t.bucket;
+  if (b < d.nb) {
+    const unsigned c0 = d.bcnt[g.cslot][b];
+    const unsigned c = c0 < (unsigned)d.capg ? c0 : (unsigned)d.capg;
+    const int64_t o = g.out + offs[g.toff + b];
+    const int64_t base = b * d.capg;
+    const double* x = d.bx[g.lay];
+    const double* v = d.bv[g.lay];
+    const double* m = d.bm[g.lay];
+    const int32_t* idx = d.bi[g.lay];
+    for (unsigned j = threadIdx.x; j < c && o + j < g.out + g.n && o + j < total;
+         j += blockDim.x) {
+      dst.x[o + j] = x[base + j];
+      dst.v[o + j] = v[base + j];
+      dst.m[o + j] = m[base + j];
+      dst.idx[o + j] = idx[base + j];
+    }
+  } else {
+    // the overflow list fills the member's last slots
+    const unsigned no0 = d.ocount[0];
+    const unsigned no = no0 < (unsigned)g.n ? no0 : (unsigned)g.n;
+    const int64_t o = g.out + g.n - no;
+    for (unsigned j = threadIdx.x; j < no && o + j < total; j += blockDim.x) {
+      dst.x[o + j] = d.ox[j];
+      dst.v[o + j] = d.ov[j];
+      dst.m[o + j] = d.om[j];
+      dst.idx[o + j] = d.oi[j];
+    }
+  }
+}
+
+void launch_batch_compact(const SimDev* devs, const BatchSeg* segs, int nseg,
+                          const BucketTask* tasks, int64_t ntasks, StateRef dst, unsigned* offs,
+                          int64_t total, cudaStream_t s) {
+  if (nseg < 1 || ntasks < 1) return;
+  k_batch_offsets<<<(unsigned)nseg, 1024, 0, s>>>(devs, segs, offs);
+  k_batch_compact<<<(unsigned)ntasks, 256, 0, s>>>(devs, segs, tasks, dst, offs, total);
+}
+
+// One block per task: bucket b of batch member j from its sorted sheets into
+// layout 0, its counts and fixed-point masses (slot 0; slots 1 and 2
+// cleared) and splitter b (the first sheet's key and index).
+__global__ void k_batch_bucketize(const SimDev* devs, const BatchSeg* segs,
+                                  const BucketTask* tasks, StateRef src, int64_t total) {
+  __shared__ u128 s_mass[32];
+  const BucketTask t = tasks[blockIdx.x];
+  const BatchSeg g = segs[t.sim];
+  const SimDev& d = devs[g.k];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t b = t.bucket;
+  const int64_t r0 = b * d.target;
+  int c = (int)((g.n - r0) < d.target ? (g.n - r0) : d.target);
+  if (g.out + r0 + c > total) c = (int)(total - g.out - r0 > 0 ? total - g.out - r0 : 0);
+  u128 msum = 0;
+  for (int j = threadIdx.x; j < c; j += blockDim.x) {
+    const int64_t o = b * d.capg + j;
+    const int64_t q = g.out + r0 + j;
+    const double mj = src.m[q];
+    d.bx[0][o] = src.x[q];
+    d.bv[0][o] = src.v[q];
+    d.bm[0][o] = mj;
+    d.bi[0][o] = src.idx[q];
+    msum += mass_to_fixed(mj, d.E);
+  }
+  msum = warp_sum_u128(msum);
+  if (lane == 0) s_mass[warp] = msum;
+  __syncthreads();
+  if (warp == 0) {
+    const u128 tm = warp_sum_u128(lane < (int)(blockDim.x >> 5) ? s_mass[lane] : (u128)0);
+    if (lane < 4) {
+      d.bmass[0][4 * b + lane] = (uint32_t)(tm >> (32 * lane));
+      d.bmass[1][4 * b + lane] = 0ull;
+      d.bmass[2][4 * b + lane] = 0ull;
+    }
+    if (lane == 0) {
+      d.bcnt[0][b] = (unsigned)c;
+      d.bcnt[1][b] = 0u;
+      d.bcnt[2][b] = 0u;
+      if (b > 0) {
+        d.qk[0][b] = key_of(fma(g.pre, src.v[g.out + r0], src.x[g.out + r0]));
+        d.qi[0][b] = src.idx[g.out + r0];
+      } else {
+        d.qk[0][0] = 0ull;
+        d.qi[0][0] = (int32_t)0x80000000;
+        d.qk[0][d.nb] = ~0ull;
+        d.qi[0][d.nb] = 0x7fffffff;
+      }
+    }
+  }
+}
+
+void launch_batch_bucketize(const SimDev* devs, const BatchSeg* segs, const BucketTask* tasks,
+                            int64_t ntasks, StateRef src, int64_t total, cudaStream_t s) {
+  if (ntasks > 0) k_batch_bucketize<<<(unsigned)ntasks, 256, 0, s>>>(devs, segs, tasks, src, total);
 }
 
 void launch_samples_to_splitters(const StateTable* table, int64_t m, uint64_t* qk, int32_t* qi,

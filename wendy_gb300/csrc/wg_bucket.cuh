@@ -17,6 +17,7 @@ constexpr int kBucketCap = 2048;      // sheets a bucket's shared-memory pass ca
 constexpr int kBucketCapBig = 3 * kBucketCap;  // sheets a bucket of a single simulation
                                                // can hold (taken in chunks above kBucketCap)
 constexpr int kSplitterWindow = 64;   // largest splitter window (buckets on each side)
+constexpr int kMemberSampleCap = 4096; // most splitter samples a pool member sorts in one CTA
 constexpr int kSortBitsMin = 9;       // smallest counting-sort offset (bits)
 constexpr int kSortBitsMax = 13;      // largest counting-sort offset (bits)
 constexpr int kMaxTarget = kBucketCap * 3 / 4;  // largest bucket target
@@ -169,6 +170,38 @@ struct StepLaunch {
 void launch_bucket_step(const StepLaunch& a, int grid, cudaStream_t s);
 // The big buckets k_bucket_step listed (launch right after it, same arguments).
 void launch_bucket_big(const StepLaunch& a, int grid, cudaStream_t s);
+// Pool members with predicted splitters (SimDev::ptab set): block k sorts the
+// nb - 1 samples member list[k] (k itself without a list) wrote in sub-step
+// `sub` in shared memory and writes them as the splitters that sub-step
+// published.  Other blocks return.
+void launch_member_splitters(const SimDev* devs, const int* list, int count, int sub,
+                             cudaStream_t s);
+// ---- pool members re-sorted together after bucket overflows ------------
+// One member of such a batch: where its sheets are and where they go.
+struct BatchSeg {
+  int k;          // index of the member in the call's SimDev array
+  int lay;        // layout holding its sheets (plus its overflow list)
+  int cslot;      // aggregate slot holding that layout's counts
+  int pad;
+  int64_t out;    // its first sheet in the batch arrays
+  int64_t n;      // its sheets
+  int64_t toff;   // its first bucket in the per-bucket offsets
+  double pre;     // the half drift its next call opens with, when it overflowed in the
+                  // call's last sub-step (else 0): it is sorted and bucketed by
+                  // x + pre v, as that sub-step would have routed it
+};
+// Every batch member's layout and overflow list -> dst[out, out + n),
+// unsorted.  tasks: (batch index, bucket) for every bucket of every member
+// plus one (batch index, nb) per member for its overflow list; offs: one
+// entry per bucket (toff + b).
+void launch_batch_compact(const SimDev* devs, const BatchSeg* segs, int nseg,
+                          const BucketTask* tasks, int64_t ntasks, StateRef dst, unsigned* offs,
+                          int64_t total, cudaStream_t s);
+// The members' sorted sheets src[out, out + n) -> fresh bucket layouts 0 with
+// exact quantile splitters of x + pre v (tasks: (batch index, bucket) for
+// every bucket).
+void launch_batch_bucketize(const SimDev* devs, const BatchSeg* segs, const BucketTask* tasks,
+                            int64_t ntasks, StateRef src, int64_t total, cudaStream_t s);
 // Splitters 1 .. m of a layout from the m sorted samples in table->cur
 // (predicted splitters): keys of their positions, and their indices.
 void launch_samples_to_splitters(const StateTable* table, int64_t m, uint64_t* qk, int32_t* qi,

@@ -13,6 +13,7 @@
 //
 // Per simulation the arithmetic is that of wendy's approximate step
 // (wendy/wendy.c:385-418); the reference has no ensemble API.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -100,13 +101,24 @@ struct PoolSim {
   bool fresh = false;      // just bucketized: the opening half drift is already applied
   bool out_valid = false;  // x_out / v_out hold the last output
   BucketTuning tune;
+  // predicted splitters (members of at most kMaxMemberSamples + 1 buckets):
+  // the sample set the sub-steps write (a StateTable whose current set holds
+  // x and idx only) and the calls they are still on for
+  StateTable* ptab = nullptr;
+  int pred_calls = 0;
 };
+
+// A member's samples are sorted by one CTA in shared memory.
+constexpr int kPredMemberCalls = 16;
 
 size_t sim_bytes(int64_t n) {
   const BucketTuning t = tuning_for(n);
   const int64_t nb = (n + t.target - 1) / t.target;
   const size_t slots = (size_t)nb * kBucketCap;
-  return 2 * (3 * al(slots * 8) + al(slots * 4)) +
+  const size_t pred = (nb >= 3 && nb - 1 <= kMemberSampleCap)
+                          ? al(sizeof(StateTable)) + al(8 * (size_t)nb) + al(4 * (size_t)nb)
+                          : 0;
+  return pred + 2 * (3 * al(slots * 8) + al(slots * 4)) +
          kAggSlots * (al(4 * (size_t)nb) + al(32 * (size_t)nb)) +
          2 * (al(8 * (size_t)(nb + 1)) + al(4 * (size_t)(nb + 1))) +
          al(sizeof(BucketRec) * (size_t)nb) + 3 * al(8 * (size_t)n) + al(4 * (size_t)n) +
@@ -139,6 +151,21 @@ void carve(PoolSim* s) {
   s->v_out = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
   s->x_out2 = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
   s->v_out2 = reinterpret_cast<double*>(p); p += al(8 * (size_t)s->n);
+  s->ptab = nullptr;
+  if (s->nb >= 3 && s->nb - 1 <= kMemberSampleCap) {
+    s->ptab = reinterpret_cast<StateTable*>(p); p += al(sizeof(StateTable));
+  }
+}
+
+// The sample set of a member with predicted splitters: x and idx of nb - 1
+// samples right after the table (carve leaves the room).
+StateTable member_sample_table(const PoolSim* s) {
+  char* p = reinterpret_cast<char*>(s->ptab) + al(sizeof(StateTable));
+  StateTable t{};
+  t.cur.x = reinterpret_cast<double*>(p);
+  t.cur.idx = reinterpret_cast<int32_t*>(p + al(8 * (size_t)s->nb));
+  t.other = t.cur;
+  return t;
 }
 
 __global__ void k_set_table(StateTable* t, StateRef cur, StateRef other) {
@@ -180,6 +207,26 @@ struct wg_pool {
   StateRef set[2];
   TileRec* trecs = nullptr;
   RadixWork radix;
+  // Batch workspace: members restarted together are compacted into bW, sorted
+  // by (member, key, index) with two radix sorts (sets bA, bB) and gathered
+  // into bO, from which their fresh layouts are filled.
+  void* bws = nullptr;
+  int64_t bws_n = 0, bws_tasks = 0, bws_segs = 0;
+  StateRef bW, bA[2], bB[2], bO;
+  StateTable* btA = nullptr;
+  StateTable* btB = nullptr;
+  StepFlags* bflag = nullptr;
+  RadixWork bradix{};
+  unsigned* boffs = nullptr;
+  BatchSeg* bsegs = nullptr;
+  int64_t* bseg_out = nullptr;
+  BucketTask* btasks = nullptr;
+  // host staging of a chunk's tables: pageable, so each upload has copied
+  // them out before it returns and the next chunk may refill them at once
+  // (a page-locked buffer would be read when the copy runs, after the refill)
+  std::vector<BatchSeg> h_bsegs;
+  std::vector<int64_t> h_bseg_out;
+  std::vector<BucketTask> h_btasks;
   unsigned* offs = nullptr;
   // small per-call arrays (device) and their pinned mirrors
   void* small = nullptr;
@@ -199,6 +246,10 @@ struct wg_pool {
   double* h_t = nullptr;
   unsigned* h_ep = nullptr;
   unsigned* h_oc = nullptr;
+  BucketTask* rtasks = nullptr;    // [cap_tasks] tasks of the simulations restarted together
+  int* rlist = nullptr;            // [cap_sims] their indices in this call
+  BucketTask* h_rtasks = nullptr;
+  int* h_rlist = nullptr;
   BucketTask* h_tasks = nullptr;
   unsigned epoch = 1;
   int64_t launches = 0;
@@ -211,7 +262,6 @@ struct wg_pool {
   int pend_count = 0, pend_nleap = 0;
   std::vector<PoolSim*> pend_act;
   std::vector<double> pend_dt;
-  std::vector<int64_t> pend_task0;
   cudaStream_t dl_stream = nullptr;  // downloads while a step runs
   int64_t g_ntasks = -1;
   void* g_small = nullptr;
@@ -228,6 +278,10 @@ void free_small(wg_pool* p) {
   if (p->h_ep) cudaFreeHost(p->h_ep);
   if (p->h_oc) cudaFreeHost(p->h_oc);
   if (p->h_tasks) cudaFreeHost(p->h_tasks);
+  if (p->h_rtasks) cudaFreeHost(p->h_rtasks);
+  if (p->h_rlist) cudaFreeHost(p->h_rlist);
+  p->h_rtasks = nullptr;
+  p->h_rlist = nullptr;
   p->small = nullptr;
   p->h_dev = nullptr;
   p->h_t = nullptr;
@@ -249,7 +303,8 @@ int ensure_small(wg_pool* p, int nsims, int nleap, int64_t ntasks) {
   const size_t b = al(sizeof(StateTable)) + al(64) + al(sizeof(StepFlags) * (cl + 1)) +
                    2 * al(4 * (size_t)cl) + al(sizeof(SimDev) * (size_t)cs) +
                    al(sizeof(StepFlags) * (size_t)cs * (cl + 1)) + al(8 * (size_t)cs * cl) +
-                   al(8 * (size_t)cs) + al(sizeof(BucketTask) * (size_t)ct);
+                   al(8 * (size_t)cs) + al(sizeof(BucketTask) * (size_t)ct) +
+                   al(sizeof(BucketTask) * (size_t)ct) + al(4 * (size_t)cs);
   PC(cudaMalloc(&p->small, b));
   char* q = static_cast<char*>(p->small);
   p->table = reinterpret_cast<StateTable*>(q); q += al(sizeof(StateTable));
@@ -262,12 +317,16 @@ int ensure_small(wg_pool* p, int nsims, int nleap, int64_t ntasks) {
   p->t_seq = reinterpret_cast<double*>(q); q += al(8 * (size_t)cs * cl);
   p->ocount = reinterpret_cast<unsigned*>(q); q += al(8 * (size_t)cs);
   p->tasks = reinterpret_cast<BucketTask*>(q); q += al(sizeof(BucketTask) * (size_t)ct);
+  p->rtasks = reinterpret_cast<BucketTask*>(q); q += al(sizeof(BucketTask) * (size_t)ct);
+  p->rlist = reinterpret_cast<int*>(q); q += al(4 * (size_t)cs);
   PC(cudaMemsetAsync(p->small, 0, b, p->stream));
   PC(cudaMallocHost(&p->h_dev, sizeof(SimDev) * (size_t)cs));
   PC(cudaMallocHost(&p->h_t, 8 * (size_t)cs * cl));
   PC(cudaMallocHost(&p->h_ep, 4 * (size_t)cl));
   PC(cudaMallocHost(&p->h_oc, 8 * (size_t)cs));
   PC(cudaMallocHost(&p->h_tasks, sizeof(BucketTask) * (size_t)ct));
+  PC(cudaMallocHost(&p->h_rtasks, sizeof(BucketTask) * (size_t)ct));
+  PC(cudaMallocHost(&p->h_rlist, 4 * (size_t)cs));
   p->cap_sims = cs;
   p->cap_leap = cl;
   p->cap_tasks = ct;
@@ -299,6 +358,112 @@ int ensure_workspace(wg_pool* p, int64_t n) {
   PC(cudaMemsetAsync(p->trecs, 0, sizeof(TileRec) * (size_t)tiles, p->stream));
   p->ws_n = n;
   return WG_OK;
+}
+
+// Sheets of one batch of members sorted together: keeps the workspace (about
+// 210 B per sheet) to a few GB.  (The second sort's key, member * 2^32 + rank,
+// stays an exact double for up to 2^21 members.)
+constexpr int64_t kBatchSheets = 1ll << 25;
+
+int ensure_batch(wg_pool* p, int64_t n, int64_t ntasks, int nsegs) {
+  if (n <= p->bws_n && ntasks <= p->bws_tasks && nsegs <= p->bws_segs && p->bws) return WG_OK;
+  PC(cudaStreamSynchronize(p->stream));
+  if (p->bws) cudaFree(p->bws);
+  p->bws = nullptr;
+  p->bws_n = p->bws_tasks = p->bws_segs = 0;
+  n = n > p->bws_n ? n : p->bws_n;
+  const size_t nd = al((size_t)n * 8), ni = al((size_t)n * 4);
+  const size_t set = 3 * nd + ni;
+  const size_t b = 6 * set + radix_bytes(n) + 2 * al(sizeof(StateTable)) + al(sizeof(StepFlags)) +
+                   al(4 * (size_t)ntasks) + al(sizeof(BatchSeg) * (size_t)nsegs) +
+                   al(8 * (size_t)(nsegs + 1)) + al(sizeof(BucketTask) * (size_t)ntasks);
+  PC(cudaMalloc(&p->bws, b));
+  char* q = static_cast<char*>(p->bws);
+  StateRef* sets[6] = {&p->bW, &p->bA[0], &p->bA[1], &p->bB[0], &p->bB[1], &p->bO};
+  for (StateRef* r : sets) {
+    r->x = reinterpret_cast<double*>(q); q += nd;
+    r->v = reinterpret_cast<double*>(q); q += nd;
+    r->m = reinterpret_cast<double*>(q); q += nd;
+    r->idx = reinterpret_cast<int32_t*>(q); q += ni;
+  }
+  radix_bind(&p->bradix, q, n);
+  q += radix_bytes(n);
+  p->btA = reinterpret_cast<StateTable*>(q); q += al(sizeof(StateTable));
+  p->btB = reinterpret_cast<StateTable*>(q); q += al(sizeof(StateTable));
+  p->bflag = reinterpret_cast<StepFlags*>(q); q += al(sizeof(StepFlags));
+  p->boffs = reinterpret_cast<unsigned*>(q); q += al(4 * (size_t)ntasks);
+  p->bsegs = reinterpret_cast<BatchSeg*>(q); q += al(sizeof(BatchSeg) * (size_t)nsegs);
+  p->bseg_out = reinterpret_cast<int64_t*>(q); q += al(8 * (size_t)(nsegs + 1));
+  p->btasks = reinterpret_cast<BucketTask*>(q);
+  p->h_bsegs.resize((size_t)nsegs);
+  p->h_bseg_out.resize((size_t)nsegs + 1);
+  p->h_btasks.resize((size_t)ntasks);
+  StepFlags f{};
+  f.unsorted = 1u;
+  PC(cudaMemcpy(p->bflag, &f, sizeof(f), cudaMemcpyHostToDevice));
+  p->bws_n = n;
+  p->bws_tasks = ntasks;
+  p->bws_segs = nsegs;
+  return WG_OK;
+}
+
+// Copy of the batch for the first sort: keys from x (moved on by the
+// member's pending half drift, if any), ties by original index, and each
+// sheet's place in the batch carried in v (as the bits of a double).
+__global__ void k_seg_prep_a(StateRef w, StateRef a, const BatchSeg* segs, int nseg, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += stride) {
+    int lo = 0, hi = nseg - 1;  // the member whose range holds q
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (segs[mid].out <= q) lo = mid; else hi = mid - 1;
+    }
+    // the key of the position the member's next sub-step will load it at
+    // (the same fma as its load): x, or x + pre v after a last sub-step
+    const double pre = segs[lo].pre;
+    a.x[q] = pre != 0.0 ? fma(pre, w.v[q], w.x[q]) : w.x[q];
+    a.v[q] = __longlong_as_double((long long)q);
+    a.m[q] = 0.0;
+    a.idx[q] = w.idx[q];
+  }
+}
+
+// Second sort's keys: (member, rank in the first sort) as one exact double,
+// so that sorting them groups the members and keeps the first order inside.
+__global__ void k_seg_prep_b(const StateTable* ta, const int64_t* seg_out, int nseg, StateRef b,
+                             int64_t n) {
+  const StateRef a = ta->cur;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += stride) {
+    const int64_t g = (int64_t)__double_as_longlong(a.v[p]);
+    int lo = 0, hi = nseg - 1;  // the member whose range holds g
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (seg_out[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    b.x[p] = (double)(((int64_t)lo << 32) | p);  // < 2^53: exact
+    b.v[p] = 0.0;
+    b.m[p] = 0.0;
+    b.idx[p] = (int32_t)p;
+  }
+}
+
+// The batch in (member, key, index) order: sheet q is the first sort's
+// rank-p sheet, whose place in the compacted batch is g.
+__global__ void k_seg_final(const StateTable* ta, const StateTable* tb, StateRef w, StateRef o,
+                            int64_t n) {
+  const StateRef a = ta->cur, b = tb->cur;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += stride) {
+    const int64_t p = b.idx[q];
+    if (p < 0 || p >= n) continue;  // never, unless a sort gave up (the error word says so)
+    const int64_t g = (int64_t)__double_as_longlong(a.v[p]);
+    if (g < 0 || g >= n) continue;
+    o.x[q] = w.x[g];
+    o.v[q] = w.v[g];
+    o.m[q] = w.m[g];
+    o.idx[q] = w.idx[g];
+  }
 }
 
 int grid_1d(int64_t n) {
@@ -441,6 +606,11 @@ int wg_pool_add(wg_pool* p, int64_t n, const double* x, const double* v, const d
   s->T_lo = (uint64_t)T;
   s->T_hi = (uint64_t)(T >> 64);
   PC(cudaMemsetAsync(s->recs, 0, sizeof(BucketRec) * (size_t)s->nb, p->stream));
+  if (s->ptab) {
+    const StateTable t = member_sample_table(s);
+    PC(cudaMemcpyAsync(s->ptab, &t, sizeof(t), cudaMemcpyHostToDevice, p->stream));
+    PC(cudaStreamSynchronize(p->stream));  // t lives on this stack frame
+  }
   PC(cudaMemcpyAsync(s->ox, x, 8 * (size_t)n, cudaMemcpyHostToDevice, p->stream));
   PC(cudaMemcpyAsync(s->ov, v, 8 * (size_t)n, cudaMemcpyHostToDevice, p->stream));
   PC(cudaMemcpyAsync(s->om, m, 8 * (size_t)n, cudaMemcpyHostToDevice, p->stream));
@@ -564,12 +734,10 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
   } swap_back{act};
   // the kernel's view of every simulation, and the task list
   int64_t t = 0;
-  std::vector<int64_t> task0((size_t)count);  // first task of each simulation
   for (int k = 0; k < count; ++k) {
     PoolSim* s = act[(size_t)k];
     SimDev& d = p->h_dev[k];
     d.rec_out = nullptr;  // members write x_out, v_out directly
-    task0[(size_t)k] = t;
     for (int j = 0; j < 2; ++j) {
       d.bx[j] = s->bx[j];
       d.bv[j] = s->bv[j];
@@ -600,7 +768,7 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
     d.window = s->tune.window;
     d.sort_bits = s->tune.sort_bits;
     d.capg = kBucketCap;  // members have no big buckets
-    d.ptab = nullptr;     // nor predicted splitters
+    d.ptab = s->pred_calls > 0 ? s->ptab : nullptr;
     d.T_lo = s->T_lo;
     d.T_hi = s->T_hi;
     d.E = s->E;
@@ -660,6 +828,10 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
       L.big_ticket = nullptr;
       L.big_cap = 0;
       launch_bucket_step(L, grid, p->stream);
+      // members with predicted splitters: their samples, sorted, become the
+      // splitters this sub-step published (one CTA per member; the others
+      // return at once)
+      launch_member_splitters(p->d_dev, nullptr, count, i, p->stream);
     }
     cudaMemcpyAsync(p->h_oc, p->ocount, 8 * (size_t)count, cudaMemcpyDeviceToHost, p->stream);
     PC(cudaStreamEndCapture(p->stream, &g));
@@ -678,13 +850,12 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
   }
   PC(cudaGraphLaunch(p->gexec, p->stream));
   swap_back.armed = false;
-  p->launches += nleap;
+  p->launches += 2 * nleap;
   p->pend_active = true;
   p->pend_count = count;
   p->pend_nleap = nleap;
   p->pend_act = act;
   p->pend_dt.assign(dt, dt + count);
-  p->pend_task0 = task0;
   return WG_OK;
 }
 
@@ -693,125 +864,196 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
 static int pool_step_end(wg_pool* p, double* time_elapsed) {
   if (!p || !p->pend_active) return pool_fail(WG_ERR_ARG, "no pool step in flight");
   p->pend_active = false;
-  const int count = p->pend_count, nleap = p->pend_nleap, L1 = p->cap_leap;
+  const int count = p->pend_count, nleap = p->pend_nleap;
   const std::vector<PoolSim*>& act = p->pend_act;
   const double* dt = p->pend_dt.data();
-  const std::vector<int64_t>& task0 = p->pend_task0;
   int rc = WG_OK;
   PC(cudaStreamSynchronize(p->stream));
-  // bookkeeping, and recovery of simulations that overflowed a bucket
+  // bookkeeping, and recovery of simulations that overflowed a bucket.  A
+  // sub-step that overflowed a bucket left the sheets complete in the layout
+  // it wrote plus the overflow list: re-sort them, lay out fresh buckets and
+  // restart the remaining sub-steps on the bucket path (a last sub-step has
+  // already written every output).  All simulations that overflowed are
+  // handled together, in rounds: one segmented re-sort of all of them (in
+  // chunks of at most kBatchSheets sheets), then one launch per sub-step over
+  // all of them (each joining from the sub-step it restarts at) and one host
+  // wait.  A simulation restarts past the sub-step that overflowed, so the
+  // rounds end within nleap.
+  std::vector<unsigned> ab((size_t)count);
+  std::vector<int> l0((size_t)count), c0((size_t)count), q0((size_t)count);
   for (int k = 0; k < count; ++k) {
     PoolSim* s = act[(size_t)k];
-    const int lay0 = s->lay, cs0 = s->cslot;
-    s->lay = (lay0 + nleap) & 1;
+    l0[(size_t)k] = s->lay;
+    c0[(size_t)k] = s->cslot;
+    s->lay = (s->lay + nleap) & 1;
     s->qsel = (s->qsel + nleap) & 1;
-    s->cslot = (cs0 + nleap) % kAggSlots;
+    s->cslot = (s->cslot + nleap) % kAggSlots;
     s->mode = 1;
     s->pending_dt = dt[k];
     s->fresh = false;
     s->out_valid = true;
-    // A sub-step that overflowed a bucket left the sheets complete in the
-    // layout it wrote plus the overflow list: re-sort them once, lay out fresh
-    // buckets and restart the remaining sub-steps of this simulation on the
-    // bucket path (a last sub-step has already written every output).
-    unsigned ab = p->h_oc[2 * k + 1];
-    int l0 = lay0, c0 = cs0, restarted_at = -1;
-    while (ab) {
-      const int kk = (int)ab - 1;
-      rc = ensure_workspace(p, s->n);
-      if (rc) return rc;
-      buckets_to_workspace(p, s, (l0 + kk + 1) & 1, (c0 + kk + 1) % kAggSlots,
-                           p->ocount + 2 * k);
-      if (kk == nleap - 1) {
-        store_compact(p, s);
-        s->mode = 0;
-        break;
-      }
-      if (restarted_at >= 0 && kk < restarted_at + 2) {
-        // overflowed again right after a re-sort: finish on the compact path
-        // (full re-sort + fused force kernel per sub-step)
-        ForceArgs f;
-        f.table = p->table;
-        f.n = s->n;
-        f.T_lo = s->T_lo;
-        f.T_hi = s->T_hi;
-        f.E = s->E;
-        f.has_omega = s->omega2 >= 0;
-        f.omega2 = s->omega2;
-        f.ext = s->ext;
-        f.t_seq = p->t_seq + (size_t)k * L1;
-        f.epochs = p->epochs;
-        f.recs = p->trecs;
-        f.err = p->err;
-        f.a_out = nullptr;
-        const int64_t tiles = (s->n + kForceTile - 1) / kForceTile;
-        PC(cudaMemsetAsync(p->tickets, 0, 4 * (size_t)nleap, p->stream));
-        // the tile records are shared by every simulation recovered in this
-        // call, under the same epochs: clear them so that no tile takes
-        // another simulation's prefix
-        PC(cudaMemsetAsync(p->trecs, 0, sizeof(TileRec) * (size_t)tiles, p->stream));
-        for (int i = kk + 1; i < nleap; ++i) {
-          PC(cudaMemsetAsync(&p->wflags[i].unsorted, 1, sizeof(unsigned), p->stream));
-          radix_sort_state(p->table, s->n, &p->radix, &p->wflags[i], p->err, p->stream);
-          f.sub = i;
-          f.dt_kick = dt[k];
-          f.dt_drift = (i == nleap - 1) ? dt[k] / 2. : dt[k];
-          f.ticket = p->tickets + i;
-          f.flag_out = &p->wflags[i + 1];
-          launch_force(f, tiles, p->stream);
-        }
-        launch_desort(p->table, s->n, s->x_out, s->v_out, p->stream);
-        store_compact(p, s);
-        p->launches += (int64_t)(nleap - kk - 1) * (1 + kRadixLaunches) + 2;
-        s->mode = 0;
-        break;
-      }
-      const int from = kk + 1;
-      restarted_at = from;
-      PC(cudaMemsetAsync(&p->wflags[from].unsorted, 1, sizeof(unsigned), p->stream));
-      radix_sort_state(p->table, s->n, &p->radix, &p->wflags[from], p->err, p->stream);
-      launch_bucketize(p->table, s->n, s->tune.target, s->nb, kBucketCap, s->E, s->bx[0], s->bv[0],
-                       s->bm[0], s->bi[0], s->bcnt, s->bmass, s->qk[0], s->qi[0], p->stream);
-      // sub-step `from` reads layout 0, aggregate slot 0 and routes by splitter set 0
-      l0 = from & 1;
-      const int q0 = from & 1;
-      c0 = (kAggSlots - from % kAggSlots) % kAggSlots;
-      SimDev d = p->h_dev[k];
-      d.lay0 = l0;
-      d.qsel0 = q0;
-      d.cs0 = c0;
-      d.pre_dt = 0.0;
-      PC(cudaMemcpyAsync(p->d_dev + k, &d, sizeof(SimDev), cudaMemcpyHostToDevice, p->stream));
-      PC(cudaMemsetAsync(p->ocount + 2 * k, 0, 8, p->stream));
-      // the launches of these sub-steps consumed their tickets
-      PC(cudaMemsetAsync(p->tickets + from, 0, 4 * (size_t)(nleap - from), p->stream));
-      for (int i = from; i < nleap; ++i) {
-        StepLaunch L;
-        L.sims = p->d_dev;
-        L.tasks = p->tasks + task0[(size_t)k];
-        L.ntasks = (int)s->nb;
-        L.sub = i;
-        L.nleap = nleap;
-        L.epochs = p->epochs;
-        L.ticket = p->tickets + i;
-        L.err = p->err;
-        L.profile = 0;
-        L.any_expr = s->ext.kind == EXT_EXPR;
-        L.big_list = nullptr;
-        L.big_count = nullptr;
-        L.big_ticket = nullptr;
-        L.big_cap = 0;
-        launch_bucket_step(L, s->tune.ctas_per_sm * p->sms, p->stream);
-      }
-      p->launches += 3 + kRadixLaunches + (nleap - from);
-      s->lay = (l0 + nleap) & 1;
-      s->qsel = (q0 + nleap) & 1;
-      s->cslot = (c0 + nleap) % kAggSlots;
-      PC(cudaMemcpyAsync(p->h_oc + 2 * k, p->ocount + 2 * k, 8, cudaMemcpyDeviceToHost,
-                         p->stream));
-      PC(cudaStreamSynchronize(p->stream));
-      ab = p->h_oc[2 * k + 1];
+    ab[(size_t)k] = p->h_oc[2 * k + 1];
+    // predicted splitters for the next calls of a member that overflowed;
+    // counted down by the calls that do not
+    if (ab[(size_t)k] && s->ptab)
+      s->pred_calls = kPredMemberCalls;
+    else if (s->pred_calls > 0)
+      --s->pred_calls;
+  }
+  for (;;) {
+    std::vector<std::pair<int, int>> batch;  // (from, k)
+    std::vector<int> lay_w((size_t)count), cs_w((size_t)count);
+    for (int k = 0; k < count; ++k) {
+      if (!ab[(size_t)k]) continue;
+      PoolSim* s = act[(size_t)k];
+      const int kk = (int)ab[(size_t)k] - 1;
+      ab[(size_t)k] = 0;
+      lay_w[(size_t)k] = (l0[(size_t)k] + kk + 1) & 1;
+      cs_w[(size_t)k] = (c0[(size_t)k] + kk + 1) % kAggSlots;
+      // (an overflow in the call's last sub-step, whose outputs are written,
+      // is re-sorted with the others and restarts nothing: from == nleap)
+      batch.emplace_back(kk + 1, k);
     }
+    if (batch.empty()) break;
+    // the restarted members, re-sorted together in chunks of at most
+    // kBatchSheets sheets: compaction of every layout and overflow list, one
+    // sort by (member, key, index) as two radix sorts, fresh layouts
+    for (size_t j0 = 0; j0 < batch.size();) {
+      size_t j1 = j0;
+      int64_t sheets = 0, nbk = 0;
+      while (j1 < batch.size()) {
+        const PoolSim* s = act[(size_t)batch[j1].second];
+        if (j1 > j0 && sheets + s->n > kBatchSheets) break;
+        sheets += s->n;
+        nbk += s->nb;
+        ++j1;
+      }
+      const int nseg = (int)(j1 - j0);
+      rc = ensure_batch(p, sheets, nbk + nseg, nseg);
+      if (rc) return rc;
+      int64_t out = 0, toff = 0, nt = 0;
+      for (int j = 0; j < nseg; ++j) {
+        const int k = batch[j0 + (size_t)j].second;
+        const PoolSim* s = act[(size_t)k];
+        BatchSeg g;
+        g.k = k;
+        g.lay = lay_w[(size_t)k];
+        g.cslot = cs_w[(size_t)k];
+        g.pad = 0;
+        g.out = out;
+        g.n = s->n;
+        g.toff = toff;
+        // after an overflow in the last sub-step the next call opens with a
+        // half drift applied while loading: sort and bucket by where it puts
+        // the sheets (a change of dt re-sorts them then)
+        g.pre = batch[j0 + (size_t)j].first == nleap ? dt[k] / 2. : 0.0;
+        p->h_bsegs[j] = g;
+        p->h_bseg_out[j] = out;
+        for (int64_t bb = 0; bb < s->nb; ++bb) p->h_btasks[nt++] = BucketTask{j, (int)bb};
+        out += s->n;
+        toff += s->nb;
+      }
+      p->h_bseg_out[nseg] = out;
+      for (int j = 0; j < nseg; ++j)  // overflow lists, after every bucket task
+        p->h_btasks[nt++] = BucketTask{j, (int)act[(size_t)batch[j0 + (size_t)j].second]->nb};
+      PC(cudaMemcpyAsync(p->bsegs, p->h_bsegs.data(), sizeof(BatchSeg) * (size_t)nseg,
+                         cudaMemcpyHostToDevice, p->stream));
+      PC(cudaMemcpyAsync(p->bseg_out, p->h_bseg_out.data(), 8 * (size_t)(nseg + 1),
+                         cudaMemcpyHostToDevice, p->stream));
+      PC(cudaMemcpyAsync(p->btasks, p->h_btasks.data(), sizeof(BucketTask) * (size_t)nt,
+                         cudaMemcpyHostToDevice, p->stream));
+      launch_batch_compact(p->d_dev, p->bsegs, nseg, p->btasks, nt, p->bW, p->boffs, sheets,
+                           p->stream);
+      StateTable ta, tb;  // pageable: copied at once
+      ta.cur = p->bA[0];
+      ta.other = p->bA[1];
+      tb.cur = p->bB[0];
+      tb.other = p->bB[1];
+      PC(cudaMemcpyAsync(p->btA, &ta, sizeof(ta), cudaMemcpyHostToDevice, p->stream));
+      PC(cudaMemcpyAsync(p->btB, &tb, sizeof(tb), cudaMemcpyHostToDevice, p->stream));
+      k_seg_prep_a<<<grid_1d(sheets), 256, 0, p->stream>>>(p->bW, p->bA[0], p->bsegs, nseg,
+                                                           sheets);
+      radix_sort_state(p->btA, sheets, &p->bradix, p->bflag, p->err, p->stream);
+      k_seg_prep_b<<<grid_1d(sheets), 256, 0, p->stream>>>(p->btA, p->bseg_out, nseg, p->bB[0],
+                                                           sheets);
+      radix_sort_state(p->btB, sheets, &p->bradix, p->bflag, p->err, p->stream);
+      k_seg_final<<<grid_1d(sheets), 256, 0, p->stream>>>(p->btA, p->btB, p->bW, p->bO, sheets);
+      launch_batch_bucketize(p->d_dev, p->bsegs, p->btasks, nbk, p->bO, sheets, p->stream);
+      p->launches += 8 + 2 * kRadixLaunches;
+      j0 = j1;
+    }
+    // their sub-steps from the restart on: `from` reads layout 0, aggregate
+    // slot 0 and routes by splitter set 0
+    for (const auto& e : batch) {
+      const int from = e.first, k = e.second;
+      PoolSim* s = act[(size_t)k];
+      l0[(size_t)k] = from & 1;
+      q0[(size_t)k] = from & 1;
+      c0[(size_t)k] = (kAggSlots - from % kAggSlots) % kAggSlots;
+      SimDev& d = p->h_dev[k];
+      d.lay0 = l0[(size_t)k];
+      d.qsel0 = q0[(size_t)k];
+      d.cs0 = c0[(size_t)k];
+      d.pre_dt = 0.0;
+      d.ptab = s->ptab;  // the restarted sub-steps predict their splitters
+      s->lay = (l0[(size_t)k] + nleap) & 1;
+      s->qsel = (q0[(size_t)k] + nleap) & 1;
+      s->cslot = (c0[(size_t)k] + nleap) % kAggSlots;
+    }
+    PC(cudaMemcpyAsync(p->d_dev, p->h_dev, sizeof(SimDev) * (size_t)count, cudaMemcpyHostToDevice,
+                       p->stream));
+    PC(cudaMemsetAsync(p->ocount, 0, 8 * (size_t)count, p->stream));
+    if (batch.empty()) break;
+    // the restarted simulations, earliest restart first: the launch of
+    // sub-step i takes the prefix of them that restart at i or before
+    std::sort(batch.begin(), batch.end());
+    int64_t nt = 0;
+    std::vector<int64_t> upto(batch.size());
+    int cps = 1;
+    bool any_expr = false;
+    for (size_t j = 0; j < batch.size(); ++j) {
+      const int k = batch[j].second;
+      PoolSim* s = act[(size_t)k];
+      for (int64_t b = 0; b < s->nb; ++b) p->h_rtasks[nt++] = BucketTask{k, (int)b};
+      upto[j] = nt;
+      p->h_rlist[j] = k;
+      cps = s->tune.ctas_per_sm > cps ? s->tune.ctas_per_sm : cps;
+      any_expr |= s->ext.kind == EXT_EXPR;
+    }
+    PC(cudaMemcpyAsync(p->rtasks, p->h_rtasks, sizeof(BucketTask) * (size_t)nt,
+                       cudaMemcpyHostToDevice, p->stream));
+    PC(cudaMemcpyAsync(p->rlist, p->h_rlist, 4 * batch.size(), cudaMemcpyHostToDevice,
+                       p->stream));
+    const int first = batch.front().first;
+    // the launches of these sub-steps consumed their tickets
+    if (first < nleap)
+      PC(cudaMemsetAsync(p->tickets + first, 0, 4 * (size_t)(nleap - first), p->stream));
+    size_t m = 0;
+    for (int i = first; i < nleap; ++i) {
+      while (m < batch.size() && batch[m].first <= i) ++m;
+      StepLaunch L;
+      L.sims = p->d_dev;
+      L.tasks = p->rtasks;
+      L.ntasks = (int)upto[m - 1];
+      L.sub = i;
+      L.nleap = nleap;
+      L.epochs = p->epochs;
+      L.ticket = p->tickets + i;
+      L.err = p->err;
+      L.profile = 0;
+      L.any_expr = any_expr;
+      L.big_list = nullptr;
+      L.big_count = nullptr;
+      L.big_ticket = nullptr;
+      L.big_cap = 0;
+      launch_bucket_step(L, cps * p->sms, p->stream);
+      launch_member_splitters(p->d_dev, p->rlist, (int)m, i, p->stream);
+      p->launches += 2;
+    }
+    PC(cudaMemcpyAsync(p->h_oc, p->ocount, 8 * (size_t)count, cudaMemcpyDeviceToHost,
+                       p->stream));
+    PC(cudaStreamSynchronize(p->stream));
+    for (const auto& e : batch) ab[(size_t)e.second] = p->h_oc[2 * e.second + 1];
   }
   PC(cudaEventRecord(p->ev1, p->stream));
   unsigned err = 0;
@@ -892,6 +1134,7 @@ int wg_pool_destroy(wg_pool* p) {
     }
   cudaStreamSynchronize(p->stream);
   if (p->ws) cudaFree(p->ws);
+  if (p->bws) cudaFree(p->bws);
   if (p->gexec) cudaGraphExecDestroy(p->gexec);
   free_small(p);
   if (p->ev0) cudaEventDestroy(p->ev0);
