@@ -130,25 +130,16 @@ def run_ensemble(args, w):
     # into page-locked host memory, each step's downloads running while the
     # next step computes (wg_pool_step_begin / wg_pool_step_end)
     from wendy_gb300 import _lib as LL
-    LLL = LL.lib()
-    xall, vall = numpy.empty(total), numpy.empty(total)
-    pinned = [a for a in (xall, vall) if LLL.wg_host_register(a.ctypes.data, a.nbytes) == 0]
-    offs = numpy.cumsum([0] + [mem[k][0] for k in range(len(ids))])
-    xb = {sid: (xall[offs[k]:offs[k + 1]], vall[offs[k]:offs[k + 1]])
-          for k, sid in enumerate(ids)}
+    xall, vall = LL.pinned_empty(total), LL.pinned_empty(total)
     t_start = time.perf_counter()
     k_e2e = max(1, min(args.steps, 3))
     for k in range(k_e2e):
         pool.step_begin(ids, dts, nleap, t0)
         if k:
-            for sid in ids:
-                pool.download(sid, *xb[sid])
+            pool.download_many(ids, xall, vall)
         pool.step_end()
-    for sid in ids:
-        pool.download(sid, *xb[sid])
+    pool.download_many(ids, xall, vall)
     wall = time.perf_counter() - t_start
-    for a in pinned:
-        LLL.wg_host_unregister(a.ctypes.data)
     pool.close()
     e2e_value = total * nleap * k_e2e / wall
     # the plain path: a sample of the same simulations, one at a time
@@ -164,8 +155,7 @@ def run_ensemble(args, w):
         x, v, m = member_inputs(n, fam, seed)
         sim = wendy_gb300.Simulation(x, v, m, numpy.sum(m), omega ** 2)
         tt = ctypes.c_double(0.0)
-        xx, vv = numpy.empty(n), numpy.empty(n)
-        pin = [a for a in (xx, vv) if LLL.wg_host_register(a.ctypes.data, a.nbytes) == 0]
+        xx, vv = LL.pinned_empty(n), LL.pinned_empty(n)
         for _ in range(args.warmup):
             sim.step(dt / nleap, nleap, tt)
         for _ in range(args.steps):
@@ -174,8 +164,6 @@ def run_ensemble(args, w):
             sim.download(xx, vv)
             solo_wall += time.perf_counter() - t1
             solo_ps += n * nleap
-        for a in pin:
-            LLL.wg_host_unregister(a.ctypes.data)
         sim.close()
     solo = solo_ps / solo_dev
     solo_e2e = solo_ps / solo_wall
@@ -604,22 +592,21 @@ def main():
             "stats": {k: st1[k] - st0[k] for k in ("sorts_full", "sorts_window", "substeps",
                                                    "substeps_compact")}}
 
-    # end to end through the reference-shaped call, page-locked host buffers.
-    # Timed before the long full run below: on the measured GB300 hosts the
-    # host-to-device copy rate falls from about 200 GB/s to under 20 GB/s
-    # after tens of seconds of sustained device-memory load (a plain torch
-    # device-to-device copy loop shows the same), and recovers only slowly.
+    # end to end through the reference-shaped call, buffers in page-locked
+    # host memory (wg_host_alloc: on the measured GB300 hosts memory page-locked
+    # by registration falls from about 190 to about 5 GB/s after tens of
+    # seconds of sustained device load, allocated page-locked memory does not)
     e2e = None
     if not args.no_e2e:
         from wendy_gb300 import _lib as LL
-        xi = numpy.zeros(n, dtype=LL.SHEET_DTYPE)
+        xi = LL.pinned_empty(n, LL.SHEET_DTYPE)
         xi["idx"] = numpy.arange(n, dtype=numpy.int32)
         xi["val"] = x
-        xx, vv, a = x.copy(), v.copy(), numpy.zeros(n)
-        mm = m.copy()
-        bufs = [xi, xx, vv, a, mm]
-        for b in bufs:
-            _lib.check(L.wg_host_register(b.ctypes.data, b.nbytes), "wg_host_register")
+        xx, vv, a, mm = (LL.pinned_empty(n) for _ in range(4))
+        xx[:] = x
+        vv[:] = v
+        a[:] = 0.0
+        mm[:] = m
         # outputs counted from t = 0 as above: W untimed, then K timed
         tt = 0.0
         for _ in range(args.warmup):
@@ -634,8 +621,7 @@ def main():
                                                  omega2, ext)
         wall = time.perf_counter() - t_start
         resorted = approx_onestep_stats()["sorts_full"] - sorts0
-        for b in bufs:
-            L.wg_host_unregister(b.ctypes.data)
+        del xi, xx, vv, a, mm
         e2e = {"value": world * n * nleap * k_e2e / wall, "unit": "particle-steps/s",
                "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 40 * n,
                "call": "wg_nbody_approx_onestep", "steps": k_e2e,

@@ -180,9 +180,16 @@ int wg_set_debug_wait(unsigned spin_limit, int64_t withhold_tile);
 
 /* Page-lock (or release) caller memory so that downloads and uploads run
    at full link speed.  No reference counterpart (wendy's buffers are plain
-   numpy arrays). */
+   numpy arrays).  On the measured GB300 hosts a registered range loses most
+   of its copy rate after tens of seconds of sustained device load (about
+   190 -> 5 GB/s) while memory from wg_host_alloc keeps it: prefer that for
+   buffers that live through long runs. */
 int wg_host_register(void *ptr, int64_t bytes);
 int wg_host_unregister(void *ptr);
+/* Page-locked host memory (cudaHostAlloc) and its release; wg_host_free of
+   NULL does nothing.  No reference counterpart. */
+int wg_host_alloc(int64_t bytes, void **ptr);
+int wg_host_free(void *ptr);
 
 /* ---- stateless entry points ------------------------------------------- */
 
@@ -258,9 +265,17 @@ int wg_pool_step(wg_pool *p, int count, const int *ids, const double *dt, int nl
 int wg_pool_step_begin(wg_pool *p, int count, const int *ids, const double *dt, int nleap,
                        double *t0);
 int wg_pool_step_end(wg_pool *p, double *time_elapsed);
+/* (time_elapsed of a pool step: the device time of its launches, and of the
+   recovery of simulations that overflowed a bucket, which runs in
+   wg_pool_step_end -- not the time its stream waits for that call.) */
 /* Positions and velocities of the last step, original order (during a step:
    of the last step completed before it). */
 int wg_pool_download(wg_pool *p, int sim_id, double *x, double *v);
+/* wg_pool_download of `count` simulations ids[] at once, their outputs one
+   after another in x and v (each simulation's sheets in original order):
+   every id is checked before anything is copied, the copies run back to back
+   and the call returns when all have landed. */
+int wg_pool_download_many(wg_pool *p, int count, const int *ids, double *x, double *v);
 int wg_pool_info(wg_pool *p, int64_t *used_bytes, int64_t *budget_bytes, int *n_sims,
                  int64_t *launches);
 int wg_pool_destroy(wg_pool *p);

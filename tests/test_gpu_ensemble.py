@@ -160,6 +160,36 @@ def test_download_during_a_step_returns_the_previous_output():
     q.close()
 
 
+def test_download_many_equals_downloads_one_by_one():
+    # wg_pool_download_many: the members' outputs one after another, in the
+    # order of ids, during a step (the output before it) and after it; a bad
+    # id fails the call before anything is copied
+    members = [ics.sech2_disk(n, seed=s, masses="lognormal") for n, s in ((3000, 1), (20000, 2),
+                                                                          (777, 3))]
+    p = Pool()
+    ids = [p.add(x, v, m, omega=1.1) for x, v, m in members]
+    order = [ids[2], ids[0], ids[1]]
+    p.step(ids, 0.002, 5)
+    for running in (False, True):
+        if running:
+            p.step_begin(ids, 0.002, 5)
+        one = [p.download(sid) for sid in order]
+        total = sum(len(a) for a, _ in one)
+        # into page-locked memory of the library's own (wg_host_alloc)
+        x, v = p.download_many(order, wendy_gb300._lib.pinned_empty(total),
+                               wendy_gb300._lib.pinned_empty(total))
+        assert numpy.array_equal(x, numpy.concatenate([a for a, _ in one]))
+        assert numpy.array_equal(v, numpy.concatenate([b for _, b in one]))
+        xs = numpy.full(len(x), 7.0)
+        bad = numpy.array([ids[0], 99], numpy.int32)
+        assert p._L.wg_pool_download_many(p._h, 2, bad.ctypes.data, xs.ctypes.data,
+                                          xs.ctypes.data) == wendy_gb300._lib.WG_ERR_ARG
+        assert numpy.all(xs == 7.0)
+        if running:
+            p.step_end()
+    p.close()
+
+
 def test_collapsing_members_match_their_solo_runs():
     # cold top-hats run through their collapse (t = pi/2) in one pool: their
     # buckets overflow, the pool recovers them and switches them to predicted

@@ -7,6 +7,7 @@ runtime cannot load it, :func:`lib` raises.
 """
 import ctypes
 import os
+import weakref
 
 import numpy
 from numpy.ctypeslib import ndpointer
@@ -27,8 +28,9 @@ EXT_NONE, EXT_HARMONIC, EXT_PULSE_TANH, EXT_EXPR = 0, 1, 2, 3
 EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", "wg_create",
            "wg_step", "wg_step_begin", "wg_step_end", "wg_download", "wg_energy", "wg_get_stats", "wg_destroy", "wg_accel", "wg_ext_force_eval",
            "wg_nbody_approx_onestep", "wg_nbody_approx_stats", "wg_profile", "wg_host_register", "wg_host_unregister",
+           "wg_host_alloc", "wg_host_free",
            "wg_accel_noalloc", "wg_pool_sim_bytes", "wg_pool_create", "wg_pool_add",
-           "wg_pool_remove", "wg_pool_step", "wg_pool_step_begin", "wg_pool_step_end", "wg_pool_download", "wg_pool_info",
+           "wg_pool_remove", "wg_pool_step", "wg_pool_step_begin", "wg_pool_step_end", "wg_pool_download", "wg_pool_download_many", "wg_pool_info",
            "wg_pool_destroy", "wg_set_tuning", "wg_get_tuning", "wg_set_debug_wait",
            "wg_exact_create", "wg_exact_step", "wg_exact_download", "wg_exact_destroy")
 
@@ -113,6 +115,8 @@ def lib():
                                           ctypes.POINTER(_I), ctypes.POINTER(_D)]
     L.wg_profile.argtypes = [_P, _I, _I, ctypes.POINTER(_D)]
     L.wg_host_register.argtypes = [_P, _I64]
+    L.wg_host_alloc.argtypes = [_I64, ctypes.POINTER(_P)]
+    L.wg_host_free.argtypes = [_P]
     L.wg_host_unregister.argtypes = [_P]
     L.wg_accel_noalloc.argtypes = [_I64, _P, _P, _D, _D, _I, _F64, _I, _D, _P, _P, _P]
     L.wg_set_debug_wait.argtypes = [ctypes.c_uint, _I64]
@@ -130,6 +134,7 @@ def lib():
     L.wg_pool_step_begin.argtypes = [_P, _I, _P, _P, _I, _P]
     L.wg_pool_step_end.argtypes = [_P, ctypes.POINTER(_D)]
     L.wg_pool_download.argtypes = [_P, _I, _P, _P]
+    L.wg_pool_download_many.argtypes = [_P, _I, _P, _P, _P]
     L.wg_pool_info.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                ctypes.POINTER(_I), ctypes.POINTER(_I64)]
     L.wg_pool_destroy.argtypes = [_P]
@@ -150,6 +155,21 @@ def check(status, where):
     if status != WG_OK:
         detail = lib().wg_last_error().decode(errors="replace")
         raise WendyGPUError(status, where, detail)
+
+
+def pinned_empty(shape, dtype=numpy.float64):
+    """An uninitialised numpy array in page-locked host memory (wg_host_alloc),
+    released when the array and every view of it are gone.  Copies to and
+    from it keep the link's rate through long runs, which registered memory
+    (wg_host_register) does not on the measured hosts."""
+    dtype = numpy.dtype(dtype)
+    count = int(numpy.prod(shape, dtype=numpy.int64))
+    nbytes = max(count * dtype.itemsize, 1)
+    ptr = ctypes.c_void_p()
+    check(lib().wg_host_alloc(nbytes, ctypes.byref(ptr)), "wg_host_alloc")
+    raw = (ctypes.c_char * nbytes).from_address(ptr.value)
+    weakref.finalize(raw, lib().wg_host_free, ptr.value)
+    return numpy.frombuffer(raw, dtype=dtype, count=count).reshape(shape)
 
 
 def ext_params(params):

@@ -1432,6 +1432,22 @@ int wg_host_unregister(void* ptr) {
   return WG_OK;
 }
 
+int wg_host_alloc(int64_t bytes, void** ptr) {
+  if (!ptr || bytes <= 0) {
+    set_error("bad arguments to wg_host_alloc");
+    return WG_ERR_ARG;
+  }
+  *ptr = nullptr;
+  WG_CUDA(cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocDefault));
+  return WG_OK;
+}
+
+int wg_host_free(void* ptr) {
+  if (!ptr) return WG_OK;
+  WG_CUDA(cudaFreeHost(ptr));
+  return WG_OK;
+}
+
 int wg_energy(wg_sim* s, double twopiG, double omega2, double* energy, double* momentum) {
   const int rc0 = check_idle(s);
   if (rc0) return rc0;

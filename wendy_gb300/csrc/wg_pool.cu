@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/wendy_gb300.h"
@@ -196,7 +197,9 @@ __global__ void k_store_compact(const StateTable* t, int64_t n, double* x, doubl
 
 struct wg_pool {
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // a step's device time: ev0 -> ev_mid (the graph) plus ev_rec -> ev1 (the
+  // recovery, which waits for the host's second half)
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr, ev_rec = nullptr;
   int sms = 152;
   int64_t budget = 0;  // bytes, 0 = no limit
   int64_t used = 0;
@@ -530,7 +533,8 @@ int wg_pool_create(int64_t budget_bytes, wg_pool** out) {
   cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
   if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&p->dl_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess) {
+      cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess ||
+      cudaEventCreate(&p->ev_mid) != cudaSuccess || cudaEventCreate(&p->ev_rec) != cudaSuccess) {
     delete p;
     return pool_fail(WG_ERR_CUDA, "stream/event creation failed");
   }
@@ -849,6 +853,7 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
     p->graph_builds++;
   }
   PC(cudaGraphLaunch(p->gexec, p->stream));
+  PC(cudaEventRecord(p->ev_mid, p->stream));
   swap_back.armed = false;
   p->launches += 2 * nleap;
   p->pend_active = true;
@@ -900,6 +905,8 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
     else if (s->pred_calls > 0)
       --s->pred_calls;
   }
+  const bool recovery = std::any_of(ab.begin(), ab.end(), [](unsigned a) { return a != 0; });
+  if (recovery) PC(cudaEventRecord(p->ev_rec, p->stream));
   for (;;) {
     std::vector<std::pair<int, int>> batch;  // (from, k)
     std::vector<int> lay_w((size_t)count), cs_w((size_t)count);
@@ -1059,9 +1066,12 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
   unsigned err = 0;
   PC(cudaMemcpyAsync(&err, p->err, 4, cudaMemcpyDeviceToHost, p->stream));
   PC(cudaStreamSynchronize(p->stream));
-  float ms = 0;
-  cudaEventElapsedTime(&ms, p->ev0, p->ev1);
-  if (time_elapsed) *time_elapsed = ms * 1e-3;
+  // the device's time: the graph, plus the recovery (not the wait for the
+  // host between the two halves of the step)
+  float ms = 0, ms_rec = 0;
+  cudaEventElapsedTime(&ms, p->ev0, p->ev_mid);
+  if (recovery) cudaEventElapsedTime(&ms_rec, p->ev_rec, p->ev1);
+  if (time_elapsed) *time_elapsed = (ms + ms_rec) * 1e-3;
   if (err) {
     cudaMemsetAsync(p->err, 0, 4, p->stream);
     return pool_fail(WG_ERR_DEVICE, "device error word 0x%x", err);
@@ -1083,28 +1093,72 @@ int wg_pool_step_begin(wg_pool* p, int count, const int* ids, const double* dt, 
 
 int wg_pool_step_end(wg_pool* p, double* time_elapsed) { return pool_step_end(p, time_elapsed); }
 
-int wg_pool_download(wg_pool* p, int sim_id, double* x, double* v) {
-  if (!p || sim_id < 0 || (size_t)sim_id >= p->sims.size() || !p->sims[(size_t)sim_id])
+// The device output a download of simulation sim_id reads: while a step is
+// running, the output completed before it (the step writes the other pair),
+// or the current one of a simulation it does not advance (stepping: the
+// simulations of the running step, by id); else the last output.
+static int download_source(wg_pool* p, int sim_id,
+                           const std::unordered_set<const PoolSim*>* stepping,
+                           const PoolSim** so, const double** sx, const double** sv) {
+  if (sim_id < 0 || (size_t)sim_id >= p->sims.size() || !p->sims[(size_t)sim_id])
     return pool_fail(WG_ERR_ARG, "no simulation %d in the pool", sim_id);
   PoolSim* s = p->sims[(size_t)sim_id];
+  *so = s;
   if (p->pend_active) {
-    // a step is running: the output completed before it (the step writes the
-    // other pair), or the current one of a simulation it does not advance,
-    // on a stream of its own
-    bool stepping = false;
-    for (PoolSim* a : p->pend_act) stepping |= a == s;
-    const double* sx = stepping ? s->done_x : (s->out_valid ? s->x_out : nullptr);
-    const double* sv = stepping ? s->done_v : (s->out_valid ? s->v_out : nullptr);
-    if (!sx) return pool_fail(WG_ERR_ARG, "simulation %d has no completed output", sim_id);
-    if (x) PC(cudaMemcpyAsync(x, sx, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->dl_stream));
-    if (v) PC(cudaMemcpyAsync(v, sv, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->dl_stream));
-    PC(cudaStreamSynchronize(p->dl_stream));
+    bool step = false;
+    if (stepping) {
+      step = stepping->count(s) != 0;
+    } else {
+      for (PoolSim* a : p->pend_act) step |= a == s;
+    }
+    *sx = step ? s->done_x : (s->out_valid ? s->x_out : nullptr);
+    *sv = step ? s->done_v : (s->out_valid ? s->v_out : nullptr);
+    if (!*sx) return pool_fail(WG_ERR_ARG, "simulation %d has no completed output", sim_id);
     return WG_OK;
   }
   if (!s->out_valid) return pool_fail(WG_ERR_ARG, "simulation %d has not been stepped", sim_id);
-  if (x) PC(cudaMemcpyAsync(x, s->x_out, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->stream));
-  if (v) PC(cudaMemcpyAsync(v, s->v_out, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, p->stream));
-  PC(cudaStreamSynchronize(p->stream));
+  *sx = s->x_out;
+  *sv = s->v_out;
+  return WG_OK;
+}
+
+int wg_pool_download(wg_pool* p, int sim_id, double* x, double* v) {
+  if (!p) return pool_fail(WG_ERR_ARG, "null pool");
+  const PoolSim* s = nullptr;
+  const double *sx = nullptr, *sv = nullptr;
+  const int rc = download_source(p, sim_id, nullptr, &s, &sx, &sv);
+  if (rc) return rc;
+  // during a step on a stream of its own
+  cudaStream_t st = p->pend_active ? p->dl_stream : p->stream;
+  if (x) PC(cudaMemcpyAsync(x, sx, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, st));
+  if (v) PC(cudaMemcpyAsync(v, sv, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, st));
+  PC(cudaStreamSynchronize(st));
+  return WG_OK;
+}
+
+int wg_pool_download_many(wg_pool* p, int count, const int* ids, double* x, double* v) {
+  if (!p || count < 0 || (count > 0 && !ids)) return pool_fail(WG_ERR_ARG, "bad arguments");
+  std::unordered_set<const PoolSim*> stepping;
+  if (p->pend_active) stepping.insert(p->pend_act.begin(), p->pend_act.end());
+  std::vector<const double*> srcx((size_t)count), srcv((size_t)count);
+  std::vector<int64_t> len((size_t)count);
+  for (int k = 0; k < count; ++k) {  // every id checked before any copy
+    const PoolSim* s = nullptr;
+    const int rc = download_source(p, ids[k], p->pend_active ? &stepping : nullptr, &s,
+                                   &srcx[(size_t)k], &srcv[(size_t)k]);
+    if (rc) return rc;
+    len[(size_t)k] = s->n;
+  }
+  // all copies enqueued back to back, one wait
+  cudaStream_t st = p->pend_active ? p->dl_stream : p->stream;
+  int64_t off = 0;
+  for (int k = 0; k < count; ++k) {
+    const size_t bytes = 8 * (size_t)len[(size_t)k];
+    if (x) PC(cudaMemcpyAsync(x + off, srcx[(size_t)k], bytes, cudaMemcpyDeviceToHost, st));
+    if (v) PC(cudaMemcpyAsync(v + off, srcv[(size_t)k], bytes, cudaMemcpyDeviceToHost, st));
+    off += len[(size_t)k];
+  }
+  PC(cudaStreamSynchronize(st));
   return WG_OK;
 }
 
@@ -1139,6 +1193,8 @@ int wg_pool_destroy(wg_pool* p) {
   free_small(p);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
+  if (p->ev_mid) cudaEventDestroy(p->ev_mid);
+  if (p->ev_rec) cudaEventDestroy(p->ev_rec);
   if (p->stream) cudaStreamDestroy(p->stream);
   if (p->dl_stream) {
     cudaStreamSynchronize(p->dl_stream);

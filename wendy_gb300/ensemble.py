@@ -93,6 +93,21 @@ class Pool:
                    "wg_pool_download")
         return x, v
 
+    def download_many(self, ids, x=None, v=None):
+        """``download`` of every simulation in ``ids`` in one call: their
+        outputs one after another in ``x`` and ``v`` (float64, contiguous)."""
+        ids = numpy.ascontiguousarray(ids, dtype=numpy.int32)
+        total = sum(self._n[int(i)] for i in ids)
+        x = numpy.empty(total) if x is None else x
+        v = numpy.empty(total) if v is None else v
+        for a in (x, v):
+            if a.dtype != numpy.float64 or not a.flags.c_contiguous or a.size != total:
+                raise ValueError("x and v must be contiguous float64 arrays of %d entries" % total)
+        _lib.check(self._L.wg_pool_download_many(self._h, len(ids), ids.ctypes.data,
+                                                 x.ctypes.data, v.ctypes.data),
+                   "wg_pool_download_many")
+        return x, v
+
     def info(self):
         used, budget, nsim, launches = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int(), \
             ctypes.c_int64()

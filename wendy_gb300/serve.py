@@ -34,15 +34,11 @@ class _Pinned:
     """Output buffers of one request, page-locked for the stream of downloads."""
 
     def __init__(self, n):
-        self.x = numpy.empty(n)
-        self.v = numpy.empty(n)
-        self._L = _lib.lib()
-        for a in (self.x, self.v):
-            _lib.check(self._L.wg_host_register(a.ctypes.data, a.nbytes), "wg_host_register")
+        self.x = _lib.pinned_empty(n)
+        self.v = _lib.pinned_empty(n)
 
     def release(self):
-        for a in (self.x, self.v):
-            self._L.wg_host_unregister(a.ctypes.data)
+        self.x = self.v = None  # freed with the last view of them
 
 
 @dataclass

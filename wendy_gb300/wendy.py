@@ -235,9 +235,16 @@ def _nbody_approx(x, v, m, dt, nleap, t0=0., omega=None, ext_force=None, sort="c
     sim = Simulation(x, v, m, totmass, omega2, ext_force)
     t = ctypes.c_double(t0)
     dt_leap = dt / nleap
-    L = _lib.lib()
-    pinned = [a for a in (x, v)
-              if a.nbytes >= (1 << 20) and L.wg_host_register(a.ctypes.data, a.nbytes) == 0]
+    if x.nbytes >= (1 << 20):
+        # the yielded copies live in page-locked memory, so that every
+        # output downloads at the link's rate
+        try:
+            xp, vp = _lib.pinned_empty(x.shape), _lib.pinned_empty(v.shape)
+            xp[:] = x
+            vp[:] = v
+            x, v = xp, vp
+        except _lib.WendyGPUError:
+            pass
     try:
         sim.step_begin(dt_leap, nleap, t)
         while True:
@@ -265,8 +272,6 @@ def _nbody_approx(x, v, m, dt, nleap, t0=0., omega=None, ext_force=None, sort="c
     finally:
         # also runs when an unclosed generator is collected at interpreter exit
         try:
-            for a in pinned:
-                L.wg_host_unregister(a.ctypes.data)
             sim.close()
         except Exception:
             pass
