@@ -119,29 +119,28 @@ def run_ensemble(args, w):
     t0 = numpy.zeros(len(ids))
     for _ in range(args.warmup):
         pool.step(ids, dts, nleap, t0)
-    launches0 = pool.info()["launches"]
-    with Clocks(0) as clk:
-        el = 0.0
-        for _ in range(args.steps):
-            el += pool.step(ids, dts, nleap, t0)
-    launches = pool.info()["launches"] - launches0
-    value = total * nleap * args.steps / el
-    # end to end: every output also copied back (x, v of every simulation)
-    # into page-locked host memory, each step's downloads running while the
-    # next step computes (wg_pool_step_begin / wg_pool_step_end)
+    st0 = pool.stats()
+    # the K timed steps, end to end: every output copied back (x, v of every
+    # simulation, wg_pool_download_many) into page-locked host memory while
+    # the next step computes (wg_pool_step_begin / wg_pool_step_end), the last
+    # one after it, wall clock; `value` is the device time of the same steps
     from wendy_gb300 import _lib as LL
     xall, vall = LL.pinned_empty(total), LL.pinned_empty(total)
-    t_start = time.perf_counter()
-    k_e2e = max(1, min(args.steps, 3))
-    for k in range(k_e2e):
-        pool.step_begin(ids, dts, nleap, t0)
-        if k:
-            pool.download_many(ids, xall, vall)
-        pool.step_end()
-    pool.download_many(ids, xall, vall)
-    wall = time.perf_counter() - t_start
+    with Clocks(0) as clk:
+        el = 0.0
+        t_start = time.perf_counter()
+        for k in range(args.steps):
+            pool.step_begin(ids, dts, nleap, t0)
+            if k:
+                pool.download_many(ids, xall, vall)
+            el += pool.step_end()
+        pool.download_many(ids, xall, vall)
+        wall = time.perf_counter() - t_start
+    st = {k: v - st0[k] for k, v in pool.stats().items()}
+    launches = st["launches"]
     pool.close()
-    e2e_value = total * nleap * k_e2e / wall
+    value = total * nleap * args.steps / el
+    e2e_value = total * nleap * args.steps / wall
     # the plain path: a sample of the same simulations, one at a time
     # the plain path on a random sample of the same simulations, one at a
     # time: each simulation's step timed on the device (CUDA events, like the
@@ -177,7 +176,11 @@ def run_ensemble(args, w):
             "e2e": {"value": e2e_value, "unit": "particle-steps/s",
                     "h2d_bytes_per_step": 16 * len(ids), "d2h_bytes_per_step": 16 * total,
                     "overlap": "every member's x, v downloaded every step into page-locked "
-                               "memory while the next step runs; the last step's after it"},
+                               "memory while the next step runs; the last step's after it",
+                    "steps": args.steps},
+            "value_timing": "device time (CUDA events) of the same timed steps",
+            "pool_stats": {k: st[k] for k in ("overflows", "recovery_rounds", "sheets_resorted",
+                                             "substeps_relaunched", "graph_builds")},
             "plain_one_at_a_time": {"value": solo, "unit": "particle-steps/s",
                                     "e2e": solo_e2e, "sample_sims": int(len(sample)),
                                     "steps_per_sim": args.steps,

@@ -276,6 +276,20 @@ int wg_pool_download(wg_pool *p, int sim_id, double *x, double *v);
    every id is checked before anything is copied, the copies run back to back
    and the call returns when all have landed. */
 int wg_pool_download_many(wg_pool *p, int count, const int *ids, double *x, double *v);
+/* Counters of a pool since its creation.  No reference counterpart. */
+typedef struct wg_pool_stats {
+  int64_t steps;              /* pool steps (one per wg_pool_step or step_begin/step_end) */
+  int64_t launches;           /* kernels the pool has launched */
+  int64_t graph_builds;       /* captures of the per-step CUDA graph */
+  int64_t members_sorted;     /* members sorted from scratch (joined, dt changed, compact) */
+  int64_t overflows;          /* member sub-steps that overflowed a bucket */
+  int64_t recovery_rounds;    /* rounds of recovery (segmented re-sort + relaunch) */
+  int64_t sheets_resorted;    /* sheets those rounds re-sorted */
+  int64_t substeps_relaunched; /* member sub-steps run again after a recovery */
+  double graph_seconds;       /* device time of the steps' launches (CUDA events) */
+  double recovery_seconds;    /* device time of their recoveries */
+} wg_pool_stats;
+int wg_pool_get_stats(wg_pool *p, wg_pool_stats *out);
 int wg_pool_info(wg_pool *p, int64_t *used_bytes, int64_t *budget_bytes, int *n_sims,
                  int64_t *launches);
 int wg_pool_destroy(wg_pool *p);

@@ -208,6 +208,12 @@ def test_collapsing_members_match_their_solo_runs():
             if k % 10 == 9:
                 for j, sid in enumerate(ids):
                     got[j].append(pool.download(sid))
+        st = pool.stats()
+    # the collapse overflowed buckets and the pool recovered them
+    assert st["steps"] == nout and st["members_sorted"] == len(members)
+    assert st["overflows"] > 0 and st["recovery_rounds"] > 0
+    assert st["sheets_resorted"] >= st["overflows"] * min(n for n, _ in members)
+    assert 0 < st["substeps_relaunched"] <= st["overflows"] * (nleap - 1)
     for j, (n, seed) in enumerate(members):
         x, v, m = ics.top_hat(n, seed=seed)
         sim = wendy_gb300.Simulation(x, v, m, numpy.sum(m), -1.)

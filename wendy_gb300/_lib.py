@@ -30,7 +30,7 @@ EXPORTS = ("wg_version", "wg_status_string", "wg_last_error", "wg_device_info", 
            "wg_nbody_approx_onestep", "wg_nbody_approx_stats", "wg_profile", "wg_host_register", "wg_host_unregister",
            "wg_host_alloc", "wg_host_free",
            "wg_accel_noalloc", "wg_pool_sim_bytes", "wg_pool_create", "wg_pool_add",
-           "wg_pool_remove", "wg_pool_step", "wg_pool_step_begin", "wg_pool_step_end", "wg_pool_download", "wg_pool_download_many", "wg_pool_info",
+           "wg_pool_remove", "wg_pool_step", "wg_pool_step_begin", "wg_pool_step_end", "wg_pool_download", "wg_pool_download_many", "wg_pool_get_stats", "wg_pool_info",
            "wg_pool_destroy", "wg_set_tuning", "wg_get_tuning", "wg_set_debug_wait",
            "wg_exact_create", "wg_exact_step", "wg_exact_download", "wg_exact_destroy")
 
@@ -55,6 +55,13 @@ class WgStats(ctypes.Structure):
                 ("device_bytes", ctypes.c_int64), ("launches", ctypes.c_int64),
                 ("last_max_count", ctypes.c_int64), ("substeps_compact", ctypes.c_int64),
                 ("big_buckets", ctypes.c_int64), ("substeps_predicted", ctypes.c_int64)]
+
+
+class WgPoolStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_int64) for f in (
+        "steps", "launches", "graph_builds", "members_sorted", "overflows", "recovery_rounds",
+        "sheets_resorted", "substeps_relaunched")] + [
+        ("graph_seconds", ctypes.c_double), ("recovery_seconds", ctypes.c_double)]
 
 
 class WgTuning(ctypes.Structure):
@@ -135,6 +142,7 @@ def lib():
     L.wg_pool_step_end.argtypes = [_P, ctypes.POINTER(_D)]
     L.wg_pool_download.argtypes = [_P, _I, _P, _P]
     L.wg_pool_download_many.argtypes = [_P, _I, _P, _P, _P]
+    L.wg_pool_get_stats.argtypes = [_P, ctypes.POINTER(WgPoolStats)]
     L.wg_pool_info.argtypes = [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                ctypes.POINTER(_I), ctypes.POINTER(_I64)]
     L.wg_pool_destroy.argtypes = [_P]

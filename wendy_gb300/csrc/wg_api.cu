@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <unistd.h>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -822,6 +823,18 @@ void store_sheets(const StateTable* table, int64_t n, wg_sheet* xi, cudaStream_t
 
 }  // namespace
 
+void wg::host_pages_dirty(void* p, size_t bytes) {
+  static const size_t page = [] {
+    const long ps = sysconf(_SC_PAGESIZE);
+    return ps > 0 ? (size_t)ps : (size_t)4096;
+  }();
+  if (!p || !bytes) return;
+  volatile char* c = static_cast<volatile char*>(p);
+  c[0] = 0;
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  for (size_t o = (page - a % page) % page; o < bytes; o += page) c[o] = 0;
+}
+
 extern "C" {
 
 int wg_version(void) { return 100; }
@@ -1243,6 +1256,8 @@ int wg_download(wg_sim* s, double* x, double* v) {
   if (s && s->pend_active && s->done_x) {
     // a split step is running: the output completed before it, on its own stream
     cudaStream_t d = s->dl_stream;
+    if (x) host_pages_dirty(x, 8 * (size_t)s->n);
+    if (v) host_pages_dirty(v, 8 * (size_t)s->n);
     WG_CUDA(cudaStreamWaitEvent(d, s->ev_done, 0));
     if (x) WG_CUDA(cudaMemcpyAsync(x, s->done_x, 8 * s->n, cudaMemcpyDeviceToHost, d));
     if (v) WG_CUDA(cudaMemcpyAsync(v, s->done_v, 8 * s->n, cudaMemcpyDeviceToHost, d));
@@ -1255,6 +1270,8 @@ int wg_download(wg_sim* s, double* x, double* v) {
     launch_desort(s->table, s->n, s->x_out, s->v_out, s->stream);
     s->out_valid = true;
   }
+  if (x) host_pages_dirty(x, 8 * (size_t)s->n);
+  if (v) host_pages_dirty(v, 8 * (size_t)s->n);
   if (x) WG_CUDA(cudaMemcpyAsync(x, s->x_out, 8 * s->n, cudaMemcpyDeviceToHost, s->stream));
   if (v) WG_CUDA(cudaMemcpyAsync(v, s->v_out, 8 * s->n, cudaMemcpyDeviceToHost, s->stream));
   WG_CUDA(cudaStreamSynchronize(s->stream));
@@ -1786,6 +1803,12 @@ int wg_nbody_approx_onestep(int n, wg_sheet* xi, double* x, double* v, const dou
   cudaStream_t down = s->down_stream;
   const wg_sim::OutSet& o = s->outs[out];
   WG_CUDA(cudaStreamWaitEvent(down, s->ev_up, 0));
+  // (the uploads have read x, v and xi before the host writes into them)
+  WG_CUDA(cudaEventSynchronize(s->ev_up));
+  host_pages_dirty(xi, sizeof(wg_sheet) * (size_t)n);
+  host_pages_dirty(x, 8 * (size_t)n);
+  host_pages_dirty(v, 8 * (size_t)n);
+  host_pages_dirty(a, 8 * (size_t)n);
   WG_CUDA(cudaMemcpyAsync(xi, o.xi, sizeof(wg_sheet) * (size_t)n, cudaMemcpyDeviceToHost, down));
   WG_CUDA(cudaMemcpyAsync(x, o.x, 8 * (size_t)n, cudaMemcpyDeviceToHost, down));
   WG_CUDA(cudaMemcpyAsync(v, o.v, 8 * (size_t)n, cudaMemcpyDeviceToHost, down));

@@ -129,6 +129,13 @@ void launch_energy(const StateTable* table, int64_t n, const double* a_sorted, d
 
 // Record a message for wg_last_error() (wg_api.cu).
 void record_last_error(const char* msg);
+// Writes one byte in every memory page of the host range [p, p + bytes),
+// which a device-to-host copy is about to overwrite.  On the measured GB300
+// hosts the copy engine's writes into page-locked pages that the host has not
+// written for some seconds run at a fraction of the link's rate (about 20
+// instead of 145 GB/s for a 9.9 GB download into a buffer written only by
+// copies); a host write to each page first restores the full rate.
+void host_pages_dirty(void* p, size_t bytes);
 
 // --- launchers (wg_radix.cu) ---
 constexpr int kRadixLaunches = 14;  // kernels radix_sort_state enqueues (hist, plan, 8 passes,

@@ -249,6 +249,7 @@ struct wg_pool {
   double* h_t = nullptr;
   unsigned* h_ep = nullptr;
   unsigned* h_oc = nullptr;
+  unsigned* d_oc = nullptr;        // h_oc as the device addresses it (mapped page-locked memory)
   BucketTask* rtasks = nullptr;    // [cap_tasks] tasks of the simulations restarted together
   int* rlist = nullptr;            // [cap_sims] their indices in this call
   BucketTask* h_rtasks = nullptr;
@@ -270,6 +271,7 @@ struct wg_pool {
   void* g_small = nullptr;
   bool g_expr = false;   // the graph launches the expression-force instantiation
   int64_t graph_builds = 0;
+  wg_pool_stats stats{};  // counters (launches and graph_builds are filled on read)
 };
 
 namespace {
@@ -290,6 +292,7 @@ void free_small(wg_pool* p) {
   p->h_t = nullptr;
   p->h_ep = nullptr;
   p->h_oc = nullptr;
+  p->d_oc = nullptr;
   p->h_tasks = nullptr;
 }
 
@@ -327,6 +330,7 @@ int ensure_small(wg_pool* p, int nsims, int nleap, int64_t ntasks) {
   PC(cudaMallocHost(&p->h_t, 8 * (size_t)cs * cl));
   PC(cudaMallocHost(&p->h_ep, 4 * (size_t)cl));
   PC(cudaMallocHost(&p->h_oc, 8 * (size_t)cs));
+  PC(cudaHostGetDevicePointer(reinterpret_cast<void**>(&p->d_oc), p->h_oc, 0));
   PC(cudaMallocHost(&p->h_tasks, sizeof(BucketTask) * (size_t)ct));
   PC(cudaMallocHost(&p->h_rtasks, sizeof(BucketTask) * (size_t)ct));
   PC(cudaMallocHost(&p->h_rlist, 4 * (size_t)cs));
@@ -364,8 +368,8 @@ int ensure_workspace(wg_pool* p, int64_t n) {
 }
 
 // Sheets of one batch of members sorted together: keeps the workspace (about
-// 210 B per sheet) to a few GB.  (The second sort's key, member * 2^32 + rank,
-// stays an exact double for up to 2^21 members.)
+// 210 B per sheet) to a few GB.  (The second sort's key, member and rank in
+// rank_bits + member bits <= 50 bits, stays below the sign and exponent bits.)
 constexpr int64_t kBatchSheets = 1ll << 25;
 
 int ensure_batch(wg_pool* p, int64_t n, int64_t ntasks, int nsegs) {
@@ -431,10 +435,11 @@ __global__ void k_seg_prep_a(StateRef w, StateRef a, const BatchSeg* segs, int n
   }
 }
 
-// Second sort's keys: (member, rank in the first sort) as one exact double,
-// so that sorting them groups the members and keeps the first order inside.
+// Second sort's keys: (member, rank in the first sort) packed into the bits
+// of one double, so that sorting them groups the members and keeps the first
+// order inside.
 __global__ void k_seg_prep_b(const StateTable* ta, const int64_t* seg_out, int nseg, StateRef b,
-                             int64_t n) {
+                             int64_t n, int rank_bits) {
   const StateRef a = ta->cur;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += stride) {
@@ -444,7 +449,10 @@ __global__ void k_seg_prep_b(const StateTable* ta, const int64_t* seg_out, int n
       const int mid = (lo + hi + 1) >> 1;
       if (seg_out[mid] <= g) lo = mid; else hi = mid - 1;
     }
-    b.x[p] = (double)(((int64_t)lo << 32) | p);  // < 2^53: exact
+    // the key as raw bits (a non-negative double whose order is that of its
+    // bits): member above rank, so that the sort's passes over the bytes
+    // above both are skipped as constant
+    b.x[p] = __longlong_as_double(((long long)lo << rank_bits) | p);
     b.v[p] = 0.0;
     b.m[p] = 0.0;
     b.idx[p] = (int32_t)p;
@@ -467,6 +475,11 @@ __global__ void k_seg_final(const StateTable* ta, const StateTable* tb, StateRef
     o.m[q] = w.m[g];
     o.idx[q] = w.idx[g];
   }
+}
+
+// n words device -> mapped host memory.
+__global__ void k_read_back(const unsigned* src, unsigned* dst, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
 }
 
 int grid_1d(int64_t n) {
@@ -710,6 +723,7 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
     if (s->mode == 0) {
       PC(cudaMemsetAsync(&p->wflags[0], 0, sizeof(StepFlags), p->stream));
       rc = to_buckets(p, s, dt[k]);
+      ++p->stats.members_sorted;
       if (rc) return rc;
       s->fresh = true;
     }
@@ -837,7 +851,10 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
       // return at once)
       launch_member_splitters(p->d_dev, nullptr, count, i, p->stream);
     }
-    cudaMemcpyAsync(p->h_oc, p->ocount, 8 * (size_t)count, cudaMemcpyDeviceToHost, p->stream);
+    // the overflow counts to the host by a kernel's stores into mapped
+    // page-locked memory, not a copy: a copy would queue on the copy engine
+    // behind downloads running meanwhile, and the step would end with them
+    k_read_back<<<1, 256, 0, p->stream>>>(p->ocount, p->d_oc, 2 * count);
     PC(cudaStreamEndCapture(p->stream, &g));
     const cudaError_t ie = cudaGraphInstantiate(&p->gexec, g, 0);
     cudaGraphDestroy(g);
@@ -854,8 +871,9 @@ static int pool_step_begin(wg_pool* p, int count, const int* ids, const double* 
   }
   PC(cudaGraphLaunch(p->gexec, p->stream));
   PC(cudaEventRecord(p->ev_mid, p->stream));
+  ++p->stats.steps;
   swap_back.armed = false;
-  p->launches += 2 * nleap;
+  p->launches += 2 * nleap + 1;
   p->pend_active = true;
   p->pend_count = count;
   p->pend_nleap = nleap;
@@ -922,6 +940,12 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
       batch.emplace_back(kk + 1, k);
     }
     if (batch.empty()) break;
+    ++p->stats.recovery_rounds;
+    p->stats.overflows += (int64_t)batch.size();
+    for (const auto& e : batch) {
+      p->stats.sheets_resorted += act[(size_t)e.second]->n;
+      p->stats.substeps_relaunched += nleap - e.first;
+    }
     // the restarted members, re-sorted together in chunks of at most
     // kBatchSheets sheets: compaction of every layout and overflow list, one
     // sort by (member, key, index) as two radix sorts, fresh layouts
@@ -981,8 +1005,10 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
       k_seg_prep_a<<<grid_1d(sheets), 256, 0, p->stream>>>(p->bW, p->bA[0], p->bsegs, nseg,
                                                            sheets);
       radix_sort_state(p->btA, sheets, &p->bradix, p->bflag, p->err, p->stream);
+      int rank_bits = 1;  // bits of a rank in the batch; with the member's, at most 2 x 31
+      while ((int64_t)1 << rank_bits < sheets) ++rank_bits;
       k_seg_prep_b<<<grid_1d(sheets), 256, 0, p->stream>>>(p->btA, p->bseg_out, nseg, p->bB[0],
-                                                           sheets);
+                                                           sheets, rank_bits);
       radix_sort_state(p->btB, sheets, &p->bradix, p->bflag, p->err, p->stream);
       k_seg_final<<<grid_1d(sheets), 256, 0, p->stream>>>(p->btA, p->btB, p->bW, p->bO, sheets);
       launch_batch_bucketize(p->d_dev, p->bsegs, p->btasks, nbk, p->bO, sheets, p->stream);
@@ -1057,8 +1083,9 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
       launch_member_splitters(p->d_dev, p->rlist, (int)m, i, p->stream);
       p->launches += 2;
     }
-    PC(cudaMemcpyAsync(p->h_oc, p->ocount, 8 * (size_t)count, cudaMemcpyDeviceToHost,
-                       p->stream));
+    k_read_back<<<1, 256, 0, p->stream>>>(p->ocount, p->d_oc, 2 * count);
+    PC(cudaGetLastError());
+    p->launches += 1;
     PC(cudaStreamSynchronize(p->stream));
     for (const auto& e : batch) ab[(size_t)e.second] = p->h_oc[2 * e.second + 1];
   }
@@ -1072,6 +1099,8 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
   cudaEventElapsedTime(&ms, p->ev0, p->ev_mid);
   if (recovery) cudaEventElapsedTime(&ms_rec, p->ev_rec, p->ev1);
   if (time_elapsed) *time_elapsed = (ms + ms_rec) * 1e-3;
+  p->stats.graph_seconds += ms * 1e-3;
+  p->stats.recovery_seconds += ms_rec * 1e-3;
   if (err) {
     cudaMemsetAsync(p->err, 0, 4, p->stream);
     return pool_fail(WG_ERR_DEVICE, "device error word 0x%x", err);
@@ -1130,6 +1159,8 @@ int wg_pool_download(wg_pool* p, int sim_id, double* x, double* v) {
   if (rc) return rc;
   // during a step on a stream of its own
   cudaStream_t st = p->pend_active ? p->dl_stream : p->stream;
+  if (x) host_pages_dirty(x, 8 * (size_t)s->n);
+  if (v) host_pages_dirty(v, 8 * (size_t)s->n);
   if (x) PC(cudaMemcpyAsync(x, sx, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, st));
   if (v) PC(cudaMemcpyAsync(v, sv, 8 * (size_t)s->n, cudaMemcpyDeviceToHost, st));
   PC(cudaStreamSynchronize(st));
@@ -1154,11 +1185,21 @@ int wg_pool_download_many(wg_pool* p, int count, const int* ids, double* x, doub
   int64_t off = 0;
   for (int k = 0; k < count; ++k) {
     const size_t bytes = 8 * (size_t)len[(size_t)k];
+    if (x) host_pages_dirty(x + off, bytes);
+    if (v) host_pages_dirty(v + off, bytes);
     if (x) PC(cudaMemcpyAsync(x + off, srcx[(size_t)k], bytes, cudaMemcpyDeviceToHost, st));
     if (v) PC(cudaMemcpyAsync(v + off, srcv[(size_t)k], bytes, cudaMemcpyDeviceToHost, st));
     off += len[(size_t)k];
   }
   PC(cudaStreamSynchronize(st));
+  return WG_OK;
+}
+
+int wg_pool_get_stats(wg_pool* p, wg_pool_stats* out) {
+  if (!p || !out) return pool_fail(WG_ERR_ARG, "null pool or output");
+  *out = p->stats;
+  out->launches = p->launches;
+  out->graph_builds = p->graph_builds;
   return WG_OK;
 }
 

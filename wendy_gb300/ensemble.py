@@ -108,6 +108,12 @@ class Pool:
                    "wg_pool_download_many")
         return x, v
 
+    def stats(self):
+        """The pool's counters (wg_pool_get_stats) as a dict."""
+        st = _lib.WgPoolStats()
+        _lib.check(self._L.wg_pool_get_stats(self._h, ctypes.byref(st)), "wg_pool_get_stats")
+        return {name: getattr(st, name) for name, _ in st._fields_}
+
     def info(self):
         used, budget, nsim, launches = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int(), \
             ctypes.c_int64()
