@@ -182,8 +182,11 @@ int wg_set_debug_wait(unsigned spin_limit, int64_t withhold_tile);
    at full link speed.  No reference counterpart (wendy's buffers are plain
    numpy arrays).  On the measured GB300 hosts a registered range loses most
    of its copy rate after tens of seconds of sustained device load (about
-   190 -> 5 GB/s) while memory from wg_host_alloc keeps it: prefer that for
-   buffers that live through long runs. */
+   190 -> 5 GB/s for downloads into it); memory from wg_host_alloc kept its
+   rate in the same test.  Every download entry of this library also writes
+   one byte per page of its destination before the copy: a page-locked
+   buffer that only copies write falls to about 20 GB/s within a minute of
+   repeated downloads, and a host write per page restores the full rate. */
 int wg_host_register(void *ptr, int64_t bytes);
 int wg_host_unregister(void *ptr);
 /* Page-locked host memory (cudaHostAlloc) and its release; wg_host_free of

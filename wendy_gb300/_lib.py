@@ -167,9 +167,10 @@ def check(status, where):
 
 def pinned_empty(shape, dtype=numpy.float64):
     """An uninitialised numpy array in page-locked host memory (wg_host_alloc),
-    released when the array and every view of it are gone.  Copies to and
-    from it keep the link's rate through long runs, which registered memory
-    (wg_host_register) does not on the measured hosts."""
+    released when the array and every view of it are gone.  On the measured
+    hosts, memory page-locked by registration (wg_host_register) loses most
+    of its copy rate after tens of seconds of device load; this memory kept
+    it in the same test."""
     dtype = numpy.dtype(dtype)
     count = int(numpy.prod(shape, dtype=numpy.int64))
     nbytes = max(count * dtype.itemsize, 1)
