@@ -226,3 +226,36 @@ def test_collapsing_members_match_their_solo_runs():
                 gx, gv = got[j][k // 10]
                 assert numpy.array_equal(gx, sx) and numpy.array_equal(gv, sv), (n, k)
         sim.close()
+
+
+def test_a_large_collapsing_member_matches_its_solo_run():
+    # a collapsing member of 2^20 sheets and a smaller one, re-sorted together
+    # after their overflows: both bit for bit
+    members = [(1 << 20, 21), (30000, 22)]
+    dt, nleap, nout = 0.002, 10, 100  # t = 0 .. 2, through the collapse
+    with Pool() as pool:
+        ids = []
+        for n, seed in members:
+            x, v, m = ics.top_hat(n, seed=seed)
+            ids.append(pool.add(x, v, m))
+        t0 = numpy.zeros(len(ids))
+        got = [[] for _ in members]
+        for k in range(nout):
+            pool.step(ids, numpy.full(len(ids), dt), nleap, t0)
+            if k % 20 == 19:
+                for j, sid in enumerate(ids):
+                    got[j].append(pool.download(sid))
+        st = pool.stats()
+    assert st["overflows"] > 0 and st["recovery_rounds"] > 0
+    for j, (n, seed) in enumerate(members):
+        x, v, m = ics.top_hat(n, seed=seed)
+        sim = wendy_gb300.Simulation(x, v, m, numpy.sum(m), -1.)
+        t = ctypes.c_double(0.)
+        for k in range(nout):
+            sim.step(dt, nleap, t)
+            if k % 20 == 19:
+                sx, sv = numpy.empty(n), numpy.empty(n)
+                sim.download(sx, sv)
+                gx, gv = got[j][k // 20]
+                assert numpy.array_equal(gx, sx) and numpy.array_equal(gv, sv), (n, k)
+        sim.close()

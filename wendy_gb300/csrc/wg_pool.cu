@@ -340,8 +340,16 @@ int ensure_small(wg_pool* p, int nsims, int nleap, int64_t ntasks) {
   return WG_OK;
 }
 
+// Smallest power of two >= v (v >= 1).
+static int64_t pow2_at_least(int64_t v) {
+  int64_t r = 1;
+  while (r < v) r <<= 1;
+  return r;
+}
+
 int ensure_workspace(wg_pool* p, int64_t n) {
   if (n <= p->ws_n && p->ws) return WG_OK;
+  n = pow2_at_least(n);  // fewer re-allocations (each waits for the device)
   PC(cudaStreamSynchronize(p->stream));
   if (p->ws) cudaFree(p->ws);
   p->ws = nullptr;
@@ -374,11 +382,15 @@ constexpr int64_t kBatchSheets = 1ll << 25;
 
 int ensure_batch(wg_pool* p, int64_t n, int64_t ntasks, int nsegs) {
   if (n <= p->bws_n && ntasks <= p->bws_tasks && nsegs <= p->bws_segs && p->bws) return WG_OK;
+  // grown, never shrunk, in powers of two: batches of changing shape reuse it
+  // (a re-allocation waits for the device)
+  n = pow2_at_least(std::max<int64_t>(n, p->bws_n));
+  ntasks = pow2_at_least(std::max<int64_t>(ntasks, p->bws_tasks));
+  nsegs = (int)pow2_at_least(std::max<int64_t>(nsegs, p->bws_segs));
   PC(cudaStreamSynchronize(p->stream));
   if (p->bws) cudaFree(p->bws);
   p->bws = nullptr;
   p->bws_n = p->bws_tasks = p->bws_segs = 0;
-  n = n > p->bws_n ? n : p->bws_n;
   const size_t nd = al((size_t)n * 8), ni = al((size_t)n * 4);
   const size_t set = 3 * nd + ni;
   const size_t b = 6 * set + radix_bytes(n) + 2 * al(sizeof(StateTable)) + al(sizeof(StepFlags)) +
@@ -463,10 +475,12 @@ __global__ void k_seg_prep_b(const StateTable* ta, const int64_t* seg_out, int n
 // rank-p sheet, whose place in the compacted batch is g.
 __global__ void k_seg_final(const StateTable* ta, const StateTable* tb, StateRef w, StateRef o,
                             int64_t n) {
-  const StateRef a = ta->cur, b = tb->cur;
+  // tb null: a batch of one member, already in order after the first sort
+  const StateRef a = ta->cur;
+  const int32_t* bidx = tb ? tb->cur.idx : nullptr;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += stride) {
-    const int64_t p = b.idx[q];
+    const int64_t p = bidx ? (int64_t)bidx[q] : q;
     if (p < 0 || p >= n) continue;  // never, unless a sort gave up (the error word says so)
     const int64_t g = (int64_t)__double_as_longlong(a.v[p]);
     if (g < 0 || g >= n) continue;
@@ -949,6 +963,9 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
     // the restarted members, re-sorted together in chunks of at most
     // kBatchSheets sheets: compaction of every layout and overflow list, one
     // sort by (member, key, index) as two radix sorts, fresh layouts
+    // (a chunk of one member needs no grouping sort; sorting large members
+    // alone that way measured slower than batching them, so members are
+    // batched in their order and a chunk holds one only when it is that large)
     for (size_t j0 = 0; j0 < batch.size();) {
       size_t j1 = j0;
       int64_t sheets = 0, nbk = 0;
@@ -1005,14 +1022,18 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
       k_seg_prep_a<<<grid_1d(sheets), 256, 0, p->stream>>>(p->bW, p->bA[0], p->bsegs, nseg,
                                                            sheets);
       radix_sort_state(p->btA, sheets, &p->bradix, p->bflag, p->err, p->stream);
-      int rank_bits = 1;  // bits of a rank in the batch; with the member's, at most 2 x 31
-      while ((int64_t)1 << rank_bits < sheets) ++rank_bits;
-      k_seg_prep_b<<<grid_1d(sheets), 256, 0, p->stream>>>(p->btA, p->bseg_out, nseg, p->bB[0],
-                                                           sheets, rank_bits);
-      radix_sort_state(p->btB, sheets, &p->bradix, p->bflag, p->err, p->stream);
-      k_seg_final<<<grid_1d(sheets), 256, 0, p->stream>>>(p->btA, p->btB, p->bW, p->bO, sheets);
+      if (nseg > 1) {
+        int rank_bits = 1;  // bits of a rank in the batch; with the member's, at most 2 x 31
+        while ((int64_t)1 << rank_bits < sheets) ++rank_bits;
+        k_seg_prep_b<<<grid_1d(sheets), 256, 0, p->stream>>>(p->btA, p->bseg_out, nseg,
+                                                             p->bB[0], sheets, rank_bits);
+        radix_sort_state(p->btB, sheets, &p->bradix, p->bflag, p->err, p->stream);
+        p->launches += 1 + kRadixLaunches;
+      }
+      k_seg_final<<<grid_1d(sheets), 256, 0, p->stream>>>(p->btA, nseg > 1 ? p->btB : nullptr,
+                                                          p->bW, p->bO, sheets);
       launch_batch_bucketize(p->d_dev, p->bsegs, p->btasks, nbk, p->bO, sheets, p->stream);
-      p->launches += 8 + 2 * kRadixLaunches;
+      p->launches += 7 + kRadixLaunches;
       j0 = j1;
     }
     // their sub-steps from the restart on: `from` reads layout 0, aggregate
