@@ -127,3 +127,34 @@ def test_shipped_tuning_table_is_valid():
     for r in rows:
         assert 64 <= r["target"] <= 1536 and 1 <= r["window"] <= 64
         assert 9 <= r["sort_bits"] <= 13 and r["ctas_per_sm"] in (1, 2)
+
+
+def header_struct(name):
+    """(type, field) pairs of `typedef struct name { ... } name;` in the header."""
+    text = open(HEADER).read()
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), text, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    return re.findall(r"(int64_t|int|double)\s+(\w+)\s*;", body)
+
+
+@pytest.mark.parametrize("name,mirror", [("wg_stats", _lib.WgStats),
+                                         ("wg_pool_stats", _lib.WgPoolStats),
+                                         ("wg_tuning", _lib.WgTuning)])
+def test_ctypes_structs_mirror_the_header(name, mirror):
+    # the Python mirrors of the ABI's structs: same fields, order and types
+    import ctypes
+    ctype = {"int64_t": ctypes.c_int64, "int": ctypes.c_int, "double": ctypes.c_double}
+    fields = header_struct(name)
+    assert [f for _, f in fields] == [f for f, _ in mirror._fields_]
+    assert [ctype[t] for t, _ in fields] == [t for _, t in mirror._fields_]
+
+
+def test_pinned_arrays_fail_loudly_without_a_device():
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("CUDA library not built here")
+    import ctypes
+    sm = ctypes.c_int(0)
+    if _lib.lib().wg_device_info(ctypes.byref(sm), None, None) == 0:
+        pytest.skip("a device is present")
+    with pytest.raises(_lib.WendyGPUError):
+        _lib.pinned_empty(16)
