@@ -211,10 +211,14 @@ def run_serve(args, w):
     with Clocks(0) as clk:
         served = srv.run([Request(**r) for r in reqs])
     rounds, waits, peak = srv.rounds, srv.budget_waits, srv.peak_bytes
+    pool_stats = srv.pool.stats()
     srv.close()
-    with Clocks(0) as clk_plain:
-        plain = serve_one_at_a_time([Request(**r) for r in reqs])
-    a, b = latency_stats(served), latency_stats(plain)
+    b, clk_plain = None, None
+    if not args.skip_plain:
+        with Clocks(0) as clk_plain:
+            plain = serve_one_at_a_time([Request(**r) for r in reqs])
+        b = latency_stats(plain)
+    a = latency_stats(served)
     line = {"metric": "served p50/p99 latency and particle-steps/s", "value": a["p99_s"],
             "unit": "s (p99 latency)", "n_gpus": 1, "steps": nreq, "warmup": 0,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -226,8 +230,11 @@ def run_serve(args, w):
                        "rounds_with_a_request_waiting_for_memory": waits,
                        "peak_admitted_bytes": peak},
             "continuous_batching": a, "plain_one_at_a_time": b,
-            "throughput_ratio": a["particle_steps_per_s"] / b["particle_steps_per_s"],
-            "clocks": clk.summary(), "clocks_plain": clk_plain.summary()}
+            "throughput_ratio": a["particle_steps_per_s"] / b["particle_steps_per_s"] if b else None,
+            "pool_stats": {k: pool_stats[k] for k in (
+                "overflows", "recovery_rounds", "sheets_resorted", "members_compact",
+                "graph_seconds", "recovery_seconds")},
+            "clocks": clk.summary(), "clocks_plain": clk_plain.summary() if clk_plain else None}
     print(json.dumps(line))
 
 HBM_FALLBACK_GBS = 6800.0
@@ -486,6 +493,8 @@ def main():
                     help="ensemble_4096: simulations of the plain one-at-a-time comparison")
     ap.add_argument("--requests", type=int, default=0,
                     help="serve_poisson: requests in the stream (default 1000)")
+    ap.add_argument("--skip-plain", action="store_true",
+                    help="serve_poisson: continuous batching only (no one-at-a-time arm)")
     ap.add_argument("--budget-gb", type=float, default=0.0,
                     help="serve_poisson: HBM budget in GB (default: the configuration's 150)")
     args = ap.parse_args()

@@ -291,6 +291,10 @@ typedef struct wg_pool_stats {
   int64_t substeps_relaunched; /* member sub-steps run again after a recovery */
   double graph_seconds;       /* device time of the steps' launches (CUDA events) */
   double recovery_seconds;    /* device time of their recoveries */
+  int64_t members_compact;    /* members (of 2^20 sheets or more) that finished a step on the
+                                 compact path, having overflowed again within two sub-steps
+                                 of a re-sort */
+  int64_t substeps_compact;   /* sub-steps they ran there (full re-sort + force kernel) */
 } wg_pool_stats;
 int wg_pool_get_stats(wg_pool *p, wg_pool_stats *out);
 int wg_pool_info(wg_pool *p, int64_t *used_bytes, int64_t *budget_bytes, int *n_sims,

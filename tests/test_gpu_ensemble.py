@@ -210,7 +210,9 @@ def test_collapsing_members_match_their_solo_runs():
                     got[j].append(pool.download(sid))
         st = pool.stats()
     # the collapse overflowed buckets and the pool recovered them
+    # (members below 2^20 sheets never finish on the compact path)
     assert st["steps"] == nout and st["members_sorted"] == len(members)
+    assert st["members_compact"] == 0 and st["substeps_compact"] == 0
     assert st["overflows"] > 0 and st["recovery_rounds"] > 0
     assert st["sheets_resorted"] >= st["overflows"] * min(n for n, _ in members)
     assert 0 < st["substeps_relaunched"] <= st["overflows"] * (nleap - 1)

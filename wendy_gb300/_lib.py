@@ -61,7 +61,8 @@ class WgPoolStats(ctypes.Structure):
     _fields_ = [(f, ctypes.c_int64) for f in (
         "steps", "launches", "graph_builds", "members_sorted", "overflows", "recovery_rounds",
         "sheets_resorted", "substeps_relaunched")] + [
-        ("graph_seconds", ctypes.c_double), ("recovery_seconds", ctypes.c_double)]
+        ("graph_seconds", ctypes.c_double), ("recovery_seconds", ctypes.c_double),
+        ("members_compact", ctypes.c_int64), ("substeps_compact", ctypes.c_int64)]
 
 
 class WgTuning(ctypes.Structure):

@@ -539,6 +539,58 @@ void store_compact(wg_pool* p, PoolSim* s) {
   p->launches += 1;
 }
 
+// Members of at least this many sheets that overflow again within two
+// sub-steps of a re-sort finish the call on the compact path (below, one
+// member at a time: for smaller members its launches cost more than the
+// batched re-sorts it saves).
+constexpr int64_t kCompactFinishSheets = 1ll << 20;
+
+// Member k of the call overflowed in sub-step kk again right after a re-sort:
+// it finishes the call on the compact path -- its layout `lay` (counts in
+// aggregate slot `cslot`) and overflow list compacted into the workspace, then
+// per remaining sub-step a full radix sort and the fused force kernel, the
+// outputs de-sorted, the state stored compact (the next call re-sorts it).
+int finish_compact(wg_pool* p, PoolSim* s, int k, int kk, int lay, int cslot, double dt,
+                   int nleap) {
+  int rc = ensure_workspace(p, s->n);
+  if (rc) return rc;
+  buckets_to_workspace(p, s, lay, cslot, p->ocount + 2 * k);
+  ForceArgs f{};
+  f.table = p->table;
+  f.n = s->n;
+  f.T_lo = s->T_lo;
+  f.T_hi = s->T_hi;
+  f.E = s->E;
+  f.has_omega = s->omega2 >= 0;
+  f.omega2 = s->omega2;
+  f.ext = s->ext;
+  f.t_seq = p->t_seq + (size_t)k * p->cap_leap;
+  f.epochs = p->epochs;
+  f.recs = p->trecs;
+  f.err = p->err;
+  f.a_out = nullptr;
+  const int64_t tiles = (s->n + kForceTile - 1) / kForceTile;
+  PC(cudaMemsetAsync(p->tickets, 0, 4 * (size_t)nleap, p->stream));
+  // the tile records are shared by every member finished this way: cleared,
+  // so that no tile takes another member's prefix
+  PC(cudaMemsetAsync(p->trecs, 0, sizeof(TileRec) * (size_t)tiles, p->stream));
+  for (int i = kk + 1; i < nleap; ++i) {
+    PC(cudaMemsetAsync(&p->wflags[i].unsorted, 1, sizeof(unsigned), p->stream));
+    radix_sort_state(p->table, s->n, &p->radix, &p->wflags[i], p->err, p->stream);
+    f.sub = i;
+    f.dt_kick = dt;
+    f.dt_drift = (i == nleap - 1) ? dt / 2. : dt;
+    f.ticket = p->tickets + i;
+    f.flag_out = &p->wflags[i + 1];
+    launch_force(f, tiles, p->stream);
+  }
+  launch_desort(p->table, s->n, s->x_out, s->v_out, p->stream);
+  store_compact(p, s);
+  p->launches += (int64_t)(nleap - kk - 1) * (1 + kRadixLaunches) + 1;
+  s->mode = 0;
+  return WG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -939,27 +991,45 @@ static int pool_step_end(wg_pool* p, double* time_elapsed) {
   }
   const bool recovery = std::any_of(ab.begin(), ab.end(), [](unsigned a) { return a != 0; });
   if (recovery) PC(cudaEventRecord(p->ev_rec, p->stream));
+  std::vector<int> restarted((size_t)count, -1);  // sub-step a member last restarted at
   for (;;) {
-    std::vector<std::pair<int, int>> batch;  // (from, k)
+    std::vector<std::pair<int, int>> batch;   // (from, k)
+    std::vector<std::pair<int, int>> finish;  // (kk, k): overflowed again right after a re-sort
     std::vector<int> lay_w((size_t)count), cs_w((size_t)count);
     for (int k = 0; k < count; ++k) {
       if (!ab[(size_t)k]) continue;
-      PoolSim* s = act[(size_t)k];
       const int kk = (int)ab[(size_t)k] - 1;
       ab[(size_t)k] = 0;
       lay_w[(size_t)k] = (l0[(size_t)k] + kk + 1) & 1;
       cs_w[(size_t)k] = (c0[(size_t)k] + kk + 1) % kAggSlots;
-      // (an overflow in the call's last sub-step, whose outputs are written,
-      // is re-sorted with the others and restarts nothing: from == nleap)
-      batch.emplace_back(kk + 1, k);
+      // a large member that overflows again within two sub-steps of its
+      // restart would keep overflowing: it finishes the call on the compact
+      // path.  (An overflow in the call's last sub-step, whose outputs are
+      // written, is re-sorted with the others and restarts nothing: from ==
+      // nleap.)
+      const int r = restarted[(size_t)k];
+      if (r >= 0 && kk < r + 2 && kk < nleap - 1 && act[(size_t)k]->n >= kCompactFinishSheets)
+        finish.emplace_back(kk, k);
+      else
+        batch.emplace_back(kk + 1, k);
     }
-    if (batch.empty()) break;
+    if (batch.empty() && finish.empty()) break;
     ++p->stats.recovery_rounds;
-    p->stats.overflows += (int64_t)batch.size();
+    p->stats.overflows += (int64_t)(batch.size() + finish.size());
     for (const auto& e : batch) {
       p->stats.sheets_resorted += act[(size_t)e.second]->n;
       p->stats.substeps_relaunched += nleap - e.first;
+      restarted[(size_t)e.second] = e.first;
     }
+    for (const auto& e : finish) {
+      const int kk = e.first, k = e.second;
+      rc = finish_compact(p, act[(size_t)k], k, kk, lay_w[(size_t)k], cs_w[(size_t)k], dt[k],
+                          nleap);
+      if (rc) return rc;
+      ++p->stats.members_compact;
+      p->stats.substeps_compact += nleap - kk - 1;
+    }
+    if (batch.empty()) break;
     // the restarted members, re-sorted together in chunks of at most
     // kBatchSheets sheets: compaction of every layout and overflow list, one
     // sort by (member, key, index) as two radix sorts, fresh layouts
